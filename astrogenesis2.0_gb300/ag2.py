@@ -1,0 +1,241 @@
+"""Python binding of the C-ABI in include/ag2.h (ctypes over lib/libag2.so).
+
+This is the host-side view the tests and bench.py use.  It mirrors the
+reference's call sequence: ``Context.build_tree`` is ``Tree::buildTree``
+(simulation/src/Physics/Tree/Tree.cpp:24-55), ``sph_density`` is
+``Tree::calcGasDensity`` (:119-150), ``forces`` is ``Tree::calculateForces``
+(:57-83), ``kick``/``drift``/``ueuler`` are ``TimeIntegration::Kick/Drift/Ueuler``
+(simulation/src/Physics/TimeIntegration.cpp:10-40).  There is no CPU fallback:
+without the compiled library (or a GPU) every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libag2.so")
+
+OK = 0
+E_INVALID, E_CUDA, E_NOMEM, E_COINCIDENT, E_DEPTH, E_STACK, E_NAN, E_CAPACITY = range(-1, -9, -1)
+PREC_FP64, PREC_FP32 = 0, 1
+FIELDS = {"pos": 0, "vel": 1, "acc": 2, "mass": 3, "h": 4, "rho": 5, "P": 6, "T": 7, "U": 8, "dUdt": 9,
+          "vdens": 10}
+VECTOR_FIELDS = {"pos", "vel", "acc"}
+
+# every exported symbol of include/ag2.h
+EXPORTS = [
+    "ag2_default_params", "ag2_create", "ag2_destroy", "ag2_set_params", "ag2_get_params", "ag2_set_stream",
+    "ag2_last_error_string", "ag2_upload", "ag2_upload_device", "ag2_set_field", "ag2_download", "ag2_count",
+    "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
+    "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
+    "ag2_topology", "ag2_interactions", "ag2_launch_count",
+]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("G", ctypes.c_double), ("e0", ctypes.c_double), ("theta", ctypes.c_double),
+                ("massInH", ctypes.c_double), ("split_threshold", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("group_size", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class AG2Error(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ag2 error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libag2.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run __graft_entry__.build() first")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    D = ctypes.c_double
+    I = ctypes.c_int
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.ag2_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.ag2_default_params.restype = None
+    L.ag2_create.argtypes = [ctypes.POINTER(P), ctypes.POINTER(Params), ctypes.c_size_t]
+    L.ag2_destroy.argtypes = [P]
+    L.ag2_set_params.argtypes = [P, ctypes.POINTER(Params)]
+    L.ag2_get_params.argtypes = [P, ctypes.POINTER(Params)]
+    L.ag2_set_stream.argtypes = [P, P]
+    L.ag2_last_error_string.argtypes = [P]
+    L.ag2_last_error_string.restype = ctypes.c_char_p
+    L.ag2_upload.argtypes = [P, ctypes.c_size_t, P, P, P, P, P]
+    L.ag2_upload_device.argtypes = [P, ctypes.c_size_t, P, P, P, P, P]
+    L.ag2_set_field.argtypes = [P, I, P, I]
+    L.ag2_download.argtypes = [P, I, P, I]
+    L.ag2_count.argtypes = [P]
+    L.ag2_count.restype = ctypes.c_size_t
+    for f in ("ag2_build_tree", "ag2_sph_density", "ag2_forces"):
+        getattr(L, f).argtypes = [P]
+    for f in ("ag2_visual_density", "ag2_kick", "ag2_drift", "ag2_kick_drift", "ag2_ueuler",
+              "ag2_scale_positions"):
+        getattr(L, f).argtypes = [P, D]
+    L.ag2_step.argtypes = [P, D, D, I, D]
+    L.ag2_root_radius.argtypes = [P, dp]
+    L.ag2_node_count.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                 ctypes.POINTER(ctypes.c_int32)]
+    L.ag2_topology.argtypes = [P] * 12
+    L.ag2_interactions.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.ag2_launch_count.argtypes = [P]
+    L.ag2_launch_count.restype = ctypes.c_int64
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """One simulation's device state (particles in HBM, tree, walk arrays)."""
+
+    def __init__(self, capacity: int, *, G: float = 1.0, e0: float = 0.01, theta: float = 0.5,
+                 massInH: float = 0.0, split_threshold: int = 100, precision: str = "fp32"):
+        self.L = load()
+        p = Params()
+        self.L.ag2_default_params(ctypes.byref(p))
+        p.G, p.e0, p.theta, p.massInH = G, e0, theta, massInH
+        p.split_threshold = split_threshold
+        p.precision = PREC_FP32 if precision == "fp32" else PREC_FP64
+        self.params = p
+        h = ctypes.c_void_p()
+        rc = self.L.ag2_create(ctypes.byref(h), ctypes.byref(p), int(capacity))
+        if rc != OK:
+            raise AG2Error(rc, "ag2_create failed")
+        self.h = h
+        self.n = 0
+
+    # -- helpers ------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != OK:
+            msg = self.L.ag2_last_error_string(self.h)
+            raise AG2Error(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.ag2_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, **kw):
+        for k, v in kw.items():
+            if k == "precision":
+                v = PREC_FP32 if v == "fp32" else PREC_FP64
+            setattr(self.params, k, v)
+        self._check(self.L.ag2_set_params(self.h, ctypes.byref(self.params)))
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.L.ag2_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
+
+    # -- particles ----------------------------------------------------------
+    def upload(self, pos, mass, type_, vel=None, U=None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        mass = np.ascontiguousarray(mass, dtype=np.float64).reshape(n)
+        type_ = np.ascontiguousarray(type_, dtype=np.uint8).reshape(n)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(n, 3)
+        U = None if U is None else np.ascontiguousarray(U, dtype=np.float64).reshape(n)
+        self._keep = (pos, mass, type_, vel, U)
+        self._check(self.L.ag2_upload(self.h, n, _ptr(pos), _ptr(vel), _ptr(mass), _ptr(U), _ptr(type_)))
+        self.n = n
+
+    def upload_device(self, n: int, pos_ptr: int, mass_ptr: int, type_ptr: int, vel_ptr: int = 0, U_ptr: int = 0):
+        """Upload from device buffers (e.g. torch tensor data_ptr()s)."""
+        v = ctypes.c_void_p
+        self._check(self.L.ag2_upload_device(self.h, n, v(pos_ptr), v(vel_ptr or None), v(mass_ptr),
+                                             v(U_ptr or None), v(type_ptr)))
+        self.n = n
+
+    def download(self, field: str) -> np.ndarray:
+        f = FIELDS[field]
+        shape = (self.n, 3) if field in VECTOR_FIELDS else (self.n,)
+        out = np.empty(shape, dtype=np.float64)
+        self._check(self.L.ag2_download(self.h, f, _ptr(out), 0))
+        return out
+
+    def download_device(self, field: str, dst_ptr: int):
+        self._check(self.L.ag2_download(self.h, FIELDS[field], ctypes.c_void_p(dst_ptr), 1))
+
+    def set_field(self, field: str, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self.L.ag2_set_field(self.h, FIELDS[field], _ptr(a), 0))
+
+    # -- hot path -----------------------------------------------------------
+    def build_tree(self):
+        self._check(self.L.ag2_build_tree(self.h))
+
+    def visual_density(self, radius: float):
+        self._check(self.L.ag2_visual_density(self.h, radius))
+
+    def sph_density(self):
+        self._check(self.L.ag2_sph_density(self.h))
+
+    def forces(self):
+        self._check(self.L.ag2_forces(self.h))
+
+    def kick(self, dt):
+        self._check(self.L.ag2_kick(self.h, dt))
+
+    def drift(self, dt):
+        self._check(self.L.ag2_drift(self.h, dt))
+
+    def kick_drift(self, dt):
+        self._check(self.L.ag2_kick_drift(self.h, dt))
+
+    def ueuler(self, dt):
+        self._check(self.L.ag2_ueuler(self.h, dt))
+
+    def scale_positions(self, f):
+        self._check(self.L.ag2_scale_positions(self.h, f))
+
+    def step(self, dt, hubble_factor=1.0, visual_density=False, visual_radius=0.0):
+        self._check(self.L.ag2_step(self.h, dt, hubble_factor, 1 if visual_density else 0, visual_radius))
+
+    # -- introspection --------------------------------------------------------
+    def root_radius(self) -> float:
+        r = ctypes.c_double()
+        self._check(self.L.ag2_root_radius(self.h, ctypes.byref(r)))
+        return r.value
+
+    def node_count(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        self._check(self.L.ag2_node_count(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def interactions(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.L.ag2_interactions(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def launches(self) -> int:
+        return int(self.L.ag2_launch_count(self.h))
+
+    def topology(self) -> dict:
+        nn, _, _ = self.node_count()
+        t = {
+            "depth": np.empty(nn, np.int32), "is_leaf": np.empty(nn, np.int32), "particle": np.empty(nn, np.int32),
+            "cp_count": np.empty(nn, np.int64), "cp_hash": np.empty(nn, np.uint64), "mass": np.empty(nn),
+            "com": np.empty((nn, 3)), "gas_mass": np.empty(nn), "mvel": np.empty((nn, 3)),
+            "center": np.empty((nn, 3)), "radius": np.empty(nn),
+        }
+        order = ["depth", "is_leaf", "particle", "cp_count", "cp_hash", "mass", "com", "gas_mass", "mvel", "center",
+                 "radius"]
+        self._check(self.L.ag2_topology(self.h, *[_ptr(t[k]) for k in order]))
+        return t

@@ -1,0 +1,520 @@
+// ag2_api.cu -- the C-ABI of include/ag2.h: context, particle upload and
+// download in the caller's order, the step driver and tree introspection.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ag2_internal.cuh"
+
+namespace ag2 {
+
+int run_close_step(Ctx *c, double dt, double f);
+
+int set_err(Ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_check(Ctx *c, cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return set_err(c, e == cudaErrorMemoryAllocation ? AG2_E_NOMEM : AG2_E_CUDA, m);
+}
+
+int sync_ctl(Ctx *c)
+{
+    AG2_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(Ctx::Ctl), cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    return AG2_OK;
+}
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__global__ void k_unpack(int n, const double *pos, const double *vel, const double *mass, const double *U,
+                         const uint8_t *type, Particles s, Ctx::Ctl *ctl)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicExch(&ctl->err_code, (int)AG2_E_NAN);
+    s.px[i] = x;
+    s.py[i] = y;
+    s.pz[i] = z;
+    s.vx[i] = vel ? vel[3 * i] : 0.0;
+    s.vy[i] = vel ? vel[3 * i + 1] : 0.0;
+    s.vz[i] = vel ? vel[3 * i + 2] : 0.0;
+    s.ax[i] = s.ay[i] = s.az[i] = 0.0;
+    s.m[i] = mass[i];
+    s.U[i] = U ? U[i] : 0.0;
+    s.dUdt[i] = 0.0;
+    s.h[i] = s.rho[i] = s.P[i] = s.T[i] = s.vdens[i] = 0.0;
+    s.type[i] = type[i];
+    s.id[i] = i;
+}
+
+__device__ double *field1(Particles &s, int f)
+{
+    switch (f) {
+    case AG2_MASS: return s.m;
+    case AG2_H: return s.h;
+    case AG2_RHO: return s.rho;
+    case AG2_P: return s.P;
+    case AG2_T: return s.T;
+    case AG2_U: return s.U;
+    case AG2_DUDT: return s.dUdt;
+    case AG2_VDENS: return s.vdens;
+    }
+    return nullptr;
+}
+
+__device__ void field3(Particles &s, int f, double *&x, double *&y, double *&z)
+{
+    if (f == AG2_POS) { x = s.px; y = s.py; z = s.pz; }
+    else if (f == AG2_VEL) { x = s.vx; y = s.vy; z = s.vz; }
+    else { x = s.ax; y = s.ay; z = s.az; }
+}
+
+// tree order -> caller order
+__global__ void k_gather_out(int n, Particles s, int f, double *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int o = s.id[i];
+    if (f <= AG2_ACC) {
+        double *x, *y, *z;
+        field3(s, f, x, y, z);
+        out[3 * o] = x[i];
+        out[3 * o + 1] = y[i];
+        out[3 * o + 2] = z[i];
+    } else {
+        out[o] = field1(s, f)[i];
+    }
+}
+
+// caller order -> tree order
+__global__ void k_scatter_in(int n, Particles s, int f, const double *in)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int o = s.id[i];
+    if (f <= AG2_ACC) {
+        double *x, *y, *z;
+        field3(s, f, x, y, z);
+        x[i] = in[3 * o];
+        y[i] = in[3 * o + 1];
+        z[i] = in[3 * o + 2];
+    } else {
+        field1(s, f)[i] = in[o];
+    }
+}
+
+int alloc_particles(Ctx *c, Particles &p, size_t cap)
+{
+    double **d[] = {&p.px, &p.py, &p.pz, &p.vx, &p.vy, &p.vz, &p.ax, &p.ay, &p.az, &p.m,
+                    &p.U,  &p.dUdt, &p.h, &p.rho, &p.P, &p.T, &p.vdens};
+    for (double **q : d)
+        if (cudaMalloc(q, cap * sizeof(double)) != cudaSuccess)
+            return set_err(c, AG2_E_NOMEM, "particle allocation failed");
+    if (cudaMalloc(&p.type, cap) != cudaSuccess || cudaMalloc(&p.id, cap * sizeof(int32_t)) != cudaSuccess)
+        return set_err(c, AG2_E_NOMEM, "particle allocation failed");
+    return AG2_OK;
+}
+
+void free_particles(Particles &p)
+{
+    double *d[] = {p.px, p.py, p.pz, p.vx, p.vy, p.vz, p.ax, p.ay, p.az, p.m, p.U, p.dUdt, p.h, p.rho, p.P, p.T,
+                   p.vdens};
+    for (double *q : d) cudaFree(q);
+    cudaFree(p.type);
+    cudaFree(p.id);
+    p = Particles{};
+}
+
+void free_nodes(Nodes &d)
+{
+    void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs, d.childmask,
+                  d.cx,    d.cy,    d.cz,    d.bkey,  d.mass,   d.comx,    d.comy, d.comz, d.gas,   d.mvx,
+                  d.mvy,   d.mvz,   d.ngas,  d.tm,    d.tmx,    d.tmy,     d.tmz,  d.tg,   d.tgvx,  d.tgvy,
+                  d.tgvz,  d.tng,   d.wA,    d.wB,    d.wD,     d.flag,    d.rho};
+    for (void *q : ps) cudaFree(q);
+    d = Nodes{};
+}
+
+bool valid_params(const ag2_params *p)
+{
+    return p && p->split_threshold >= 1 && (p->precision == AG2_PREC_FP64 || p->precision == AG2_PREC_FP32) &&
+           p->theta > 0.0;
+}
+
+int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const double *mass, const double *U,
+                  const uint8_t *type)
+{
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    c->cur = 0;
+    AG2_LAUNCH(c, k_unpack, grid_for(n, kBlock), kBlock, 0, (int)n, pos, vel, mass, U, type, c->S(), c->ctl);
+    c->n = n;
+    c->have_tree = false;
+    int rc = sync_ctl(c);
+    if (rc) return rc;
+    if (c->ctl_host->err_code == AG2_E_NAN) return set_err(c, AG2_E_NAN, "non-finite particle position");
+    return AG2_OK;
+}
+
+}  // namespace
+}  // namespace ag2
+
+using namespace ag2;
+
+struct ag2_ctx : public ag2::Ctx {};
+
+extern "C" {
+
+void ag2_default_params(ag2_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->G = 1.0;
+    p->e0 = 0.01;
+    p->theta = 0.5;
+    p->massInH = 0.0;
+    p->split_threshold = 100;
+    p->precision = AG2_PREC_FP32;
+    p->group_size = 32;
+}
+
+int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
+{
+    if (!out) return AG2_E_INVALID;
+    *out = nullptr;
+    if (!valid_params(params) || capacity > (size_t)INT32_MAX / 4) return AG2_E_INVALID;
+    ag2_ctx *c = new (std::nothrow) ag2_ctx();
+    if (!c) return AG2_E_NOMEM;
+    c->prm = *params;
+    cudaGetDevice(&c->device);
+    size_t cap = std::max(capacity, (size_t)1);
+    c->cap = cap;
+    int rc = AG2_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        rc = cuda_check(c, e, "cudaStreamCreate");
+        delete c;
+        return rc;
+    }
+    c->stream = c->own_stream;
+    bool ok = alloc_particles(c, c->st[0], cap) == AG2_OK && alloc_particles(c, c->st[1], cap) == AG2_OK;
+    ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->digit, cap) == cudaSuccess &&
+         cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&
+         cudaMalloc(&c->width_part, 2 * 1024 * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&c->ctl, sizeof(Ctx::Ctl)) == cudaSuccess &&
+         cudaMallocHost(&c->ctl_host, sizeof(Ctx::Ctl)) == cudaSuccess;
+    if (ok) ok = ensure_node_capacity(c, 4 * cap + 1024) == AG2_OK;
+    if (!ok) {
+        ag2_destroy(c);
+        return AG2_E_NOMEM;
+    }
+    cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream);
+    std::memset(c->ctl_host, 0, sizeof(Ctx::Ctl));
+    cudaStreamSynchronize(c->stream);
+    *out = c;
+    return AG2_OK;
+}
+
+int ag2_destroy(ag2_ctx *c)
+{
+    if (!c) return AG2_E_INVALID;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_particles(c->st[0]);
+    free_particles(c->st[1]);
+    free_nodes(c->nd);
+    void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->finalnode, c->nodelist, c->digit,
+                  c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8, c->width_part, c->ctl};
+    for (void *q : ps) cudaFree(q);
+    if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return AG2_OK;
+}
+
+int ag2_set_params(ag2_ctx *c, const ag2_params *p)
+{
+    if (!c || !valid_params(p)) return set_err(c, AG2_E_INVALID, "invalid parameters");
+    bool retree = p->split_threshold != c->prm.split_threshold;
+    c->prm = *p;
+    if (retree) c->have_tree = false;
+    return AG2_OK;
+}
+
+int ag2_get_params(const ag2_ctx *c, ag2_params *p)
+{
+    if (!c || !p) return AG2_E_INVALID;
+    *p = c->prm;
+    return AG2_OK;
+}
+
+int ag2_set_stream(ag2_ctx *c, void *stream)
+{
+    if (!c) return AG2_E_INVALID;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return AG2_OK;
+}
+
+const char *ag2_last_error_string(const ag2_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+int ag2_upload(ag2_ctx *c, size_t n, const double *pos, const double *vel, const double *mass, const double *U,
+               const uint8_t *type)
+{
+    if (!c) return AG2_E_INVALID;
+    if (n > c->cap) return set_err(c, AG2_E_CAPACITY, "more particles than the context capacity");
+    if (n && (!pos || !mass || !type)) return set_err(c, AG2_E_INVALID, "pos, mass and type are required");
+    if (n == 0) {
+        c->n = 0;
+        c->have_tree = false;
+        return AG2_OK;
+    }
+    // host -> staging (positions | velocities), masses and U into the spare
+    // state half, which the unpack kernel does not write
+    Particles &spare = c->st[1];
+    double *pos_d = c->staging, *vel_d = vel ? c->staging + 3 * n : nullptr;
+    AG2_CUDA(c, cudaMemcpyAsync(pos_d, pos, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (vel) AG2_CUDA(c, cudaMemcpyAsync(vel_d, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(spare.m, mass, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (U) AG2_CUDA(c, cudaMemcpyAsync(spare.U, U, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(c->staging_u8, type, n, cudaMemcpyHostToDevice, c->stream));
+    return upload_common(c, n, pos_d, vel_d, spare.m, U ? spare.U : nullptr, c->staging_u8);
+}
+
+int ag2_upload_device(ag2_ctx *c, size_t n, const double *pos, const double *vel, const double *mass,
+                      const double *U, const uint8_t *type)
+{
+    if (!c) return AG2_E_INVALID;
+    if (n > c->cap) return set_err(c, AG2_E_CAPACITY, "more particles than the context capacity");
+    if (n && (!pos || !mass || !type)) return set_err(c, AG2_E_INVALID, "pos, mass and type are required");
+    if (n == 0) {
+        c->n = 0;
+        c->have_tree = false;
+        return AG2_OK;
+    }
+    return upload_common(c, n, pos, vel, mass, U, type);
+}
+
+int ag2_set_field(ag2_ctx *c, int f, const double *src, int src_is_device)
+{
+    if (!c || !src || f < AG2_POS || f > AG2_VDENS) return set_err(c, AG2_E_INVALID, "bad field");
+    size_t cnt = (f <= AG2_ACC ? 3 : 1) * c->n;
+    if (!c->n) return AG2_OK;
+    const double *in = src;
+    if (!src_is_device) {
+        AG2_CUDA(c, cudaMemcpyAsync(c->staging, src, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        in = c->staging;
+    }
+    AG2_LAUNCH(c, k_scatter_in, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), f, in);
+    if (f == AG2_POS || f == AG2_MASS) c->have_tree = false;
+    if (f == AG2_MASS) c->gas_table_mass = -1.0;
+    return AG2_OK;
+}
+
+int ag2_download(ag2_ctx *c, int f, double *dst, int dst_is_device)
+{
+    if (!c || !dst || f < AG2_POS || f > AG2_VDENS) return set_err(c, AG2_E_INVALID, "bad field");
+    size_t cnt = (f <= AG2_ACC ? 3 : 1) * c->n;
+    if (!c->n) return AG2_OK;
+    double *out = dst_is_device ? dst : c->staging;
+    AG2_LAUNCH(c, k_gather_out, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), f, out);
+    if (!dst_is_device) {
+        AG2_CUDA(c, cudaMemcpyAsync(dst, c->staging, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return AG2_OK;
+}
+
+size_t ag2_count(const ag2_ctx *c) { return c ? c->n : 0; }
+
+int ag2_build_tree(ag2_ctx *c)
+{
+    if (!c) return AG2_E_INVALID;
+    return build_tree(c);
+}
+
+int ag2_visual_density(ag2_ctx *c, double R)
+{
+    if (!c) return AG2_E_INVALID;
+    return run_visual_density(c, R);
+}
+
+int ag2_sph_density(ag2_ctx *c)
+{
+    if (!c) return AG2_E_INVALID;
+    return run_sph_density(c);
+}
+
+static int check_walk(Ctx *c)
+{
+    int rc = sync_ctl(c);
+    if (rc) return rc;
+    c->inter_grav = (int64_t)c->ctl_host->inter_grav;
+    c->inter_sph = (int64_t)c->ctl_host->inter_sph;
+    if (c->ctl_host->err_code == AG2_E_STACK)
+        return set_err(c, AG2_E_STACK, "walk stack overflow (tree deeper than the walk stack supports)");
+    return AG2_OK;
+}
+
+int ag2_forces(ag2_ctx *c)
+{
+    if (!c) return AG2_E_INVALID;
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    int rc = run_forces(c);
+    if (rc) return rc;
+    return check_walk(c);
+}
+
+int ag2_kick(ag2_ctx *c, double dt) { return c ? run_kick(c, dt) : AG2_E_INVALID; }
+int ag2_drift(ag2_ctx *c, double dt) { return c ? run_drift(c, dt) : AG2_E_INVALID; }
+int ag2_kick_drift(ag2_ctx *c, double dt) { return c ? run_kick_drift(c, dt) : AG2_E_INVALID; }
+int ag2_ueuler(ag2_ctx *c, double dt) { return c ? run_ueuler(c, dt) : AG2_E_INVALID; }
+int ag2_scale_positions(ag2_ctx *c, double f) { return c ? run_scale(c, f) : AG2_E_INVALID; }
+
+int ag2_step(ag2_ctx *c, double dt, double hubble_factor, int with_visual, double Rv)
+{
+    if (!c) return AG2_E_INVALID;
+    int rc;
+    if ((rc = run_kick_drift(c, dt))) return rc;
+    if ((rc = build_tree(c))) return rc;
+    if (with_visual && (rc = run_visual_density(c, Rv))) return rc;
+    if ((rc = run_sph_density(c))) return rc;
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    if ((rc = run_forces(c))) return rc;
+    if ((rc = run_close_step(c, dt, hubble_factor))) return rc;
+    return check_walk(c);
+}
+
+int ag2_root_radius(ag2_ctx *c, double *r)
+{
+    if (!c || !r) return AG2_E_INVALID;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
+    *r = c->root_radius;
+    return AG2_OK;
+}
+
+int ag2_node_count(ag2_ctx *c, int64_t *nodes, int64_t *internal, int32_t *max_depth)
+{
+    if (!c) return AG2_E_INVALID;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
+    if (nodes) *nodes = c->nnodes;
+    if (internal) *internal = c->ninternal;
+    if (max_depth) *max_depth = c->max_level;
+    return AG2_OK;
+}
+
+int ag2_interactions(ag2_ctx *c, int64_t *g, int64_t *s)
+{
+    if (!c) return AG2_E_INVALID;
+    if (g) *g = c->inter_grav;
+    if (s) *s = c->inter_sph;
+    return AG2_OK;
+}
+
+int64_t ag2_launch_count(const ag2_ctx *c) { return c ? c->launches : 0; }
+
+static uint64_t id_hash(uint64_t id)
+{
+    uint64_t z = id + 1 + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle, int64_t *cp_count,
+                 uint64_t *cp_hash, double *mass, double *com3, double *gas_mass, double *mvel3, double *center3,
+                 double *radius)
+{
+    if (!c) return AG2_E_INVALID;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
+    const int64_t nn = c->nnodes;
+    const size_t n = c->n;
+    std::vector<int32_t> start(nn), count(nn), ndrop(nn), first(nn), leafpos(nn), id(n);
+    std::vector<int8_t> level(nn);
+    std::vector<uint8_t> mode(nn);
+    std::vector<double> m(nn), cx(nn), cy(nn), cz(nn), g(nn), vx(nn), vy(nn), vz(nn), ccx(nn), ccy(nn), ccz(nn);
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+    };
+    Nodes &d = c->nd;
+    AG2_CUDA(c, cp(start.data(), d.start, nn * 4));
+    AG2_CUDA(c, cp(count.data(), d.count, nn * 4));
+    AG2_CUDA(c, cp(ndrop.data(), d.ndrop, nn * 4));
+    AG2_CUDA(c, cp(first.data(), d.first, nn * 4));
+    AG2_CUDA(c, cp(leafpos.data(), d.leafpos, nn * 4));
+    AG2_CUDA(c, cp(level.data(), d.level, nn));
+    AG2_CUDA(c, cp(mode.data(), d.mode, nn));
+    AG2_CUDA(c, cp(m.data(), d.mass, nn * 8));
+    AG2_CUDA(c, cp(cx.data(), d.comx, nn * 8));
+    AG2_CUDA(c, cp(cy.data(), d.comy, nn * 8));
+    AG2_CUDA(c, cp(cz.data(), d.comz, nn * 8));
+    AG2_CUDA(c, cp(g.data(), d.gas, nn * 8));
+    AG2_CUDA(c, cp(vx.data(), d.mvx, nn * 8));
+    AG2_CUDA(c, cp(vy.data(), d.mvy, nn * 8));
+    AG2_CUDA(c, cp(vz.data(), d.mvz, nn * 8));
+    AG2_CUDA(c, cp(ccx.data(), d.cx, nn * 8));
+    AG2_CUDA(c, cp(ccy.data(), d.cy, nn * 8));
+    AG2_CUDA(c, cp(ccz.data(), d.cz, nn * 8));
+    if (n) AG2_CUDA(c, cp(id.data(), c->S().id, n * 4));
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    // prefix sums of member hashes over tree-order slots
+    std::vector<uint64_t> hp(n + 1, 0);
+    for (size_t i = 0; i < n; i++) hp[i + 1] = hp[i] + id_hash((uint64_t)id[i]);
+    auto hsum = [&](int32_t a, int32_t b) { return hp[b] - hp[a]; };
+    // depth-first preorder, children 0..7
+    std::vector<int64_t> stack;
+    stack.push_back(0);
+    int64_t k = 0;
+    while (!stack.empty()) {
+        int64_t v = stack.back();
+        stack.pop_back();
+        int32_t s = start[v], e = s + count[v], re = e - ndrop[v];
+        int64_t cc = 0;
+        uint64_t ch = 0;
+        bool root = (v == 0);
+        switch (mode[v]) {
+        case MODE_PAR:
+        case MODE_VEC1:
+            if (!root) { cc = e - s; ch = hsum(s, e); }
+            break;
+        case MODE_SER_ENTRY:
+            if (root) { cc = re - s; ch = hsum(s, re); }
+            else { cc = (e - s) + (re - s); ch = hsum(s, e) + hsum(s, re); }
+            break;
+        case MODE_SER:
+            cc = re - s;
+            ch = hsum(s, re);
+            break;
+        default:
+            break;
+        }
+        if (depth) depth[k] = level[v];
+        if (is_leaf) is_leaf[k] = first[v] < 0 ? 1 : 0;
+        if (particle) particle[k] = leafpos[v] >= 0 ? id[leafpos[v]] : -1;
+        if (cp_count) cp_count[k] = cc;
+        if (cp_hash) cp_hash[k] = ch;
+        if (mass) mass[k] = m[v];
+        if (com3) { com3[3 * k] = cx[v]; com3[3 * k + 1] = cy[v]; com3[3 * k + 2] = cz[v]; }
+        if (gas_mass) gas_mass[k] = g[v];
+        if (mvel3) { mvel3[3 * k] = vx[v]; mvel3[3 * k + 1] = vy[v]; mvel3[3 * k + 2] = vz[v]; }
+        if (center3) { center3[3 * k] = ccx[v]; center3[3 * k + 1] = ccy[v]; center3[3 * k + 2] = ccz[v]; }
+        if (radius) radius[k] = std::ldexp(c->root_radius, -(int)level[v]);
+        k++;
+        if (first[v] >= 0)
+            for (int o = 7; o >= 0; o--) stack.push_back(first[v] + o);
+    }
+    return AG2_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,734 @@
+// ag2_build.cu -- device octree build with the reference's subdivision rule.
+//
+// Reference: simulation/src/Physics/Tree/Tree.cpp:24-55 (buildTree), :86-117
+// (calcTreeWidth); simulation/src/Physics/Tree/Node.cpp:405-534 (vector
+// insertion), :597-699 (serial insertion), :702-719 (getOctant).
+//
+// The reference decides octants by FP64 comparisons against node centres that
+// are accumulated as c + r*(+-0.5) from the root, with inclusive bounds tests
+// at every node.  This build is a most-significant-digit radix sort of the
+// particles by those decisions, one tree level per pass: each node that is
+// split at level L gets one pass in which every particle of its range computes
+// its 4-bit digit (octant 0..7, or 8 = outside this node's bounds) against the
+// node's precomputed bounds, and the range is partitioned by digit.  The digit
+// sequence of a particle is its Morton key under the reference's own rounding.
+// Node centres are computed once per node in FP64 exactly as the reference
+// does; particles only compare (as order-preserving 64-bit integers), so the
+// topology is bit-exact.
+//
+// Node modes reproduce Node::insert's switch at threads*100 particles: lists of
+// at least split_threshold particles take the parallel path (always split,
+// mass over the whole list), single-particle lists become leaves, and shorter
+// lists are inserted one by one (split when two particles land in-bounds).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "ag2_internal.cuh"
+
+namespace ag2 {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWidthBlocks = 608;  // 4 x 152 SMs
+constexpr int kSeqWidthMax = 32768;
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// warp-aggregated atomicAdd(&arr[slot], 1); returns the value before this
+// lane's increment
+__device__ __forceinline__ int agg_inc(int32_t *arr, int slot)
+{
+    unsigned act = __activemask();
+    unsigned peers = __match_any_sync(act, slot);
+    int leader = __ffs(peers) - 1;
+    int lane = lane_id();
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    int v = 0;
+    if (lane == leader) v = atomicAdd(&arr[slot], __popc(peers));
+    v = __shfl_sync(peers, v, leader);
+    return v + rank;
+}
+
+__device__ __forceinline__ double dist0(double x, double y, double z)
+{
+    // vec3::length(): sqrt(x*x + y*y + z*z), evaluated left to right, no FMA
+    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+}
+
+// ---- Tree::calcTreeWidth ---------------------------------------------------
+
+// Small N: the reference's sequential sums, bit for bit (Tree.cpp:99-103).
+__global__ void k_width_seq(const double *px, const double *py, const double *pz, int n, Ctx::Ctl *ctl)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0, s2 = 0.0;
+    for (int i = 0; i < n; i++) {
+        double d = dist0(px[i], py[i], pz[i]);
+        s = __dadd_rn(s, d);
+        s2 = __dadd_rn(s2, __dmul_rn(d, d));
+    }
+    ctl->sum_d = s;
+    ctl->sum_d2 = s2;
+}
+
+// Large N: deterministic two-stage FP64 sums.
+__global__ void k_width_partial(const double *px, const double *py, const double *pz, int n, double *part)
+{
+    __shared__ double sh[2][kBlock];
+    double s = 0.0, s2 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double d = dist0(px[i], py[i], pz[i]);
+        s += d;
+        s2 += d * d;
+    }
+    sh[0][threadIdx.x] = s;
+    sh[1][threadIdx.x] = s2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = sh[0][0];
+        part[2 * blockIdx.x + 1] = sh[1][0];
+    }
+}
+
+__global__ void k_width_final(const double *part, int nparts, Ctx::Ctl *ctl)
+{
+    if (threadIdx.x != 0) return;
+    double s = 0.0, s2 = 0.0;
+    for (int b = 0; b < nparts; b++) {
+        s += part[2 * b];
+        s2 += part[2 * b + 1];
+    }
+    ctl->sum_d = s;
+    ctl->sum_d2 = s2;
+}
+
+__global__ void k_width_thr(int n, Ctx::Ctl *ctl)
+{
+    if (threadIdx.x != 0) return;
+    double mean = ctl->sum_d / (double)n;
+    double sd = sqrt(__dsub_rn(ctl->sum_d2 / (double)n, __dmul_rn(mean, mean)));
+    ctl->thr = __dadd_rn(mean, __dmul_rn(10.0, sd));  // mean + acceptanceRatio*stdev (Tree.cpp:89,105)
+    ctl->R = 0.0;
+}
+
+__global__ void k_width_max(const double *px, const double *py, const double *pz, int n, Ctx::Ctl *ctl)
+{
+    // R = max |x| over |x| <= thr (Tree.cpp:107-116); a NaN threshold keeps R = 0
+    __shared__ unsigned long long sh[kBlock];
+    double thr = ctl->thr;
+    unsigned long long best = 0ull;  // key of +0.0
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double d = dist0(px[i], py[i], pz[i]);
+        if (d <= thr && d > 0.0) {
+            unsigned long long k = (unsigned long long)__double_as_longlong(d);
+            best = k > best ? k : best;
+        }
+    }
+    sh[threadIdx.x] = best;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] = max(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && sh[0] != 0ull) atomicMax((unsigned long long *)&ctl->R, sh[0]);
+}
+
+// ---- level-wise partition --------------------------------------------------
+
+__device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
+{
+    int64_t *k = nd.bkey + 9 * c;
+    double cx = nd.cx[c], cy = nd.cy[c], cz = nd.cz[c];
+    k[0] = okey(__dsub_rn(cx, r));
+    k[1] = okey(__dsub_rn(cy, r));
+    k[2] = okey(__dsub_rn(cz, r));
+    k[3] = okey(__dadd_rn(cx, r));
+    k[4] = okey(__dadd_rn(cy, r));
+    k[5] = okey(__dadd_rn(cz, r));
+    k[6] = okey(cx);
+    k[7] = okey(cy);
+    k[8] = okey(cz);
+}
+
+__global__ void k_root_init(Nodes nd, Ctx::Ctl *ctl, int n, int thresh, int32_t *pnode)
+{
+    if (threadIdx.x != 0) return;
+    double R = ctl->R;
+    nd.start[0] = 0;
+    nd.count[0] = n;
+    nd.ndrop[0] = 0;
+    nd.first[0] = -1;
+    nd.parent[0] = -1;
+    nd.level[0] = 0;
+    nd.cx[0] = 0.0;
+    nd.cy[0] = 0.0;
+    nd.cz[0] = 0.0;
+    uint8_t mode = n == 0 ? MODE_EMPTY : n == 1 ? MODE_VEC1 : n < thresh ? MODE_SER_ENTRY : MODE_PAR;
+    nd.mode[0] = mode;
+    uint8_t needs = (mode == MODE_PAR || mode == MODE_SER_ENTRY) ? 1 : 0;
+    nd.needs[0] = needs;
+    nd.leafpos[0] = (mode == MODE_VEC1) ? 0 : -1;
+    if (mode == MODE_VEC1) pnode[0] = 0;
+    if (needs) set_bounds(nd, 0, R);
+    ctl->node_count = 1;
+    ctl->next_needs = needs;
+    ctl->err_code = 0;
+    ctl->err_info = 0;
+    ctl->any_drop = 0;
+}
+
+__global__ void k_init_positions(int n, int root_needs, int32_t *perm, int32_t *posnode)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    perm[i] = i;
+    posnode[i] = root_needs ? 0 : -1;
+}
+
+// digit of every particle of a node being split at this level
+__global__ void k_digit(int n, int64_t base, const int32_t *__restrict__ posnode, const int32_t *__restrict__ perm,
+                        const double *__restrict__ px, const double *__restrict__ py,
+                        const double *__restrict__ pz, Nodes nd, uint8_t *__restrict__ digit,
+                        int32_t *__restrict__ hist)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int nid = posnode[i];
+    if (nid < 0) return;
+    int p = perm[i];
+    int64_t kx = okey(px[p]), ky = okey(py[p]), kz = okey(pz[p]);
+    const int64_t *k = nd.bkey + 9 * (int64_t)nid;
+    int d;
+    // inclusive bounds of Node::getOctant / insert(Particle*) (Node.cpp:606-608, 706-708)
+    if (kx < k[0] || kx > k[3] || ky < k[1] || ky > k[4] || kz < k[2] || kz > k[5]) {
+        d = 8;
+    } else {
+        d = (kx > k[6] ? 1 : 0) | (ky > k[7] ? 2 : 0) | (kz > k[8] ? 4 : 0);  // Node.cpp:714-716
+    }
+    digit[i] = (uint8_t)d;
+    agg_inc(hist, (int)((int64_t)nid - base) * 9 + d);
+}
+
+// split decisions and children of the nodes of one level
+__global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, int64_t node_cap, Nodes nd,
+                        Ctx::Ctl *ctl, const int32_t *__restrict__ hist, int32_t *__restrict__ cursor,
+                        int max_depth)
+{
+    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= count_lvl) return;
+    int64_t nid = base + j;
+    if (!nd.needs[nid]) return;
+    const int32_t *h = hist + 9 * j;
+    int32_t cnt = nd.count[nid];
+    int32_t start = nd.start[nid];
+    int32_t ndrop = h[8];
+    int32_t reached = cnt - ndrop;
+    uint8_t mode = nd.mode[nid];
+    nd.ndrop[nid] = ndrop;
+    if (ndrop) ctl->any_drop = 1;
+    int32_t acc = start;
+    for (int d = 0; d < 9; d++) {
+        cursor[9 * j + d] = acc;
+        acc += h[d];
+    }
+    bool internal = (mode == MODE_PAR) || (reached >= 2);
+    if (!internal) {
+        nd.first[nid] = -1;
+        nd.leafpos[nid] = (reached == 1) ? start : -1;
+        return;
+    }
+    if (level + 1 >= max_depth) {
+        atomicExch(&ctl->err_code, (int)AG2_E_COINCIDENT);
+        atomicExch(&ctl->err_info, (int)nid);
+        nd.first[nid] = -1;
+        nd.leafpos[nid] = -1;
+        return;
+    }
+    unsigned long long cb = atomicAdd((unsigned long long *)&ctl->node_count, 8ull);
+    if ((int64_t)cb + 8 > node_cap) {
+        atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+        nd.first[nid] = -1;
+        return;
+    }
+    int64_t c0 = (int64_t)cb;
+    nd.first[nid] = (int32_t)c0;
+    nd.leafpos[nid] = -1;
+    // child centres c + r*(+-0.5) and radius r/2 (Node.cpp:433-443, 630-642)
+    double r = ldexp(ctl->R, -level);
+    double rc = ldexp(ctl->R, -(level + 1));
+    double cx = nd.cx[nid], cy = nd.cy[nid], cz = nd.cz[nid];
+    bool par = (mode == MODE_PAR);
+    int nneeds = 0;
+    int32_t s = start;
+    for (int o = 0; o < 8; o++) {
+        int64_t c = c0 + o;
+        int32_t cc = h[o];
+        nd.cx[c] = __dadd_rn(cx, __dmul_rn(r, (o & 1) ? 0.5 : -0.5));
+        nd.cy[c] = __dadd_rn(cy, __dmul_rn(r, (o & 2) ? 0.5 : -0.5));
+        nd.cz[c] = __dadd_rn(cz, __dmul_rn(r, (o & 4) ? 0.5 : -0.5));
+        nd.start[c] = s;
+        nd.count[c] = cc;
+        nd.ndrop[c] = 0;
+        nd.first[c] = -1;
+        nd.parent[c] = (int32_t)nid;
+        nd.level[c] = (int8_t)(level + 1);
+        uint8_t cm;
+        if (cc == 0)
+            cm = MODE_EMPTY;
+        else if (!par)
+            cm = MODE_SER;
+        else if (cc == 1)
+            cm = MODE_VEC1;
+        else if (cc < thresh)
+            cm = MODE_SER_ENTRY;
+        else
+            cm = MODE_PAR;
+        nd.mode[c] = cm;
+        uint8_t needs = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER) ? 1 : 0;
+        nd.needs[c] = needs;
+        nd.leafpos[c] = (cm == MODE_VEC1) ? s : -1;
+        if (needs) set_bounds(nd, c, rc);
+        nneeds += needs;
+        s += cc;
+    }
+    if (nneeds) atomicAdd(&ctl->next_needs, nneeds);
+}
+
+__global__ void k_scatter(int n, int64_t base, const int32_t *__restrict__ posnode, const int32_t *__restrict__ perm,
+                          const uint8_t *__restrict__ digit, Nodes nd, int32_t *__restrict__ cursor,
+                          int32_t *__restrict__ perm2, int32_t *__restrict__ posnode2, int32_t *__restrict__ pnode)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int nid = posnode[i];
+    if (nid < 0) return;
+    int d = digit[i];
+    int np = agg_inc(cursor, (int)((int64_t)nid - base) * 9 + d);
+    perm2[np] = perm[i];
+    int32_t first = nd.first[nid];
+    if (first >= 0 && d < 8) {
+        int32_t child = first + d;
+        if (nd.needs[child]) {
+            posnode2[np] = child;
+        } else {
+            posnode2[np] = -1;
+            pnode[np] = child;  // single-particle leaf
+        }
+    } else {
+        posnode2[np] = -1;
+        pnode[np] = nid;  // leaf of a serial node, or the node's out-of-bounds tail
+    }
+}
+
+// Out-of-bounds tails are the only ranges whose order the partition leaves
+// open; put them in upload order so the build is deterministic.
+__global__ void k_sort_drops(int64_t nnodes, Nodes nd, int32_t *perm, const int32_t *id)
+{
+    int64_t nid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (nid >= nnodes) return;
+    int32_t nd8 = nd.ndrop[nid];
+    if (nd8 < 2) return;
+    int32_t e = nd.start[nid] + nd.count[nid];
+    int32_t b = e - nd8;
+    for (int32_t i = b + 1; i < e; i++) {
+        int32_t v = perm[i];
+        int32_t key = id[v];
+        int32_t j = i - 1;
+        while (j >= b && id[perm[j]] > key) {
+            perm[j + 1] = perm[j];
+            j--;
+        }
+        perm[j + 1] = v;
+    }
+}
+
+__global__ void k_reorder(int n, const int32_t *__restrict__ perm, Particles s, Particles d)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = perm[i];
+    d.px[i] = s.px[p];
+    d.py[i] = s.py[p];
+    d.pz[i] = s.pz[p];
+    d.vx[i] = s.vx[p];
+    d.vy[i] = s.vy[p];
+    d.vz[i] = s.vz[p];
+    d.ax[i] = s.ax[p];
+    d.ay[i] = s.ay[p];
+    d.az[i] = s.az[p];
+    d.m[i] = s.m[p];
+    d.U[i] = s.U[p];
+    d.dUdt[i] = s.dUdt[p];
+    d.h[i] = s.h[p];
+    d.rho[i] = s.rho[p];
+    d.P[i] = s.P[p];
+    d.T[i] = s.T[p];
+    d.vdens[i] = s.vdens[p];
+    d.type[i] = s.type[p];
+    d.id[i] = s.id[p];
+}
+
+// ---- moments, bottom-up ----------------------------------------------------
+
+struct Sums {
+    double m, mx, my, mz, g, gvx, gvy, gvz;
+    int32_t ng;
+    __device__ void zero() { m = mx = my = mz = g = gvx = gvy = gvz = 0.0; ng = 0; }
+    __device__ void add_particle(const Particles &P, int i)
+    {
+        double mi = P.m[i];
+        m += mi;
+        mx += P.px[i] * mi;
+        my += P.py[i] * mi;
+        mz += P.pz[i] * mi;
+        if (P.type[i] == 2) {
+            g += mi;
+            gvx += P.vx[i] * mi;
+            gvy += P.vy[i] * mi;
+            gvz += P.vz[i] * mi;
+            ng += 1;
+        }
+    }
+    __device__ void add_node(const Nodes &nd, int64_t c)
+    {
+        m += nd.tm[c];
+        mx += nd.tmx[c];
+        my += nd.tmy[c];
+        mz += nd.tmz[c];
+        g += nd.tg[c];
+        gvx += nd.tgvx[c];
+        gvy += nd.tgvy[c];
+        gvz += nd.tgvz[c];
+        ng += nd.tng[c];
+    }
+};
+
+__global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P, const double *gas_prefix,
+                          int gas_uniform, double theta, double R)
+{
+    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= count_lvl) return;
+    int64_t nid = base + j;
+    int32_t start = nd.start[nid], cnt = nd.count[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
+    uint8_t mode = nd.mode[nid];
+    int level = nd.level[nid];
+    Sums tot, own;  // tot: whole routed range; own: the reference's mass set
+    tot.zero();
+    own.zero();
+    uint8_t cmask = 0;
+    if (first >= 0) {
+        for (int o = 0; o < 8; o++) {
+            int64_t c = first + o;
+            own.add_node(nd, c);
+            if (nd.mass[c] != 0.0) cmask |= (uint8_t)(1u << o);
+        }
+        tot = own;
+        for (int32_t i = start + cnt - ndrop; i < start + cnt; i++) tot.add_particle(P, i);
+        if (mode == MODE_PAR) own = tot;  // the parallel path sums escapers too (Node.cpp:477-499)
+    } else {
+        for (int32_t i = start; i < start + cnt; i++) tot.add_particle(P, i);
+        if (mode == MODE_VEC1) {
+            own = tot;
+        } else {
+            for (int32_t i = start; i < start + cnt - ndrop; i++) own.add_particle(P, i);
+        }
+    }
+    nd.tm[nid] = tot.m;
+    nd.tmx[nid] = tot.mx;
+    nd.tmy[nid] = tot.my;
+    nd.tmz[nid] = tot.mz;
+    nd.tg[nid] = tot.g;
+    nd.tgvx[nid] = tot.gvx;
+    nd.tgvy[nid] = tot.gvy;
+    nd.tgvz[nid] = tot.gvz;
+    nd.tng[nid] = tot.ng;
+    nd.childmask[nid] = cmask;
+
+    double mass = own.m, cx = 0.0, cy = 0.0, cz = 0.0, gas = own.g, mvx = 0.0, mvy = 0.0, mvz = 0.0;
+    int32_t lp = nd.leafpos[nid];
+    bool leaf = first < 0;
+    if (leaf && lp >= 0) {
+        double mp = P.m[lp];
+        bool isgas = P.type[lp] == 2;
+        if (mode == MODE_VEC1) {
+            // Node.cpp:409-418: COM is the position itself, mVel stays zero
+            mass = mp;
+            cx = P.px[lp];
+            cy = P.py[lp];
+            cz = P.pz[lp];
+            gas = isgas ? mp : 0.0;
+        } else {
+            // one serial insertion into an empty leaf (Node.cpp:678-698)
+            mass = __dadd_rn(0.0, mp);
+            if (mass != 0.0) {
+                cx = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(P.px[lp], mp)), mass);
+                cy = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(P.py[lp], mp)), mass);
+                cz = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(P.pz[lp], mp)), mass);
+            }
+            gas = isgas ? __dadd_rn(0.0, mp) : 0.0;
+            if (isgas && gas > 0) {
+                mvx = __ddiv_rn(__dmul_rn(P.vx[lp], mp), gas);
+                mvy = __ddiv_rn(__dmul_rn(P.vy[lp], mp), gas);
+                mvz = __ddiv_rn(__dmul_rn(P.vz[lp], mp), gas);
+            }
+        }
+    } else {
+        if (mass > 0.0) {
+            cx = own.mx / mass;
+            cy = own.my / mass;
+            cz = own.mz / mass;
+        }
+        if (gas_uniform) gas = gas_prefix[own.ng];
+        if (own.g > 0) {
+            mvx = own.gvx / own.g;
+            mvy = own.gvy / own.g;
+            mvz = own.gvz / own.g;
+        }
+    }
+    nd.mass[nid] = mass;
+    nd.comx[nid] = cx;
+    nd.comy[nid] = cy;
+    nd.comz[nid] = cz;
+    nd.gas[nid] = gas;
+    nd.mvx[nid] = mvx;
+    nd.mvy[nid] = mvy;
+    nd.mvz[nid] = mvz;
+    nd.ngas[nid] = own.ng;
+
+    // FP32 walk record: COM split into hi + lo floats
+    float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    float lx = (float)(cx - (double)hx), ly = (float)(cy - (double)hy), lz = (float)(cz - (double)hz);
+    nd.wA[nid] = make_float4(hx, hy, hz, (float)mass);
+    float mac;
+    if (leaf) {
+        mac = -1.0f;
+    } else {
+        double q = ldexp(R, -level) / theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
+        mac = (float)(q * q);
+    }
+    nd.wB[nid] = make_float4(lx, ly, lz, mac);
+    if (leaf && lp >= 0)
+        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)gas);
+    else
+        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)gas);
+}
+
+__global__ void k_gas_stats(int n, const double *m, const uint8_t *type, Ctx::Ctl *ctl)
+{
+    __shared__ double smin[kBlock], smax[kBlock];
+    __shared__ int scnt[kBlock];
+    double lo = 1e308, hi = -1e308;
+    int cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (type[i] == 2) {
+            lo = fmin(lo, m[i]);
+            hi = fmax(hi, m[i]);
+            cnt++;
+        }
+    }
+    smin[threadIdx.x] = lo;
+    smax[threadIdx.x] = hi;
+    scnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
+            scnt[threadIdx.x] += scnt[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctl->gas_mass_min = smin[0];
+        ctl->gas_mass_max = smax[0];
+        ctl->ngas_total = scnt[0];
+    }
+}
+
+// gasMass of a node whose gas particles all weigh mg: the reference adds them
+// one at a time (Node.cpp:479-480, 681), so its value is the k-th partial sum
+__global__ void k_gas_prefix(int ngas, double mg, double *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    out[0] = 0.0;
+    for (int k = 1; k <= ngas; k++) {
+        s = __dadd_rn(s, mg);
+        out[k] = s;
+    }
+}
+
+template <class T>
+int grow(Ctx *c, T *&p, size_t old_n, size_t new_n)
+{
+    T *np = nullptr;
+    cudaError_t e = cudaMalloc((void **)&np, new_n * sizeof(T));
+    if (e != cudaSuccess) return set_err(c, AG2_E_NOMEM, "node pool allocation failed");
+    if (p && old_n) {
+        AG2_CUDA(c, cudaMemcpyAsync(np, p, old_n * sizeof(T), cudaMemcpyDeviceToDevice, c->stream));
+        AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    if (p) cudaFree(p);
+    p = np;
+    return AG2_OK;
+}
+
+}  // namespace
+
+int ensure_node_capacity(Ctx *c, size_t need)
+{
+    if (need <= c->node_cap) return AG2_OK;
+    size_t old = c->node_cap;
+    size_t nc = std::max(need + need / 4 + 1024, (size_t)1024);
+    nc = (nc + 3) & ~(size_t)3;  // byte flags are updated as 32-bit words
+    Nodes &d = c->nd;
+    int rc = AG2_OK;
+#define G(x) \
+    if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
+    G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
+    G(cx) G(cy) G(cz) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
+    G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(wA) G(wB) G(wD) G(flag) G(rho)
+#undef G
+    if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;
+    c->node_cap = nc;
+    return AG2_OK;
+}
+
+static int ensure_hist(Ctx *c, size_t nodes_in_level)
+{
+    size_t need = 9 * nodes_in_level;
+    if (need <= c->hist_cap) return AG2_OK;
+    size_t nc = std::max(need * 2, (size_t)4096);
+    if (c->hist) cudaFree(c->hist);
+    if (c->cursor) cudaFree(c->cursor);
+    c->hist = c->cursor = nullptr;
+    if (cudaMalloc(&c->hist, nc * sizeof(int32_t)) != cudaSuccess ||
+        cudaMalloc(&c->cursor, nc * sizeof(int32_t)) != cudaSuccess)
+        return set_err(c, AG2_E_NOMEM, "histogram allocation failed");
+    c->hist_cap = nc;
+    return AG2_OK;
+}
+
+static int prepare_gas_table(Ctx *c, int n, bool *uniform)
+{
+    Particles &S = c->S();
+    AG2_LAUNCH(c, k_gas_stats, 1, kBlock, 0, n, S.m, S.type, c->ctl);
+    int rc = sync_ctl(c);
+    if (rc) return rc;
+    const Ctx::Ctl &h = *c->ctl_host;
+    *uniform = h.ngas_total > 0 && h.gas_mass_min == h.gas_mass_max;
+    size_t need = (size_t)h.ngas_total + 1;
+    if (need > c->gas_prefix_cap) {
+        if (c->gas_prefix) cudaFree(c->gas_prefix);
+        c->gas_prefix = nullptr;
+        if (cudaMalloc(&c->gas_prefix, need * sizeof(double)) != cudaSuccess)
+            return set_err(c, AG2_E_NOMEM, "gas table allocation failed");
+        c->gas_prefix_cap = need;
+        c->gas_table_mass = -1.0;
+    }
+    if (*uniform && (c->gas_table_mass != h.gas_mass_min || c->gas_table_n != h.ngas_total)) {
+        AG2_LAUNCH(c, k_gas_prefix, 1, 1, 0, h.ngas_total, h.gas_mass_min, c->gas_prefix);
+        c->gas_table_mass = h.gas_mass_min;
+        c->gas_table_n = h.ngas_total;
+    }
+    return AG2_OK;
+}
+
+int build_tree(Ctx *c)
+{
+    const int n = (int)c->n;
+    c->have_tree = false;
+    Particles &S = c->S();
+    int rc;
+    bool gas_uniform = false;
+    if ((rc = prepare_gas_table(c, n, &gas_uniform)) != AG2_OK) return rc;
+
+    // root half-width
+    if (n > 0) {
+        if (n <= kSeqWidthMax) {
+            AG2_LAUNCH(c, k_width_seq, 1, 1, 0, S.px, S.py, S.pz, n, c->ctl);
+        } else {
+            AG2_LAUNCH(c, k_width_partial, kWidthBlocks, kBlock, 0, S.px, S.py, S.pz, n, c->width_part);
+            AG2_LAUNCH(c, k_width_final, 1, 32, 0, c->width_part, kWidthBlocks, c->ctl);
+        }
+        AG2_LAUNCH(c, k_width_thr, 1, 32, 0, n, c->ctl);
+        AG2_LAUNCH(c, k_width_max, kWidthBlocks, kBlock, 0, S.px, S.py, S.pz, n, c->ctl);
+    } else {
+        AG2_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream));
+    }
+    if ((rc = ensure_node_capacity(c, 1024)) != AG2_OK) return rc;
+    const int thresh = c->prm.split_threshold;
+    AG2_LAUNCH(c, k_root_init, 1, 32, 0, c->nd, c->ctl, n, thresh, c->pnode);
+    if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+    c->root_radius = c->ctl_host->R;
+    int root_needs = c->ctl_host->next_needs;
+    AG2_LAUNCH(c, k_init_positions, grid_for(n, kBlock), kBlock, 0, n, root_needs, c->perm, c->posnode);
+
+    c->level_base.assign({0, 1});
+    int level = 0;
+    int needs = root_needs;
+    while (needs > 0) {
+        int64_t base = c->level_base[level];
+        int64_t cnt_lvl = c->level_base[level + 1] - base;
+        if ((rc = ensure_hist(c, (size_t)cnt_lvl)) != AG2_OK) return rc;
+        if ((rc = ensure_node_capacity(c, (size_t)(c->level_base[level + 1] + 8 * cnt_lvl))) != AG2_OK) return rc;
+        AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, 9 * cnt_lvl * sizeof(int32_t), c->stream));
+        AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_needs, 0, sizeof(int32_t), c->stream));
+        Particles &Sp = c->S();
+        AG2_LAUNCH(c, k_digit, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, Sp.px, Sp.py, Sp.pz,
+                   c->nd, c->digit, c->hist);
+        AG2_LAUNCH(c, k_nodes, grid_for((size_t)cnt_lvl, kBlock), kBlock, 0, base, cnt_lvl, level, thresh,
+                   (int64_t)c->node_cap, c->nd, c->ctl, c->hist, c->cursor, (int)AG2_MAX_DEPTH);
+        AG2_CUDA(c, cudaMemcpyAsync(c->perm2, c->perm, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+        AG2_CUDA(c, cudaMemsetAsync(c->posnode2, 0xFF, n * sizeof(int32_t), c->stream));
+        AG2_LAUNCH(c, k_scatter, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, c->digit, c->nd,
+                   c->cursor, c->perm2, c->posnode2, c->pnode);
+        std::swap(c->perm, c->perm2);
+        std::swap(c->posnode, c->posnode2);
+        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        const Ctx::Ctl &h = *c->ctl_host;
+        if (h.err_code) {
+            if (h.err_code == AG2_E_COINCIDENT)
+                return set_err(c, AG2_E_COINCIDENT,
+                               "particles too close to separate within AG2_MAX_DEPTH levels "
+                               "(the reference recurses without end on coincident particles)");
+            return set_err(c, h.err_code, "octree build failed");
+        }
+        c->level_base.push_back(h.node_count);
+        needs = h.next_needs;
+        level++;
+    }
+    c->max_level = (int)c->level_base.size() - 2;
+    c->nnodes = c->level_base.back();
+    c->ninternal = (c->nnodes - 1) / 8;
+    if (c->ctl_host->any_drop)
+        AG2_LAUNCH(c, k_sort_drops, grid_for((size_t)c->nnodes, kBlock), kBlock, 0, c->nnodes, c->nd, c->perm, S.id);
+
+    // particle state into tree order
+    Particles &src = c->st[c->cur];
+    Particles &dst = c->st[c->cur ^ 1];
+    AG2_LAUNCH(c, k_reorder, grid_for(n, kBlock), kBlock, 0, n, c->perm, src, dst);
+    c->cur ^= 1;
+
+    // moments, deepest level first
+    for (int L = c->max_level; L >= 0; L--) {
+        int64_t base = c->level_base[L];
+        int64_t cnt = c->level_base[L + 1] - base;
+        AG2_LAUNCH(c, k_moments, grid_for((size_t)cnt, kBlock), kBlock, 0, base, cnt, c->nd, c->S(),
+                   c->gas_prefix, gas_uniform ? 1 : 0, c->prm.theta, c->root_radius);
+    }
+    c->have_tree = true;
+    c->tree_theta = c->prm.theta;
+    return AG2_OK;
+}
+
+}  // namespace ag2

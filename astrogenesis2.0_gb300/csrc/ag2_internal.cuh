@@ -1,0 +1,184 @@
+// ag2_internal.cuh -- device-side layout of the AstroGen2 GB300 hot path.
+//
+// Particle state lives in HBM as structure-of-arrays in *tree order*: every
+// ag2_build_tree re-sorts it so that each octree node owns a contiguous range
+// of particles and each walk group (32 consecutive particles) is spatially
+// compact.  `id` maps a tree-order slot back to the caller's upload index.
+//
+// The octree is a pool of nodes in structure-of-arrays form.  Every split node
+// owns 8 consecutive children (empty ones included, exactly as the reference's
+// Node::insert creates all 8, Node.cpp:433-443 / 630-642), so the node count
+// equals the reference's.  Nodes of one level are contiguous in the pool.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "ag2.h"
+
+namespace ag2 {
+
+// Node modes: how Node::insert(vector, cores) treats the node (Node.cpp:405-428).
+enum NodeMode : uint8_t {
+    MODE_EMPTY = 0,      // nothing routed here
+    MODE_PAR = 1,        // list of >= split_threshold particles: parallel partition
+    MODE_VEC1 = 2,       // list of exactly one particle: leaf without bounds test
+    MODE_SER_ENTRY = 3,  // list of 2..threshold-1: serial insertion, list kept in childParticles
+    MODE_SER = 4         // below a serial node: one-by-one insertion
+};
+
+struct Particles {
+    double *px, *py, *pz;
+    double *vx, *vy, *vz;
+    double *ax, *ay, *az;
+    double *m, *U, *dUdt, *h, *rho, *P, *T, *vdens;
+    uint8_t *type;
+    int32_t *id;
+};
+
+struct Nodes {
+    // topology (written by the level-wise build)
+    int32_t *start, *count, *ndrop, *first, *parent, *leafpos;
+    int8_t *level;
+    uint8_t *mode;
+    uint8_t *needs;      // node gets a digit pass at its level
+    uint8_t *childmask;  // bit o: child o has mass != 0
+    double *cx, *cy, *cz;
+    int64_t *bkey;       // 9 ordered-integer keys per node: lo xyz, hi xyz, centre xyz
+    // moments (reference semantics, FP64)
+    double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz;
+    int32_t *ngas;
+    // sums over the whole routed range (bottom-up helper)
+    double *tm, *tmx, *tmy, *tmz, *tg, *tgvx, *tgvy, *tgvz;
+    int32_t *tng;
+    // walk records (FP32 view)
+    float4 *wA;  // com_hi.xyz, mass
+    float4 *wB;  // com_lo.xyz, mac radius^2 (leaf: -1)
+    float4 *wD;  // gas velocity (mVel or the leaf particle's velocity), gasMass
+    // SPH / visual density scratch
+    uint8_t *flag;
+    double *rho;
+};
+
+struct Ctx {
+    ag2_params prm;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int device = 0;
+    size_t cap = 0;      // particle capacity
+    size_t n = 0;        // particles uploaded
+    size_t node_cap = 0; // node pool capacity
+    int64_t nnodes = 0;  // nodes in the current tree
+    int64_t ninternal = 0;
+    int max_level = 0;
+    std::vector<int64_t> level_base;  // node index of the first node of each level
+    bool have_tree = false;
+    double root_radius = 0.0;
+    int64_t launches = 0;
+    int64_t inter_grav = 0, inter_sph = 0;
+    std::string err;
+
+    Particles st[2] = {};
+    int cur = 0;
+
+    // build scratch
+    int32_t *perm = nullptr, *perm2 = nullptr, *posnode = nullptr, *posnode2 = nullptr;
+    int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
+    int32_t *finalnode = nullptr; // SPH / visual density result node per slot
+    int32_t *nodelist = nullptr;  // compacted node list (SPH density nodes)
+    uint8_t *digit = nullptr;
+    int32_t *hist = nullptr;      // 9 per node of a level
+    int32_t *cursor = nullptr;
+    size_t hist_cap = 0;
+    double *gas_prefix = nullptr; // sequential sums k*m_gas (uniform gas mass)
+    size_t gas_prefix_cap = 0;
+    double *staging = nullptr;    // 6n doubles for upload/download
+    uint8_t *staging_u8 = nullptr;
+    double *width_part = nullptr; // per-block partial sums of the root width
+    double gas_table_mass = -1.0; // gas particle mass the gasMass table was built for
+    int32_t gas_table_n = -1;
+    bool gas_uniform = false;
+    double tree_theta = 0.0;      // opening angle baked into the walk records
+
+    // small device control block
+    struct Ctl {
+        double sum_d, sum_d2, thr, R;
+        int64_t node_count;
+        int32_t err_code;
+        int32_t err_info;
+        int32_t next_needs;     // nodes needing a digit pass at the next level
+        int32_t any_drop;
+        int32_t gas_uniform;
+        int32_t ngas_total;
+        double gas_mass_min, gas_mass_max;
+        unsigned long long inter_grav, inter_sph;
+        int32_t list_count;
+        int32_t pad;
+    };
+    Ctl *ctl = nullptr;      // device
+    Ctl *ctl_host = nullptr; // pinned mirror
+
+    Nodes nd = {};
+
+    Particles &S() { return st[cur]; }
+};
+
+// ordered 64-bit integer key of a double: a < b (as doubles, -0 == +0 mapped
+// to +0) iff key(a) < key(b)
+__host__ __device__ inline int64_t okey(double x)
+{
+    x = x + 0.0;  // -0.0 -> +0.0
+    long long b;
+#ifdef __CUDA_ARCH__
+    b = __double_as_longlong(x);
+#else
+    __builtin_memcpy(&b, &x, 8);
+#endif
+    return b >= 0 ? (int64_t)b : (int64_t)(b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+
+// status helpers
+int set_err(Ctx *c, int code, const std::string &msg);
+int cuda_check(Ctx *c, cudaError_t e, const char *what);
+#define AG2_CUDA(c, call)                                   \
+    do {                                                    \
+        cudaError_t _e = (call);                            \
+        if (_e != cudaSuccess) return cuda_check(c, _e, #call); \
+    } while (0)
+
+inline unsigned grid_for(size_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// launch accounting: every kernel launch goes through this
+#define AG2_LAUNCH(c, kern, grid, block, smem, ...)                          \
+    do {                                                                     \
+        if ((grid) > 0) {                                                    \
+            kern<<<(grid), (block), (smem), (c)->stream>>>(__VA_ARGS__);     \
+            (c)->launches++;                                                 \
+            cudaError_t _le = cudaGetLastError();                            \
+            if (_le != cudaSuccess) return cuda_check(c, _le, #kern);        \
+        }                                                                    \
+    } while (0)
+
+// entry points implemented per translation unit
+int build_tree(Ctx *c);
+int ensure_node_capacity(Ctx *c, size_t need);
+int run_forces(Ctx *c);
+int run_sph_density(Ctx *c);
+int run_visual_density(Ctx *c, double R);
+int run_kick(Ctx *c, double dt);
+int run_drift(Ctx *c, double dt);
+int run_kick_drift(Ctx *c, double dt);
+int run_ueuler(Ctx *c, double dt);
+int run_scale(Ctx *c, double f);
+int sync_ctl(Ctx *c);  // copy ctl to host (synchronises the stream)
+
+// physical constants of the reference (Constants.h:14-15, Particle.h:40)
+constexpr double kGamma = 5.0 / 3.0;
+constexpr double kBoltzmann = 1.38064852e-23;
+constexpr double kProton = 1.6726219e-27;
+constexpr double kPi = 3.14159265358979323846;
+
+}  // namespace ag2

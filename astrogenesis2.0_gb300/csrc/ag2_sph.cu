@@ -1,0 +1,257 @@
+// ag2_sph.cu -- SPH density and visual density on the device octree.
+//
+// Reference: simulation/src/Physics/Tree/Tree.cpp:119-150 (calcGasDensity),
+// :152-175 (calcVisualDensity); Node.cpp:722-796 (Node::calcGasDensity),
+// :832-877 (Node::calcVisualDensity); kernel.cpp:4-16 (cubic spline).
+//
+// The reference runs a serial loop in particle order: a gas particle whose h is
+// still 0 climbs from its leaf while its node holds less than massInH of gas
+// and the parent's gas mass is strictly closer to massInH, then (if the stop
+// node is strictly closer than its own parent) sets h = 2*radius and one
+// node-level density for every gas particle in that node's childParticles.
+// Later firings overwrite earlier ones.  Because the stop rule depends only on
+// the node, and a node that fired covers every particle inside it, the nodes
+// that fire inside a given node always fire before it; so the value a particle
+// ends with comes from the outermost valid stop node that contains it.  The
+// kernels below compute exactly that without the serial loop:
+//   k_climb   every gas leaf particle climbs in parallel and flags its stop node
+//   k_final   every gas particle walks up its path and keeps the outermost
+//             flagged node whose childParticles hold it
+//   k_rho     one warp per selected node sums m W(|x - COM|, 2 r) over the
+//             node's childParticles (with the reference's duplicates)
+//   k_assign  h, rho, P, T per particle
+#include <algorithm>
+
+#include "ag2_internal.cuh"
+
+namespace ag2 {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+struct TreeView {
+    const int32_t *start, *count, *ndrop, *parent, *leafpos, *pnode;
+    const int8_t *level;
+    const uint8_t *mode;
+    const double *mass, *comx, *comy, *comz, *gas;
+};
+
+TreeView view(Ctx *c)
+{
+    TreeView t;
+    t.start = c->nd.start;
+    t.count = c->nd.count;
+    t.ndrop = c->nd.ndrop;
+    t.parent = c->nd.parent;
+    t.leafpos = c->nd.leafpos;
+    t.pnode = c->pnode;
+    t.level = c->nd.level;
+    t.mode = c->nd.mode;
+    t.mass = c->nd.mass;
+    t.comx = c->nd.comx;
+    t.comy = c->nd.comy;
+    t.comz = c->nd.comz;
+    t.gas = c->nd.gas;
+    return t;
+}
+
+// Is tree-order slot i in node n's childParticles?  (Node.cpp:515-522 gives a
+// non-root list to every node the parallel path creates; serial insertion
+// pushes only particles inside the node's bounds, Node.cpp:606-615; the root
+// receives no list.)
+__device__ __forceinline__ bool cp_member(const TreeView &t, int64_t n, int i)
+{
+    uint8_t md = t.mode[n];
+    int32_t reached_end = t.start[n] + t.count[n] - t.ndrop[n];
+    if (t.parent[n] < 0) return md == MODE_SER_ENTRY && i < reached_end;
+    if (md == MODE_SER) return i < reached_end;
+    return md != MODE_EMPTY;
+}
+
+__global__ void k_climb(int n, TreeView t, const uint8_t *type, double M, uint8_t *flag)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || type[i] != 2) return;
+    int pn = t.pnode[i];
+    if (pn < 0 || t.leafpos[pn] != i) return;  // no leaf (Particle::node is null)
+    int64_t nd = pn;
+    for (;;) {
+        double g = t.gas[nd];
+        if (g == 0) return;
+        int32_t par = t.parent[nd];
+        if (par < 0) return;
+        double md = M - g, pmd = M - t.gas[par];
+        if (g < M && fabs(md) > fabs(pmd)) {
+            nd = par;
+            continue;
+        }
+        if (fabs(md) < fabs(pmd) && g != 0) flag[nd] = 1;
+        return;
+    }
+}
+
+__global__ void k_final(int n, TreeView t, const uint8_t *type, uint8_t *flag, int32_t *finalnode,
+                        int32_t *list, Ctx::Ctl *ctl)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (type[i] != 2) {
+        finalnode[i] = -1;
+        return;
+    }
+    int64_t nd = t.pnode[i];
+    int32_t fin = -1;
+    while (nd >= 0) {
+        if ((flag[nd] & 1) && cp_member(t, nd, i)) fin = (int32_t)nd;
+        nd = t.parent[nd];
+    }
+    finalnode[i] = fin;
+    if (fin >= 0) {
+        unsigned int *w = (unsigned int *)(flag + (fin & ~3));
+        unsigned int bit = 2u << (8 * (fin & 3));
+        unsigned int old = atomicOr(w, bit);
+        if (!(old & bit)) list[atomicAdd(&ctl->list_count, 1)] = fin;
+    }
+}
+
+__device__ __forceinline__ double cubic_spline(double r, double h)
+{
+    // kernel::cubicSplineKernel (kernel.cpp:4-16)
+    double alpha = 1.0 / (kPi * h * h * h);
+    double q = r / h;
+    if (q < 1.0) return alpha * (1 - 1.5 * q * q + 0.75 * q * q * q);
+    if (q < 2.0) {
+        double t = 2 - q;
+        return alpha * 0.25 * (t * t * t);
+    }
+    return 0.0;
+}
+
+__global__ void k_rho(TreeView t, const double *px, const double *py, const double *pz, const double *m,
+                      const uint8_t *type, const int32_t *list, const Ctx::Ctl *ctl, double R, double *rho_node)
+{
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (w >= ctl->list_count) return;
+    int64_t nd = list[w];
+    double h = 2.0 * ldexp(R, -(int)t.level[nd]);  // h = radius * 2 (Node.cpp:765)
+    double cx = t.comx[nd], cy = t.comy[nd], cz = t.comz[nd];
+    int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
+    uint8_t md = t.mode[nd];
+    double acc = 0.0;
+    for (int32_t j = s + lane; j < e; j += 32) {
+        if (type[j] != 2) continue;
+        int mult;
+        if (md == MODE_SER_ENTRY)
+            mult = j < reached_end ? 2 : 1;  // list from the parent plus serial insertion (Node.cpp:518, 615)
+        else if (md == MODE_SER)
+            mult = j < reached_end ? 1 : 0;
+        else
+            mult = 1;
+        if (!mult) continue;
+        double dx = px[j] - cx, dy = py[j] - cy, dz = pz[j] - cz;
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        acc += mult * (m[j] * cubic_spline(r, h));
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) rho_node[nd] = acc;
+}
+
+__global__ void k_assign(int n, TreeView t, const int32_t *finalnode, const uint8_t *type, const double *U,
+                         const double *rho_node, double R, double *h, double *rho, double *P, double *T)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || type[i] != 2) return;
+    int32_t f = finalnode[i];
+    if (f < 0) {
+        h[i] = 0.0;  // Tree.cpp:123-133 resets h; rho, P, T keep their old values
+        return;
+    }
+    h[i] = ldexp(R, -(int)t.level[f]) * 2;
+    double r = rho_node[f];
+    rho[i] = r;
+    P[i] = (kGamma - 1.0) * U[i] * r;                           // Node.cpp:789
+    T[i] = (kGamma - 1.0) * U[i] * kProton * 0.58 / kBoltzmann;  // Node.cpp:791, mu = 0.58
+}
+
+// ---- visual density --------------------------------------------------------
+
+__global__ void k_vclimb(int n, TreeView t, double R, double Rv, uint8_t *flag)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int pn = t.pnode[i];
+    if (pn < 0 || t.leafpos[pn] != i) return;
+    int64_t nd = pn;
+    for (;;) {
+        int32_t par = t.parent[nd];
+        if (par < 0) return;
+        double r = ldexp(R, -(int)t.level[nd]);
+        double rp = ldexp(R, -(int)t.level[par]);
+        if (fabs(Rv - r) > fabs(Rv - rp)) {
+            nd = par;
+            continue;
+        }
+        double vol = r * r * r;
+        double mass = t.mass[nd];
+        if (vol == 0 || mass == 0) return;
+        double dens = mass / vol;
+        if (dens == 0 || isinf(dens)) return;
+        flag[nd] = 1;
+        return;
+    }
+}
+
+__global__ void k_vfinal(int n, TreeView t, const uint8_t *flag, double R, double *vdens)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t nd = t.pnode[i];
+    double v = 0.0;
+    while (nd >= 0) {
+        if (flag[nd] && cp_member(t, nd, i)) {
+            double r = ldexp(R, -(int)t.level[nd]);
+            v = t.mass[nd] / (r * r * r);
+        }
+        nd = t.parent[nd];
+    }
+    vdens[i] = v;
+}
+
+}  // namespace
+
+int run_sph_density(Ctx *c)
+{
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_sph_density needs a tree (call ag2_build_tree)");
+    const int n = (int)c->n;
+    if (n == 0 || c->ctl_host->ngas_total == 0) return AG2_OK;
+    Particles &S = c->S();
+    TreeView t = view(c);
+    AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
+    AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->prm.massInH, c->nd.flag);
+    AG2_LAUNCH(c, k_final, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->nd.flag, c->finalnode, c->nodelist,
+               c->ctl);
+    const int ngas = c->ctl_host->ngas_total;
+    AG2_LAUNCH(c, k_rho, grid_for((size_t)ngas * 32, kBlock), kBlock, 0, t, S.px, S.py, S.pz, S.m, S.type,
+               c->nodelist, c->ctl, c->root_radius, c->nd.rho);
+    AG2_LAUNCH(c, k_assign, grid_for(n, kBlock), kBlock, 0, n, t, c->finalnode, S.type, S.U, c->nd.rho,
+               c->root_radius, S.h, S.rho, S.P, S.T);
+    return AG2_OK;
+}
+
+int run_visual_density(Ctx *c, double Rv)
+{
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_visual_density needs a tree (call ag2_build_tree)");
+    const int n = (int)c->n;
+    if (n == 0) return AG2_OK;
+    Particles &S = c->S();
+    TreeView t = view(c);
+    AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
+    AG2_LAUNCH(c, k_vclimb, grid_for(n, kBlock), kBlock, 0, n, t, c->root_radius, Rv, c->nd.flag);
+    AG2_LAUNCH(c, k_vfinal, grid_for(n, kBlock), kBlock, 0, n, t, c->nd.flag, c->root_radius, S.vdens);
+    return AG2_OK;
+}
+
+}  // namespace ag2

@@ -1,0 +1,577 @@
+// ag2_walk.cu -- Barnes-Hut walk with softened gravity and in-walk SPH force.
+//
+// Reference: simulation/src/Physics/Tree/Tree.cpp:57-83 (calculateForces),
+// Node.cpp:247-399 (calculateGravityForce), :285-305 (softened pair law),
+// :88-172 (calcSPHForce), simulation/src/Math/kernel.cpp (kernels).
+//
+// One warp walks the tree for a group of 32 consecutive tree-order particles
+// (one per lane).  The reference decides per particle: open a node unless
+// radius/r < theta, with r the distance to the node's centre of mass.  To keep
+// those decisions per particle, every stack entry carries a 32-bit lane mask:
+// a node is opened for exactly the lanes whose own test failed, and a lane
+// that accepted a node never sees its descendants.  The stack lives in shared
+// memory (one slice per warp); node records are broadcast loads (every lane
+// reads the same address).  Groups are handed out by an atomic counter so
+// dense regions do not stall a fixed partition.
+//
+// Two arithmetic forms:
+//   FP64  -- "plain": everything in double, opening test exactly as the
+//            reference writes it (radius / r < theta).
+//   FP32  -- positions become float offsets from the group's centre; node
+//            centres of mass are stored as hi+lo float pairs, so a nearby node's
+//            offset keeps ~48 bits.  Opening tests and forces run in FP32; a
+//            test within 1e-5 of the threshold (or a distance that rounds to
+//            ~0) is re-decided in FP64 so the accepted node set matches the
+//            FP64 walk.  Accelerations are summed per child batch and added to a
+//            compensated (Kahan) accumulator.
+#include <algorithm>
+#include <cstdio>
+
+#include "ag2_internal.cuh"
+
+namespace ag2 {
+
+namespace {
+
+constexpr int kWalkBlock = 128;  // 4 warps
+constexpr int kStack = 512;      // entries per warp
+constexpr float kGuard = 1e-5f;
+
+struct WalkArgs {
+    int n;
+    const double *px, *py, *pz, *vx, *vy, *vz, *m, *h, *rho, *P;
+    const uint8_t *type;
+    const int32_t *pnode;
+    double *ax, *ay, *az, *dUdt;
+    const float4 *wA, *wB, *wD;
+    const int32_t *first, *leafpos;
+    const uint8_t *childmask;
+    const int8_t *level;
+    const double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz;
+    double R, theta, e0, G;
+    Ctx::Ctl *ctl;
+};
+
+// ---- reference kernels (FP64) ------------------------------------------------
+
+__device__ double softening_kernel(double u)
+{
+    // kernel::softeningKernel (kernel.cpp:41-56), same polynomial
+    if (u >= 0 && u < 0.5)
+        return (16.0 / 3.0) * (u * u) - (48.0 / 5.0) * pow(u, 4.0) + (32.0 / 5.0) * pow(u, 5.0) - (14.0 / 5.0);
+    if (u >= 0.5 && u < 1.0)
+        return (1.0 / (15.0 * u)) + (32.0 / 3.0) * (u * u) - 16.0 * pow(u, 3.0) - (48.0 / 5.0) * pow(u, 4.0) -
+               (32.0 / 15.0) * pow(u, 5.0) - (16.0 / 5.0);
+    if (u >= 1.0) return -1.0 / u;
+    return 0.0;
+}
+
+// Softening length actually used by Node.cpp:285-305.  The reference writes
+// abs(e) unqualified; in its translation unit that is int abs(int), so the test
+// e0*1e-4 < |e| < 1e30 sees |e| truncated to an integer (x86-64 conversion
+// semantics out of range).  Returns false where the reference returns early.
+__device__ bool general_eps2(double r, double e0, double *eps2)
+{
+    double u = r / (2.8 * e0);
+    double K = softening_kernel(u);
+    if ((K - r) == 0) return false;
+    double e = -(2.8 * e0) / (K - r);
+    if (isnan(e)) return false;
+    double ae;
+    if (!(e > -2147483649.0 && e < 2147483648.0))
+        ae = -2147483648.0;
+    else
+        ae = fabs(trunc(e));
+    double eps = (ae > e0 * 0.0001 && ae < 1e30) ? e : e0;
+    *eps2 = eps * eps;
+    return true;
+}
+
+template <class F>
+struct Vec3 {
+    F x, y, z;
+};
+
+// kernel::gradientCubicSplineKernel (kernel.cpp:18-39): returns the scalar s
+// with gradW = d * s
+template <class F>
+__device__ __forceinline__ F grad_w_scale(F r, F h)
+{
+    if (r == F(0)) return F(0);
+    F alpha = F(1) / (F(kPi) * h * h * h);
+    F q = r / h;
+    F g;
+    if (q < F(1))
+        g = alpha * (F(-3) * q + F(2.25) * q * q);
+    else if (q < F(2))
+        g = alpha * (F(-0.75) * (F(2) - q) * (F(2) - q));
+    else
+        return F(0);
+    g = g / h;
+    return g / r;
+}
+
+// Node::calcSPHForce with j = i substitutions (Node.cpp:88-172).
+// dd = x_i - COM, vij = v_i - v_j.  Adds to f (unless NaN) and du.
+template <class F>
+__device__ __forceinline__ void sph_pair(F gm, F dx, F dy, F dz, F r, F vx, F vy, F vz, F h, F pr, F c,
+                                         Vec3<F> &f, F &du)
+{
+    F s = grad_w_scale<F>(r, h);
+    F gx = dx * s, gy = dy * s, gz = dz * s;
+    F fx = -gm * pr * gx, fy = -gm * pr * gy, fz = -gm * pr * gz;
+    F vd = vx * dx + vy * dy + vz * dz;
+    F mu = h * vd / (r * r + F(0.01) * (h * h));
+    F MU = F(0);
+    if (vd < F(0)) MU = F(-0.5) * c * mu + F(1) * (mu * mu);
+    fx += -gm * MU * gx;
+    fy += -gm * MU * gy;
+    fz += -gm * MU * gz;
+    du += F(0.5) * gm * (pr + MU) * (vx * gx + vy * gy + vz * gz);
+    if (isnan(fx) || isnan(fy) || isnan(fz)) return;
+    f.x += fx;
+    f.y += fy;
+    f.z += fz;
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v)
+{
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// ---- FP64 plain walk ---------------------------------------------------------
+
+template <bool kGeneral, bool kGas>
+__global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
+{
+    __shared__ int2 stk_all[(kWalkBlock / 32) * kStack];
+    const int lane = threadIdx.x & 31;
+    int2 *stk = stk_all + (threadIdx.x >> 5) * kStack;
+    const int ngroups = (a.n + 31) >> 5;
+    const double eps02 = a.e0 * a.e0;
+    unsigned long long cnt_g = 0, cnt_s = 0;
+    for (;;) {
+        int grp = 0;
+        if (lane == 0) grp = atomicAdd(&a.ctl->list_count, 1);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= ngroups) break;
+        const int i = grp * 32 + lane;
+        const bool valid = i < a.n && a.m[i] != 0.0;
+        double xi = 0, yi = 0, zi = 0, hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
+        bool gas_i = false;
+        int myleaf = -1;
+        if (i < a.n) {
+            xi = a.px[i];
+            yi = a.py[i];
+            zi = a.pz[i];
+            int pn = a.pnode[i];
+            myleaf = (pn >= 0 && a.leafpos[pn] == i) ? pn : -1;
+            if (kGas && a.type[i] == 2) {
+                gas_i = true;
+                hi_ = a.h[i];
+                double rho = a.rho[i], P = a.P[i];
+                pr = P / (rho * rho) + P / (rho * rho);
+                cs = sqrt(kGamma * P / rho);
+                vxi = a.vx[i];
+                vyi = a.vy[i];
+                vzi = a.vz[i];
+            }
+        }
+        Vec3<double> acc = {0, 0, 0};
+        double du = 0;
+        const unsigned all = __ballot_sync(0xffffffffu, valid);
+        int sp = 0;
+        bool overflow = false;
+        if (all && a.mass[0] != 0.0) {
+            stk[0] = make_int2(0, (int)all);  // evaluate the root itself
+            sp = 1;
+        }
+        __syncwarp();
+        // stack entries: (node, lanes) -- evaluate `node` for these lanes
+        while (sp > 0) {
+            sp--;
+            const int2 e = stk[sp];
+            __syncwarp();
+            const int c = e.x;
+            const unsigned msk = (unsigned)e.y;
+            const bool in = (msk >> lane) & 1u;
+            bool open = false;
+            const int32_t fc = a.first[c];
+            const bool leaf = fc < 0;
+            if (in && !(leaf && c == myleaf)) {
+                double dx = a.comx[c] - xi, dy = a.comy[c] - yi, dz = a.comz[c] - zi;
+                double r = sqrt(dx * dx + dy * dy + dz * dz);
+                if (r != 0.0) {
+                    bool interact = leaf;
+                    if (!leaf) {
+                        double rad = ldexp(a.R, -(int)a.level[c]);
+                        if (rad / r < a.theta)
+                            interact = true;
+                        else
+                            open = true;
+                    }
+                    if (interact) {
+                        double e2 = eps02;
+                        bool ok = true;
+                        if (kGeneral) ok = general_eps2(r, a.e0, &e2);
+                        if (ok) {
+                            double s = a.G * a.mass[c] / (r * r + e2);
+                            double gx = (dx / r) * s, gy = (dy / r) * s, gz = (dz / r) * s;
+                            if (!(isnan(gx) || isnan(gy) || isnan(gz))) {
+                                acc.x += gx;
+                                acc.y += gy;
+                                acc.z += gz;
+                                cnt_g++;
+                                if (kGas && gas_i && r < hi_ * 2) {
+                                    double gm = a.gas[c];
+                                    if (gm > 0) {
+                                        double vjx, vjy, vjz;
+                                        if (leaf) {
+                                            int lp = a.leafpos[c];
+                                            vjx = a.vx[lp];
+                                            vjy = a.vy[lp];
+                                            vjz = a.vz[lp];
+                                        } else {
+                                            vjx = a.mvx[c];
+                                            vjy = a.mvy[c];
+                                            vjz = a.mvz[c];
+                                        }
+                                        sph_pair<double>(gm, -dx, -dy, -dz, r, vxi - vjx, vyi - vjy, vzi - vjz, hi_,
+                                                         pr, cs, acc, du);
+                                        cnt_s++;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            const unsigned om = __ballot_sync(0xffffffffu, open);
+            if (om) {
+                const unsigned cm = a.childmask[c];
+                const int nch = __popc(cm);
+                if (sp + nch > kStack) {
+                    overflow = true;
+                    break;
+                }
+                // push children 7..0 so that child 0 is evaluated first (DFS order)
+                for (int o = 7; o >= 0; o--)
+                    if ((cm >> o) & 1u) {
+                        if (lane == 0) stk[sp] = make_int2(fc + o, (int)om);
+                        sp++;
+                    }
+            }
+            __syncwarp();
+        }
+        if (overflow && lane == 0) {
+            atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
+            atomicExch(&a.ctl->err_info, grp);
+        }
+        if (i < a.n) {
+            a.ax[i] = valid ? acc.x : 0.0;
+            a.ay[i] = valid ? acc.y : 0.0;
+            a.az[i] = valid ? acc.z : 0.0;
+            if (kGas && gas_i && valid) a.dUdt[i] += du;
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt_g += __shfl_down_sync(0xffffffffu, cnt_g, o);
+        cnt_s += __shfl_down_sync(0xffffffffu, cnt_s, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.ctl->inter_grav, cnt_g);
+        atomicAdd(&a.ctl->inter_sph, cnt_s);
+    }
+}
+
+// ---- FP32-offset walk --------------------------------------------------------
+
+__device__ __forceinline__ double warp_min(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <bool kGeneral, bool kGas>
+__global__ void __launch_bounds__(kWalkBlock) k_walk32(WalkArgs a)
+{
+    __shared__ int2 stk_all[(kWalkBlock / 32) * kStack];
+    const int lane = threadIdx.x & 31;
+    int2 *stk = stk_all + (threadIdx.x >> 5) * kStack;
+    const int ngroups = (a.n + 31) >> 5;
+    const float G = (float)a.G;
+    const float eps02 = (float)(a.e0 * a.e0);
+    unsigned long long cnt_g = 0, cnt_s = 0;
+    for (;;) {
+        int grp = 0;
+        if (lane == 0) grp = atomicAdd(&a.ctl->list_count, 1);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= ngroups) break;
+        const int i = grp * 32 + lane;
+        const bool valid = i < a.n && a.m[i] != 0.0;
+        double xi = 0, yi = 0, zi = 0;
+        if (i < a.n) {
+            xi = a.px[i];
+            yi = a.py[i];
+            zi = a.pz[i];
+        }
+        // group centre: middle of the bounding box of the valid lanes
+        double gx = 0, gy = 0, gz = 0;
+        {
+            double lx = valid ? xi : 1e300, ly = valid ? yi : 1e300, lz = valid ? zi : 1e300;
+            double ux = valid ? xi : -1e300, uy = valid ? yi : -1e300, uz = valid ? zi : -1e300;
+            lx = warp_min(lx);
+            ly = warp_min(ly);
+            lz = warp_min(lz);
+            ux = warp_max(ux);
+            uy = warp_max(uy);
+            uz = warp_max(uz);
+            if (lx <= ux) {
+                gx = 0.5 * (lx + ux);
+                gy = 0.5 * (ly + uy);
+                gz = 0.5 * (lz + uz);
+            }
+        }
+        const float ghx = (float)gx, ghy = (float)gy, ghz = (float)gz;
+        const float glx = (float)(gx - (double)ghx), gly = (float)(gy - (double)ghy),
+                    glz = (float)(gz - (double)ghz);
+        const float ox = (float)(xi - gx), oy = (float)(yi - gy), oz = (float)(zi - gz);
+        int myleaf = -1;
+        float hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
+        bool gas_i = false;
+        if (i < a.n) {
+            int pn = a.pnode[i];
+            myleaf = (pn >= 0 && a.leafpos[pn] == i) ? pn : -1;
+            if (kGas && a.type[i] == 2) {
+                gas_i = true;
+                hi_ = (float)a.h[i];
+                double rho = a.rho[i], P = a.P[i];
+                pr = (float)(P / (rho * rho) + P / (rho * rho));
+                cs = (float)sqrt(kGamma * P / rho);
+                vxi = (float)a.vx[i];
+                vyi = (float)a.vy[i];
+                vzi = (float)a.vz[i];
+            }
+        }
+        const float h2x4 = 4.0f * hi_ * hi_;
+        float sx = 0, sy = 0, sz = 0, kx = 0, ky = 0, kz = 0;  // Kahan sums
+        float du = 0;
+        const unsigned all = __ballot_sync(0xffffffffu, valid);
+        int sp = 0;
+        bool overflow = false;
+
+        // evaluate one node for this lane: returns 0 skip, 1 accepted, 2 open
+        auto eval = [&](int c, const float4 &A, const float4 &B, Vec3<float> &bs, bool in) -> int {
+            if (!in) return 0;
+            const bool leaf = B.w < 0.0f;
+            if (leaf && c == myleaf) return 0;
+            float dx = ((A.x - ghx) + (B.x - glx)) - ox;
+            float dy = ((A.y - ghy) + (B.y - gly)) - oy;
+            float dz = ((A.z - ghz) + (B.z - glz)) - oz;
+            float r2 = dx * dx + dy * dy + dz * dz;
+            int decision;
+            const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * B.w;
+            if (r2 <= tiny || (!leaf && fabsf(r2 - B.w) <= kGuard * B.w)) {
+                // re-decide exactly as the FP64 walk
+                double ddx = a.comx[c] - xi, ddy = a.comy[c] - yi, ddz = a.comz[c] - zi;
+                double r = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+                if (r == 0.0) return 0;
+                if (leaf)
+                    decision = 1;
+                else
+                    decision = (ldexp(a.R, -(int)a.level[c]) / r < a.theta) ? 1 : 2;
+                if (decision == 2) return 2;
+                if (r2 <= tiny) {
+                    // distance too small for the float offsets: FP64 force
+                    double e2 = a.e0 * a.e0;
+                    if (kGeneral && !general_eps2(r, a.e0, &e2)) return 1;
+                    double s = a.G * a.mass[c] / (r * r + e2);
+                    bs.x += (float)((ddx / r) * s);
+                    bs.y += (float)((ddy / r) * s);
+                    bs.z += (float)((ddz / r) * s);
+                    cnt_g++;
+                    return 1;
+                }
+            } else {
+                decision = (leaf || r2 > B.w) ? 1 : 2;
+                if (decision == 2) return 2;
+            }
+            const float ir = rsqrtf(r2);
+            float e2 = eps02;
+            if (kGeneral) {
+                double de2;
+                if (!general_eps2((double)(r2 * ir), a.e0, &de2)) return 1;
+                e2 = (float)de2;
+            }
+            const float s = __fdividef(G * A.w * ir, r2 + e2);
+            bs.x += dx * s;
+            bs.y += dy * s;
+            bs.z += dz * s;
+            cnt_g++;
+            if (kGas && gas_i && r2 < h2x4) {
+                const float4 D = a.wD[c];
+                if (D.w > 0.0f) {
+                    sph_pair<float>(D.w, -dx, -dy, -dz, r2 * ir, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs, bs,
+                                    du);
+                    cnt_s++;
+                }
+            }
+            return 1;
+        };
+
+        if (all) {
+            // the root on its own
+            Vec3<float> bs = {0, 0, 0};
+            const float4 A = a.wA[0], B = a.wB[0];
+            int d = (a.mass[0] != 0.0) ? eval(0, A, B, bs, valid) : 0;
+            kahan_add(sx, kx, bs.x);
+            kahan_add(sy, ky, bs.y);
+            kahan_add(sz, kz, bs.z);
+            const unsigned om = __ballot_sync(0xffffffffu, d == 2);
+            if (om) {
+                if (lane == 0) stk[0] = make_int2(0, (int)om);
+                sp = 1;
+            }
+        }
+        __syncwarp();
+        // stack entries: (parent, lanes) -- evaluate the non-empty children of parent
+        while (sp > 0) {
+            sp--;
+            const int2 e = stk[sp];
+            __syncwarp();
+            const int p = e.x;
+            const unsigned msk = (unsigned)e.y;
+            const bool in = (msk >> lane) & 1u;
+            const int32_t fc = a.first[p];
+            const unsigned cm = a.childmask[p];
+            Vec3<float> bs = {0, 0, 0};
+            unsigned om[8];
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                om[o] = 0;
+                if ((cm >> o) & 1u) {
+                    const int c = fc + o;
+                    const float4 A = a.wA[c];
+                    const float4 B = a.wB[c];
+                    int d = eval(c, A, B, bs, in);
+                    om[o] = __ballot_sync(0xffffffffu, d == 2);
+                }
+            }
+            kahan_add(sx, kx, bs.x);
+            kahan_add(sy, ky, bs.y);
+            kahan_add(sz, kz, bs.z);
+            int npush = 0;
+#pragma unroll
+            for (int o = 0; o < 8; o++) npush += om[o] ? 1 : 0;
+            if (sp + npush > kStack) {
+                overflow = true;
+                break;
+            }
+#pragma unroll
+            for (int o = 7; o >= 0; o--)
+                if (om[o]) {
+                    if (lane == 0) stk[sp] = make_int2(fc + o, (int)om[o]);
+                    sp++;
+                }
+            __syncwarp();
+        }
+        if (overflow && lane == 0) {
+            atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
+            atomicExch(&a.ctl->err_info, grp);
+        }
+        if (i < a.n) {
+            a.ax[i] = valid ? (double)sx - (double)kx : 0.0;
+            a.ay[i] = valid ? (double)sy - (double)ky : 0.0;
+            a.az[i] = valid ? (double)sz - (double)kz : 0.0;
+            if (kGas && gas_i && valid) a.dUdt[i] += (double)du;
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt_g += __shfl_down_sync(0xffffffffu, cnt_g, o);
+        cnt_s += __shfl_down_sync(0xffffffffu, cnt_s, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&a.ctl->inter_grav, cnt_g);
+        atomicAdd(&a.ctl->inter_sph, cnt_s);
+    }
+}
+
+__global__ void k_update_mac(int64_t nnodes, const int32_t *first, const int8_t *level, float4 *wB, double R,
+                             double theta)
+{
+    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= nnodes) return;
+    if (first[j] < 0) return;
+    double q = ldexp(R, -(int)level[j]) / theta;
+    wB[j].w = (float)(q * q);
+}
+
+}  // namespace
+
+int run_forces(Ctx *c)
+{
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_forces needs a tree (call ag2_build_tree)");
+    if (c->n == 0) return AG2_OK;
+    if (c->prm.theta != c->tree_theta) {
+        AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.level,
+                   c->nd.wB, c->root_radius, c->prm.theta);
+        c->tree_theta = c->prm.theta;
+    }
+    Particles &S = c->S();
+    WalkArgs a;
+    a.n = (int)c->n;
+    a.px = S.px; a.py = S.py; a.pz = S.pz;
+    a.vx = S.vx; a.vy = S.vy; a.vz = S.vz;
+    a.m = S.m; a.h = S.h; a.rho = S.rho; a.P = S.P;
+    a.type = S.type;
+    a.pnode = c->pnode;
+    a.ax = S.ax; a.ay = S.ay; a.az = S.az; a.dUdt = S.dUdt;
+    a.wA = c->nd.wA; a.wB = c->nd.wB; a.wD = c->nd.wD;
+    a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.childmask = c->nd.childmask; a.level = c->nd.level;
+    a.mass = c->nd.mass; a.comx = c->nd.comx; a.comy = c->nd.comy; a.comz = c->nd.comz;
+    a.gas = c->nd.gas; a.mvx = c->nd.mvx; a.mvy = c->nd.mvy; a.mvz = c->nd.mvz;
+    a.R = c->root_radius;
+    a.theta = c->prm.theta;
+    a.e0 = c->prm.e0;
+    a.G = c->prm.G;
+    a.ctl = c->ctl;
+    // The softening law reduces to Plummer softening with e0 whenever the
+    // truncated |e| of Node.cpp:302 is 0 for every distance, i.e. e0 < 0.66.
+    const bool general = !(c->prm.e0 > 0.0 && c->prm.e0 < 0.6);
+    const bool gas = c->ctl_host->ngas_total > 0;
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->inter_grav, 0, 2 * sizeof(unsigned long long), c->stream));
+    int dev_sms = 152;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int ngroups = (int)((c->n + 31) / 32);
+    int blocks = std::min((ngroups + 3) / 4, dev_sms * 16);
+    if (blocks < 1) blocks = 1;
+#define WALK(K) AG2_LAUNCH(c, K, blocks, kWalkBlock, 0, a)
+    if (c->prm.precision == AG2_PREC_FP64) {
+        if (general) {
+            if (gas) WALK((k_walk64<true, true>)); else WALK((k_walk64<true, false>));
+        } else {
+            if (gas) WALK((k_walk64<false, true>)); else WALK((k_walk64<false, false>));
+        }
+    } else {
+        if (general) {
+            if (gas) WALK((k_walk32<true, true>)); else WALK((k_walk32<true, false>));
+        } else {
+            if (gas) WALK((k_walk32<false, true>)); else WALK((k_walk32<false, false>));
+        }
+    }
+#undef WALK
+    return AG2_OK;
+}
+
+}  // namespace ag2

@@ -1,0 +1,149 @@
+/*
+ * ag2.h -- C-ABI of the GB300 (sm_103a) implementation of AstroGen2's force hot
+ * path: octree build, SPH density, Barnes-Hut walk with in-walk SPH force, and
+ * the leapfrog kick/drift.
+ *
+ * Every entry point returns an int status (AG2_OK = 0, negative = AG2_E_*).
+ * Work is ordered on the context's CUDA stream; calls that hand results back
+ * to host memory synchronise that stream.  One context per host thread.  Host
+ * buffers are only borrowed for the duration of a call.  Quantities are FP64
+ * in the caller's units with gravitational constant params.G (1 for code
+ * units).
+ *
+ * Mapping to the reference (simulation/src/...):
+ *   ag2_build_tree      Tree::buildTree            Physics/Tree/Tree.cpp:24-55
+ *                       (+ Node::insert            Physics/Tree/Node.cpp:405-534, 597-719)
+ *   ag2_root_radius     Tree::calcTreeWidth        Physics/Tree/Tree.cpp:86-117
+ *   ag2_visual_density  Tree::calcVisualDensity    Physics/Tree/Tree.cpp:152-175, Node.cpp:832-877
+ *   ag2_sph_density     Tree::calcGasDensity       Physics/Tree/Tree.cpp:119-150, Node.cpp:722-796
+ *   ag2_forces          Tree::calculateForces      Physics/Tree/Tree.cpp:57-83, Node.cpp:88-172, 247-399
+ *   ag2_kick            TimeIntegration::Kick      Physics/TimeIntegration.cpp:10-19
+ *   ag2_drift           TimeIntegration::Drift     Physics/TimeIntegration.cpp:21-25
+ *   ag2_ueuler          TimeIntegration::Ueuler    Physics/TimeIntegration.cpp:28-40
+ *   ag2_step            one pass of the step loop  Physics/Simulation.cpp:256-341
+ *   ag2_upload/download Simulation::particles       Physics/Simulation.h:70, Physics/Particle.h:9-57
+ */
+#ifndef AG2_C_ABI_H_
+#define AG2_C_ABI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AG2_ABI_VERSION 1
+
+enum ag2_status {
+    AG2_OK = 0,
+    AG2_E_INVALID = -1,     /* bad argument or state (e.g. forces before a tree) */
+    AG2_E_CUDA = -2,        /* a CUDA runtime call failed */
+    AG2_E_NOMEM = -3,       /* device allocation failed */
+    AG2_E_COINCIDENT = -4,  /* particles too close to separate: the reference recurses without end */
+    AG2_E_DEPTH = -5,       /* octree deeper than AG2_MAX_DEPTH levels */
+    AG2_E_STACK = -6,       /* walk stack overflow (reported by the kernel, no fault) */
+    AG2_E_NAN = -7,         /* non-finite particle position */
+    AG2_E_CAPACITY = -8     /* more particles than the context was created for */
+};
+
+#define AG2_MAX_DEPTH 96
+
+enum ag2_precision {
+    AG2_PREC_FP64 = 0,      /* plain walk: all arithmetic in FP64 */
+    AG2_PREC_FP32 = 1       /* FP32 offsets from the walk group's centre + compensated sums */
+};
+
+enum ag2_field {
+    AG2_POS = 0,   /* 3n doubles, xyz interleaved */
+    AG2_VEL = 1,   /* 3n */
+    AG2_ACC = 2,   /* 3n */
+    AG2_MASS = 3,  /* n  */
+    AG2_H = 4,     /* n  smoothing length */
+    AG2_RHO = 5,   /* n  */
+    AG2_P = 6,     /* n  */
+    AG2_T = 7,     /* n  */
+    AG2_U = 8,     /* n  internal energy */
+    AG2_DUDT = 9,  /* n  */
+    AG2_VDENS = 10 /* n  visualDensity */
+};
+
+typedef struct ag2_params {
+    double G;             /* gravitational constant */
+    double e0;            /* softening length, Simulation::e0 */
+    double theta;         /* opening angle, Simulation::theta */
+    double massInH;       /* SPH neighbour mass, Simulation::massInH */
+    int32_t split_threshold; /* Node::insert switches to serial insertion below this
+                                many particles; the reference uses
+                                omp_get_max_threads()*100 (Node.cpp:420) */
+    int32_t precision;    /* enum ag2_precision */
+    int32_t group_size;   /* particles per walk group (32; reserved for tuning) */
+    int32_t reserved;
+} ag2_params;
+
+typedef struct ag2_ctx ag2_ctx;
+
+/* Defaults: G = 1, e0 = 0.01, theta = 0.5, massInH = 0, split_threshold = 100,
+ * FP32 walk, group_size 32. */
+void ag2_default_params(ag2_params *p);
+
+/* Create a context on the current CUDA device for up to `capacity` particles.
+ * All device memory is allocated here (and grown by ag2_build_tree when the
+ * octree outgrows its node pool). */
+int ag2_create(ag2_ctx **ctx, const ag2_params *params, size_t capacity);
+int ag2_destroy(ag2_ctx *ctx);
+int ag2_set_params(ag2_ctx *ctx, const ag2_params *params);
+int ag2_get_params(const ag2_ctx *ctx, ag2_params *params);
+/* Order all work on `stream` (a cudaStream_t; NULL = the context's own stream). */
+int ag2_set_stream(ag2_ctx *ctx, void *stream);
+const char *ag2_last_error_string(const ag2_ctx *ctx);
+
+/* Copy n particles in: FP64 xyz position/velocity, mass, internal energy U and
+ * type (1 star, 2 gas, 3 dark matter).  vel/U may be NULL (zero).  Clears
+ * acc, dUdt, h, rho, P, T and visualDensity, drops any tree.  The _device
+ * variant takes device pointers. */
+int ag2_upload(ag2_ctx *ctx, size_t n, const double *pos, const double *vel, const double *mass,
+               const double *U, const uint8_t *type);
+int ag2_upload_device(ag2_ctx *ctx, size_t n, const double *pos, const double *vel, const double *mass,
+                      const double *U, const uint8_t *type);
+/* Overwrite one field (host or device buffer) in the original particle order. */
+int ag2_set_field(ag2_ctx *ctx, int field, const double *src, int src_is_device);
+/* Read one field back in the original particle order (host or device buffer). */
+int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
+size_t ag2_count(const ag2_ctx *ctx);
+
+/* Hot path.  The tree is device resident until the next build or upload. */
+int ag2_build_tree(ag2_ctx *ctx);
+int ag2_visual_density(ag2_ctx *ctx, double visualDensityRadius);
+int ag2_sph_density(ag2_ctx *ctx);
+int ag2_forces(ag2_ctx *ctx);
+int ag2_kick(ag2_ctx *ctx, double dt);
+int ag2_drift(ag2_ctx *ctx, double dt);
+int ag2_kick_drift(ag2_ctx *ctx, double dt);
+int ag2_ueuler(ag2_ctx *ctx, double dt);
+int ag2_scale_positions(ag2_ctx *ctx, double factor);
+/* One step of Simulation::run with every particle active at the same dt:
+ * kick+drift, build, [visual density], SPH density, forces, Ueuler (gas),
+ * Hubble factor, kick. */
+int ag2_step(ag2_ctx *ctx, double dt, double hubble_factor, int with_visual_density,
+             double visualDensityRadius);
+
+/* Tree introspection (synchronises). */
+int ag2_root_radius(ag2_ctx *ctx, double *radius);
+int ag2_node_count(ag2_ctx *ctx, int64_t *nodes, int64_t *internal, int32_t *max_depth);
+/* Depth-first preorder export, children in octant order 0..7, same layout as the
+ * checker's orc_topology.  Arrays hold `nodes` entries (any may be NULL); the
+ * particle index is the original upload index. */
+int ag2_topology(ag2_ctx *ctx, int32_t *depth, int32_t *is_leaf, int32_t *particle, int64_t *cp_count,
+                 uint64_t *cp_hash, double *mass, double *com3, double *gas_mass, double *mvel3,
+                 double *center3, double *radius);
+/* Interactions counted by the last ag2_forces: gravity (P2P + accepted nodes)
+ * and SPH pairs. */
+int ag2_interactions(ag2_ctx *ctx, int64_t *gravity, int64_t *sph);
+/* Number of kernels this library launched since the context was created. */
+int64_t ag2_launch_count(const ag2_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
