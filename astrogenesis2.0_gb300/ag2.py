@@ -31,7 +31,8 @@ EXPORTS = [
     "ag2_last_error_string", "ag2_upload", "ag2_upload_device", "ag2_set_field", "ag2_download", "ag2_count",
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
-    "ag2_topology", "ag2_interactions", "ag2_launch_count",
+    "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
+    "ag2_diagnostics", "ag2_fp32_peak_probe",
 ]
 
 
@@ -87,7 +88,11 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_node_count.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                  ctypes.POINTER(ctypes.c_int32)]
     L.ag2_topology.argtypes = [P] * 12
+    L.ag2_particle_node.argtypes = [P, P]
     L.ag2_interactions.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.ag2_direct_sum.argtypes = [P, ctypes.c_size_t, P, P]
+    L.ag2_diagnostics.argtypes = [P, P]
+    L.ag2_fp32_peak_probe.argtypes = [P, dp]
     L.ag2_launch_count.argtypes = [P]
     L.ag2_launch_count.restype = ctypes.c_int64
     _lib = L
@@ -163,10 +168,13 @@ class Context:
                                              v(U_ptr or None), v(type_ptr)))
         self.n = n
 
-    def download(self, field: str) -> np.ndarray:
+    def download(self, field: str, out: np.ndarray | None = None) -> np.ndarray:
         f = FIELDS[field]
         shape = (self.n, 3) if field in VECTOR_FIELDS else (self.n,)
-        out = np.empty(shape, dtype=np.float64)
+        if out is None:
+            out = np.empty(shape, dtype=np.float64)
+        elif out.shape != shape or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape %s" % (shape,))
         self._check(self.L.ag2_download(self.h, f, _ptr(out), 0))
         return out
 
@@ -219,10 +227,31 @@ class Context:
         self._check(self.L.ag2_node_count(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
 
+    def particle_node(self) -> np.ndarray:
+        out = np.empty(self.n, np.int64)
+        self._check(self.L.ag2_particle_node(self.h, _ptr(out)))
+        return out
+
     def interactions(self):
         a, b = ctypes.c_int64(), ctypes.c_int64()
         self._check(self.L.ag2_interactions(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def direct_sum(self, ids) -> np.ndarray:
+        ids = np.ascontiguousarray(ids, np.int64)
+        out = np.empty((ids.size, 3))
+        self._check(self.L.ag2_direct_sum(self.h, ids.size, _ptr(ids), _ptr(out)))
+        return out
+
+    def diagnostics(self) -> dict:
+        out = np.empty(8)
+        self._check(self.L.ag2_diagnostics(self.h, _ptr(out)))
+        return {"mass": out[0], "ekin": out[1], "momentum": out[2:5], "angmom": out[5:8]}
+
+    def fp32_peak_gflops(self) -> float:
+        g = ctypes.c_double()
+        self._check(self.L.ag2_fp32_peak_probe(self.h, ctypes.byref(g)))
+        return g.value
 
     def launches(self) -> int:
         return int(self.L.ag2_launch_count(self.h))

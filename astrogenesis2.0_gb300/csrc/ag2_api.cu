@@ -209,7 +209,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     bool ok = alloc_particles(c, c->st[0], cap) == AG2_OK && alloc_particles(c, c->st[1], cap) == AG2_OK;
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->refnode, cap * 4) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->digit, cap) == cudaSuccess &&
          cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&
@@ -235,7 +235,7 @@ int ag2_destroy(ag2_ctx *c)
     free_particles(c->st[0]);
     free_particles(c->st[1]);
     free_nodes(c->nd);
-    void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->finalnode, c->nodelist, c->digit,
+    void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->finalnode, c->nodelist, c->digit,
                   c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8, c->width_part, c->ctl};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
@@ -424,12 +424,56 @@ int ag2_interactions(ag2_ctx *c, int64_t *g, int64_t *s)
 
 int64_t ag2_launch_count(const ag2_ctx *c) { return c ? c->launches : 0; }
 
+int ag2_direct_sum(ag2_ctx *c, size_t ns, const int64_t *ids, double *out)
+{
+    if (!c || (ns && (!ids || !out))) return AG2_E_INVALID;
+    return run_direct_sum(c, ns, ids, out);
+}
+
+int ag2_diagnostics(ag2_ctx *c, double *out8)
+{
+    if (!c || !out8) return AG2_E_INVALID;
+    return run_diagnostics(c, out8);
+}
+
+int ag2_fp32_peak_probe(ag2_ctx *c, double *gflops)
+{
+    if (!c || !gflops) return AG2_E_INVALID;
+    return run_fma_probe(c, gflops);
+}
+
 static uint64_t id_hash(uint64_t id)
 {
     uint64_t z = id + 1 + 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
+}
+
+int ag2_particle_node(ag2_ctx *c, int64_t *out)
+{
+    if (!c || !out) return AG2_E_INVALID;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
+    const int64_t nn = c->nnodes;
+    const size_t n = c->n;
+    std::vector<int32_t> first(nn), ref(n), id(n);
+    AG2_CUDA(c, cudaMemcpyAsync(first.data(), c->nd.first, nn * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (n) {
+        AG2_CUDA(c, cudaMemcpyAsync(ref.data(), c->refnode, n * 4, cudaMemcpyDeviceToHost, c->stream));
+        AG2_CUDA(c, cudaMemcpyAsync(id.data(), c->S().id, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<int64_t> pre(nn, -1), stack{0};
+    int64_t k = 0;
+    while (!stack.empty()) {
+        int64_t v = stack.back();
+        stack.pop_back();
+        pre[v] = k++;
+        if (first[v] >= 0)
+            for (int o = 7; o >= 0; o--) stack.push_back(first[v] + o);
+    }
+    for (size_t i = 0; i < n; i++) out[id[i]] = ref[i] >= 0 ? pre[ref[i]] : -1;
+    return AG2_OK;
 }
 
 int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle, int64_t *cp_count,

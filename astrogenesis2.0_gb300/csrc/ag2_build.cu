@@ -377,6 +377,32 @@ __global__ void k_reorder(int n, const int32_t *__restrict__ perm, Particles s, 
     d.id[i] = s.id[p];
 }
 
+// Particle::node as the reference leaves it.  A particle lands on a node when
+// it is the first to reach it during serial insertion and keeps the pointer as
+// the node splits and the particle moves down (Node.cpp:621-625, 645-651).  So a
+// leaf particle points at its leaf; a particle that fails the bounds of a
+// serial child keeps pointing at the parent if it was the first (lowest upload
+// index) to reach that parent, and is null otherwise (the parallel root resets
+// every pointer, Node.cpp:472).
+__global__ void k_refnode(int n, Nodes nd, const int32_t *__restrict__ pnode, const int32_t *__restrict__ id,
+                          int32_t *__restrict__ refnode)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t pn = pnode[i];
+    int32_t ref = -1;
+    if (nd.leafpos[pn] == i) {
+        ref = pn;
+    } else if (nd.mode[pn] == MODE_SER && i >= nd.start[pn] + nd.count[pn] - nd.ndrop[pn]) {
+        int32_t X = nd.parent[pn];
+        int32_t b = nd.start[X], e = b + nd.count[X] - nd.ndrop[X];
+        int32_t lo = INT32_MAX;
+        for (int32_t j = b; j < e; j++) lo = min(lo, id[j]);
+        if (id[i] == lo) ref = X;
+    }
+    refnode[i] = ref;
+}
+
 // ---- moments, bottom-up ----------------------------------------------------
 
 struct Sums {
@@ -718,6 +744,7 @@ int build_tree(Ctx *c)
     Particles &dst = c->st[c->cur ^ 1];
     AG2_LAUNCH(c, k_reorder, grid_for(n, kBlock), kBlock, 0, n, c->perm, src, dst);
     c->cur ^= 1;
+    AG2_LAUNCH(c, k_refnode, grid_for(n, kBlock), kBlock, 0, n, c->nd, c->pnode, c->S().id, c->refnode);
 
     // moments, deepest level first
     for (int L = c->max_level; L >= 0; L--) {

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -87,6 +88,7 @@ struct Ctx {
     // build scratch
     int32_t *perm = nullptr, *perm2 = nullptr, *posnode = nullptr, *posnode2 = nullptr;
     int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
+    int32_t *refnode = nullptr;   // the reference's Particle::node per slot (-1 = null)
     int32_t *finalnode = nullptr; // SPH / visual density result node per slot
     int32_t *nodelist = nullptr;  // compacted node list (SPH density nodes)
     uint8_t *digit = nullptr;
@@ -174,6 +176,9 @@ int run_kick_drift(Ctx *c, double dt);
 int run_ueuler(Ctx *c, double dt);
 int run_scale(Ctx *c, double f);
 int sync_ctl(Ctx *c);  // copy ctl to host (synchronises the stream)
+int run_direct_sum(Ctx *c, size_t ns, const int64_t *ids_host, double *out_host);
+int run_diagnostics(Ctx *c, double *out8);
+int run_fma_probe(Ctx *c, double *gflops);
 
 // physical constants of the reference (Constants.h:14-15, Particle.h:40)
 constexpr double kGamma = 5.0 / 3.0;

@@ -31,7 +31,7 @@ namespace {
 constexpr int kBlock = 256;
 
 struct TreeView {
-    const int32_t *start, *count, *ndrop, *parent, *leafpos, *pnode;
+    const int32_t *start, *count, *ndrop, *parent, *leafpos, *pnode, *refnode;
     const int8_t *level;
     const uint8_t *mode;
     const double *mass, *comx, *comy, *comz, *gas;
@@ -46,6 +46,7 @@ TreeView view(Ctx *c)
     t.parent = c->nd.parent;
     t.leafpos = c->nd.leafpos;
     t.pnode = c->pnode;
+    t.refnode = c->refnode;
     t.level = c->nd.level;
     t.mode = c->nd.mode;
     t.mass = c->nd.mass;
@@ -73,8 +74,8 @@ __global__ void k_climb(int n, TreeView t, const uint8_t *type, double M, uint8_
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || type[i] != 2) return;
-    int pn = t.pnode[i];
-    if (pn < 0 || t.leafpos[pn] != i) return;  // no leaf (Particle::node is null)
+    int pn = t.refnode[i];
+    if (pn < 0) return;  // Particle::node is null
     int64_t nd = pn;
     for (;;) {
         double g = t.gas[nd];
@@ -181,8 +182,8 @@ __global__ void k_vclimb(int n, TreeView t, double R, double Rv, uint8_t *flag)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int pn = t.pnode[i];
-    if (pn < 0 || t.leafpos[pn] != i) return;
+    int pn = t.refnode[i];
+    if (pn < 0) return;
     int64_t nd = pn;
     for (;;) {
         int32_t par = t.parent[nd];

@@ -1,0 +1,376 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 force hot path (one JSON line on rank 0).
+
+A step is one pass of the reference's step loop (Simulation.cpp:256-341) over
+the whole workload with every particle active: kick + drift, octree build, SPH
+density, Barnes-Hut walk with in-walk SPH force, Ueuler for gas, kick.  The
+default workload is the 4,194,304-particle galaxy merger (two 2,097,152-particle
+disk galaxies with dark halo, stellar disk and gas) at theta = 0.5, eps = 0.02,
+dt = 1e-3, computed with the FP32-offset walk.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   # the reference's CPU algorithm on host cores
+
+value     particle-steps/s, state resident in HBM, CUDA events on the stream
+e2e       the same metric through the public C-ABI with host (pinned) buffers:
+          every step uploads the particle state and reads it back
+roofline  the walk kernel (FP32 FMA / MUFU bound) against this GPU's measured
+          FP32 FMA throughput
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "astrogenesis2.0_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import ics  # noqa: E402
+
+METRIC = "particle-steps/s, FP32+batched vs plain, at <=1e-4 force error; p99 latency"
+UNIT = "particle-steps/s"
+FLOP_GRAV = 23  # per gravity interaction (P2P or accepted node)
+FLOP_SPH = 60   # per SPH pair
+
+WORKLOADS = {
+    "merger4m": dict(desc="galaxy merger, 2 x 2,097,152 particles (3/4 dark halo, 3/16 stars, 1/16 gas), "
+                          "parabolic orbit r_peri=5 at separation 40, disks inclined 30/60 deg",
+                     make=lambda: ics.merger(2097152, seed=3), e0=0.02, theta=0.5, dt=1e-3),
+    "disk1m": dict(desc="isolated disk galaxy, 786,432 DM + 196,608 stars + 65,536 gas",
+                   make=lambda: ics.disk_galaxy(seed=2), e0=0.02, theta=0.5, dt=1e-3),
+    "plummer16k": dict(desc="Plummer sphere N=16,384, M=1, a=1", make=lambda: ics.plummer(16384, seed=1), e0=0.01,
+                       theta=0.5, dt=1e-3),
+}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+CLOCK_Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+           "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+           "clocks_event_reasons.sw_power_cap")
+
+
+def clocks_start(gpu: int):
+    try:
+        return subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={CLOCK_Q}", "--format=csv,noheader,nounits",
+                                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return None
+
+
+def clocks_stop(p) -> dict:
+    if p is None:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    time.sleep(0.25)
+    p.terminate()
+    try:
+        out, _ = p.communicate(timeout=5)
+    except subprocess.TimeoutExpired:
+        p.kill()
+        out, _ = p.communicate()
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.splitlines():
+        f = [x.strip() for x in line.split(",")]
+        if len(f) < 7:
+            continue
+        try:
+            sm.append(float(f[0]))
+            smax.append(float(f[1]))
+        except ValueError:
+            continue
+        for name, v in zip(names, f[3:7]):
+            if v.lower().startswith("active"):
+                reasons.add(name)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle restatement: test infrastructure, used here only as the
+# timed CPU baseline / reference arm)
+# ---------------------------------------------------------------------------
+def cpu_step_time(d: dict, wl: dict, walk_fraction: int, threads: int, world=None) -> tuple[float, object, str]:
+    """One step of the reference's algorithm on the host: kick+drift, build,
+    gas density, walk for 1/walk_fraction of the particles (time scaled), Ueuler,
+    kick.  Returns (seconds per full step, world, sample description)."""
+    import numpy as np
+
+    import oracle
+
+    n = len(d["mass"])
+    if world is None:
+        world = oracle.World(d["pos"], d["mass"], d["type"], d["vel"], d["U"], kind="port")
+    dt = wl["dt"]
+    idx = np.arange(0, n, walk_fraction, dtype=np.int32)
+    t0 = time.perf_counter()
+    world.kick(dt)
+    world.drift(dt)
+    t1 = time.perf_counter()
+    world.build(threads)
+    if (d["type"] == 2).any():
+        world.gas_density(d.get("massInH", 0.0))
+    t2 = time.perf_counter()
+    world.forces_subset(wl["e0"], wl["theta"], idx, threads)
+    t3 = time.perf_counter()
+    world.ueuler(dt)
+    world.kick(dt)
+    t4 = time.perf_counter()
+    scaled = (t1 - t0) + (t2 - t1) + (t3 - t2) * (n / idx.size) + (t4 - t3)
+    sample = (f"full build + SPH density + kick/drift over all {n} particles, walk for every "
+              f"{walk_fraction}th particle ({idx.size}) scaled by {n / idx.size:.1f}")
+    return scaled, world, sample
+
+
+def reference_arm(args, wl, d):
+    from dist import finalize, init
+
+    D = init(backend="gloo")
+    if D.rank != 0:
+        finalize(D)
+        return
+    threads = os.cpu_count() or 1
+    n = len(d["mass"])
+    world = None
+    times = []
+    for k in range(args.warmup + args.steps):
+        t, world, sample = cpu_step_time(d, wl, args.ref_walk_fraction, threads, world)
+        if k >= args.warmup:
+            times.append(t)
+    per = sum(times) / len(times)
+    value = n / per
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_block(args, wl, d, walk="fp64 recursive walk on host cores", split_threshold=100 * threads),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    finalize(D)
+
+
+L2_BYTES = 129 * 2 ** 20
+BYTES_PER_PARTICLE = 1400  # particle state (~200 B) + ~3.9 nodes of ~300 B
+
+
+def needs_flush(n: int) -> bool:
+    return n * BYTES_PER_PARTICLE < 4 * L2_BYTES
+
+
+def config_block(args, wl, d, walk=None, split_threshold=100):
+    import numpy as np
+
+    n = int(len(d["mass"]))
+    l2 = (f"per-step working set ~{n * BYTES_PER_PARTICLE / 2**30:.1f} GiB, far above the 129 MB L2 (no flush)"
+          if not needs_flush(n) else "L2 flushed (512 MiB write) between timed steps")
+    return {"workload": f"{args.workload}: {wl['desc']}", "particles": n,
+            "gas_particles": int(np.sum(d["type"] == 2)), "theta": wl["theta"], "eps": wl["e0"], "dt": wl["dt"],
+            "G": 1.0, "walk": walk or args.precision, "split_threshold": split_threshold, "parallelism": "replicas",
+            "l2": l2}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def our_arm(args, wl, d):
+    import numpy as np
+    import torch
+
+    import ag2
+    from dist import barrier, finalize, init, max_over_ranks
+
+    D = init()
+    torch.cuda.set_device(D.local_rank)
+    n = len(d["mass"])
+    mih = d.get("massInH", 0.0)
+    ctx = ag2.Context(n, e0=wl["e0"], theta=wl["theta"], massInH=mih, precision=args.precision)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    dt = wl["dt"]
+    # initial forces as Simulation::init does (Simulation.cpp:120-139)
+    ctx.build_tree()
+    ctx.sph_density()
+    ctx.forces()
+
+    walk_ev = []
+
+    def step(ev=None):
+        ctx.kick_drift(dt)
+        ctx.build_tree()
+        ctx.sph_density()
+        if ev is not None:
+            ev[0].record(stream)
+        ctx.forces()
+        if ev is not None:
+            ev[1].record(stream)
+        ctx.ueuler(dt)
+        ctx.kick(dt)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(D)
+    clk = clocks_start(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(D.local_rank)).split(",")[0])
+                       if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else D.local_rank)
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device="cuda") if needs_flush(n) else None
+    l0 = ctx.launches()
+    inter_g = inter_s = 0
+    step_ev = []
+    for _ in range(args.steps):
+        if flush is not None:
+            flush.fill_(1.0)
+        se = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        se[0].record(stream)
+        step(ev)
+        se[1].record(stream)
+        walk_ev.append(ev)
+        step_ev.append(se)
+        g, s = ctx.interactions()
+        inter_g += g
+        inter_s += s
+    torch.cuda.synchronize()
+    barrier(D)
+    clocks = clocks_stop(clk)
+    launches = ctx.launches() - l0
+    t = sum(a.elapsed_time(b) for a, b in step_ev) / 1e3
+    tmax = max_over_ranks(t, D)
+    value = n * args.steps * D.world / tmax
+    walk_ms = [a.elapsed_time(b) for a, b in walk_ev]
+    walk_avg_s = sum(walk_ms) / len(walk_ms) / 1e3
+    flop_per_walk = (FLOP_GRAV * inter_g + FLOP_SPH * inter_s) / args.steps
+    achieved = flop_per_walk / walk_avg_s / 1e12
+    peak = ctx.fp32_peak_gflops() / 1e3
+
+    # plain FP64 walk on the same workload (the reference's arithmetic on the GPU)
+    ctx.set(precision="fp64")
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(args.plain_steps):
+        step()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain = n * args.plain_steps / (p0.elapsed_time(p1) / 1e3)
+    ctx.set(precision=args.precision)
+
+    # force error of both walks against FP64 direct summation on sampled
+    # gravity-only particles (gas particles also carry SPH forces)
+    rng = np.random.default_rng(12345)
+    types = d["type"]
+    cand = np.nonzero(types != 2)[0]
+    ids = np.sort(rng.choice(cand, size=min(args.error_samples, cand.size), replace=False))
+    ctx.build_tree()
+    ctx.sph_density()
+    ctx.forces()
+    a32 = ctx.download("acc")[ids]
+    direct = ctx.direct_sum(ids)
+    ctx.set(precision="fp64")
+    ctx.forces()
+    a64 = ctx.download("acc")[ids]
+    ctx.set(precision=args.precision)
+    nrm = np.maximum(np.linalg.norm(direct, axis=1), 1e-300)
+    err32 = np.linalg.norm(a32 - direct, axis=1) / nrm
+    err64 = np.linalg.norm(a64 - direct, axis=1) / nrm
+
+    # end to end through the C-ABI with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        hpos, hvel, hmass = pin(ctx.download("pos")), pin(ctx.download("vel")), pin(d["mass"])
+        hU, htype, hacc = pin(ctx.download("U")), pin(d["type"]), pin(ctx.download("acc"))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            ctx.upload(hpos, hmass, htype, vel=hvel, U=hU)
+            ctx.set_field("acc", hacc)
+            ctx.step(dt)
+            ctx.download("pos", out=hpos)
+            ctx.download("vel", out=hvel)
+            ctx.download("acc", out=hacc)
+            ctx.download("U", out=hU)
+        te = time.perf_counter() - t0
+        te = max_over_ranks(te, D)
+        e2e = {"value": n * args.e2e_steps * D.world / te, "unit": UNIT,
+               "h2d_bytes_per_step": int(n * (24 + 24 + 8 + 8 + 1 + 24)),
+               "d2h_bytes_per_step": int(n * (24 + 24 + 24 + 8))}
+
+    cpu = None
+    if D.rank == 0 and D.world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        tcpu, _, sample = cpu_step_time(d, wl, args.cpu_walk_fraction, threads)
+        cpu = {"value": n / tcpu, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "walk_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            traffic = tj.get(args.workload, {}).get(args.precision)
+        except (OSError, ValueError):
+            traffic = None
+
+    if D.rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": D.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tmax / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic", "config": config_block(args, wl, d), "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks,
+            "roofline": {"bound": "fp32", "kernel": "k_walk32" if args.precision == "fp32" else "k_walk64",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_source": "measured FP32 FMA throughput (ag2_fp32_peak_probe, "
+                                                            "this run)", "walk_ms": walk_avg_s * 1e3,
+                         "flop_per_launch": flop_per_walk},
+            "cpu_baseline": cpu,
+            "interactions_per_s": (inter_g + inter_s) / args.steps / walk_avg_s,
+            "interactions_per_step": {"gravity": inter_g / args.steps, "sph": inter_s / args.steps},
+            "plain_fp64": {"value": plain, "unit": UNIT, "steps": args.plain_steps},
+            "speedup_vs_plain": value / plain,
+            "force_error": {"against": "FP64 direct summation", "samples": int(ids.size),
+                            "median": float(np.median(err32)), "p99": float(np.quantile(err32, 0.99)),
+                            "p999": float(np.quantile(err32, 0.999)), "fp64_walk_median": float(np.median(err64)),
+                            "fp64_walk_p99": float(np.quantile(err64, 0.99))},
+        }
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    finalize(D)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="merger4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--error-samples", type=int, default=2048)
+    ap.add_argument("--cpu-walk-fraction", type=int, default=8)
+    ap.add_argument("--ref-walk-fraction", type=int, default=32)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    d = wl["make"]()
+    if args.impl == "reference":
+        reference_arm(args, wl, d)
+    else:
+        our_arm(args, wl, d)
+
+
+if __name__ == "__main__":
+    main()

@@ -137,9 +137,23 @@ int ag2_node_count(ag2_ctx *ctx, int64_t *nodes, int64_t *internal, int32_t *max
 int ag2_topology(ag2_ctx *ctx, int32_t *depth, int32_t *is_leaf, int32_t *particle, int64_t *cp_count,
                  uint64_t *cp_hash, double *mass, double *com3, double *gas_mass, double *mvel3,
                  double *center3, double *radius);
+/* For each particle (original upload order): the preorder index, in the
+ * ag2_topology numbering, of the node the reference's Particle::node points at
+ * after the build (its leaf; see Node.cpp:412-413, 621-625), or -1 for null. */
+int ag2_particle_node(ag2_ctx *ctx, int64_t *out);
 /* Interactions counted by the last ag2_forces: gravity (P2P + accepted nodes)
  * and SPH pairs. */
 int ag2_interactions(ag2_ctx *ctx, int64_t *gravity, int64_t *sph);
+/* Diagnostics.  FP64 direct summation with the reference's softened pair law
+ * (Node.cpp:285-305) for `ns` particles given by upload index: out[3k..3k+2] =
+ * acceleration of particle ids[k] due to all others (host buffers).  No
+ * counterpart in the reference beyond its unused, unsoftened
+ * Simulation::calculateForcesWithoutOctree (Simulation.cpp:367-382). */
+int ag2_direct_sum(ag2_ctx *ctx, size_t ns, const int64_t *ids, double *out);
+/* out[0..7] = total mass, kinetic energy, momentum xyz, angular momentum xyz. */
+int ag2_diagnostics(ag2_ctx *ctx, double *out8);
+/* FP32 FMA throughput of this GPU in GFLOP/s (roofline denominator of the walk). */
+int ag2_fp32_peak_probe(ag2_ctx *ctx, double *gflops);
 /* Number of kernels this library launched since the context was created. */
 int64_t ag2_launch_count(const ag2_ctx *ctx);
 

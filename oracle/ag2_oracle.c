@@ -495,6 +495,22 @@ int orc_forces(orc_world *w, double e0, double theta, int threads)
     return 0;
 }
 
+int orc_forces_subset(orc_world *w, double e0, double theta, int threads, int ns, const int32_t *idx)
+{
+    if (!w->root) return -1;
+    if (threads < 1) threads = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+#endif
+    for (int k = 0; k < ns; k++) {
+        int i = idx[k];
+        double *a = w->a + 3 * (size_t)i;
+        a[0] = a[1] = a[2] = 0.0;
+        walk(w, w->root, i, e0, theta, a);
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* SPH density (Tree.cpp:119-150, Node.cpp:722-796)                           */
 /* ------------------------------------------------------------------------- */

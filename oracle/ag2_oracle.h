@@ -60,6 +60,9 @@ int orc_gas_density(orc_world *w, double massInH);
 /* Tree::calculateForces (Tree.cpp:57-83) for every particle (all active). */
 int orc_forces(orc_world *w, double e0, double theta, int threads);
 
+/* The same walk for `ns` particles only (timing samples of the CPU baseline). */
+int orc_forces_subset(orc_world *w, double e0, double theta, int threads, int ns, const int32_t *idx);
+
 /* TimeIntegration (TimeIntegration.cpp:10-40) over all particles. */
 void orc_kick(orc_world *w, double dt);
 void orc_drift(orc_world *w, double dt);

@@ -48,6 +48,7 @@ def load(kind: str = "port") -> ctypes.CDLL:
     L.orc_visual_density.argtypes = [P, D]
     L.orc_gas_density.argtypes = [P, D]
     L.orc_forces.argtypes = [P, D, D, I]
+    L.orc_forces_subset.argtypes = [P, D, D, I, I, P]
     for f in ("orc_kick", "orc_drift", "orc_ueuler", "orc_scale_positions"):
         getattr(L, f).argtypes = [P, D]
         getattr(L, f).restype = None
@@ -113,6 +114,10 @@ class World:
 
     def forces(self, e0: float, theta: float, threads: int = 1):
         self.L.orc_forces(self.h, e0, theta, threads)
+
+    def forces_subset(self, e0: float, theta: float, idx, threads: int = 1):
+        idx = np.ascontiguousarray(idx, np.int32)
+        self.L.orc_forces_subset(self.h, e0, theta, threads, idx.size, _p(idx))
 
     def kick(self, dt):
         self.L.orc_kick(self.h, dt)

@@ -115,6 +115,19 @@ int orc_forces(orc_world *w, double e0, double theta, int)
     return 0;
 }
 
+int orc_forces_subset(orc_world *w, double e0, double theta, int threads, int ns, const int32_t *idx)
+{
+    if (!w->tree) return -1;
+    omp_set_num_threads(threads < 1 ? 1 : threads);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int k = 0; k < ns; k++) {
+        Particle *p = w->sim->particles[idx[k]];
+        p->acc = vec3(0.0, 0.0, 0.0);
+        w->tree->root->calculateGravityForce(p, e0, theta);
+    }
+    return 0;
+}
+
 void orc_kick(orc_world *w, double dt)
 {
     for (Particle *p : w->sim->particles) w->ti.Kick(p, dt);
