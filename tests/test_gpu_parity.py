@@ -230,7 +230,8 @@ def test_edge_cases():
         if n:
             np.testing.assert_allclose(c.download("acc"), w.get("acc"), rtol=1e-12, atol=0)
     # coincident particles: the reference recurses without end; here an error
-    d = {"pos": np.array([[0.1, 0.2, 0.3]] * 3), "mass": np.ones(3), "type": np.ones(3, np.uint8)}
+    pos = np.concatenate([[[0.1, 0.2, 0.3]] * 3, ics.plummer(40, seed=2)["pos"]])
+    d = {"pos": pos, "mass": np.ones(len(pos)), "type": np.ones(len(pos), np.uint8)}
     c = ctx_for(d)
     with pytest.raises(ag2.AG2Error) as ei:
         c.build_tree()
