@@ -32,7 +32,7 @@ EXPORTS = [
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
-    "ag2_diagnostics", "ag2_fp32_peak_probe",
+    "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune",
 ]
 
 
@@ -93,6 +93,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_direct_sum.argtypes = [P, ctypes.c_size_t, P, P]
     L.ag2_diagnostics.argtypes = [P, P]
     L.ag2_fp32_peak_probe.argtypes = [P, dp]
+    L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.ag2_launch_count.argtypes = [P]
     L.ag2_launch_count.restype = ctypes.c_int64
     _lib = L
@@ -252,6 +253,11 @@ class Context:
         g = ctypes.c_double()
         self._check(self.L.ag2_fp32_peak_probe(self.h, ctypes.byref(g)))
         return g.value
+
+    def autotune(self) -> int:
+        v = ctypes.c_int()
+        self._check(self.L.ag2_autotune(self.h, ctypes.byref(v)))
+        return v.value
 
     def launches(self) -> int:
         return int(self.L.ag2_launch_count(self.h))

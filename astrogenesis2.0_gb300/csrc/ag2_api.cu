@@ -159,6 +159,7 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
     AG2_LAUNCH(c, k_unpack, grid_for(n, kBlock), kBlock, 0, (int)n, pos, vel, mass, U, type, c->S(), c->ctl);
     c->n = n;
     c->have_tree = false;
+    c->gas_stats_dirty = true;
     int rc = sync_ctl(c);
     if (rc) return rc;
     if (c->ctl_host->err_code == AG2_E_NAN) return set_err(c, AG2_E_NAN, "non-finite particle position");
@@ -318,7 +319,7 @@ int ag2_set_field(ag2_ctx *c, int f, const double *src, int src_is_device)
     }
     AG2_LAUNCH(c, k_scatter_in, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), f, in);
     if (f == AG2_POS || f == AG2_MASS) c->have_tree = false;
-    if (f == AG2_MASS) c->gas_table_mass = -1.0;
+    if (f == AG2_MASS) c->gas_stats_dirty = true;
     return AG2_OK;
 }
 
@@ -428,6 +429,15 @@ int ag2_direct_sum(ag2_ctx *c, size_t ns, const int64_t *ids, double *out)
 {
     if (!c || (ns && (!ids || !out))) return AG2_E_INVALID;
     return run_direct_sum(c, ns, ids, out);
+}
+
+int ag2_autotune(ag2_ctx *c, int *variant)
+{
+    if (!c || !variant) return AG2_E_INVALID;
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    int rc = run_autotune(c, variant);
+    if (rc) return rc;
+    return check_walk(c);
 }
 
 int ag2_diagnostics(ag2_ctx *c, double *out8)

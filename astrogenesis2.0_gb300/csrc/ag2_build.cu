@@ -21,6 +21,7 @@
 // mass over the whole list), single-particle lists become leaves, and shorter
 // lists are inserted one by one (split when two particles land in-bounds).
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 
@@ -253,7 +254,17 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
         nd.leafpos[nid] = -1;
         return;
     }
-    unsigned long long cb = atomicAdd((unsigned long long *)&ctl->node_count, 8ull);
+    // one atomic per warp for the 8-child blocks of all splitting lanes
+    unsigned long long cb;
+    {
+        unsigned act = __activemask();
+        int lane = lane_id();
+        int leader = __ffs(act) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd((unsigned long long *)&ctl->node_count, 8ull * __popc(act));
+        base = __shfl_sync(act, base, leader);
+        cb = base + 8ull * __popc(act & ((1u << lane) - 1u));
+    }
     if ((int64_t)cb + 8 > node_cap) {
         atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
         nd.first[nid] = -1;
@@ -300,7 +311,12 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
         nneeds += needs;
         s += cc;
     }
-    if (nneeds) atomicAdd(&ctl->next_needs, nneeds);
+    {
+        unsigned act = __activemask();
+        int sum = (int)__reduce_add_sync(act, (unsigned)nneeds);
+        if (lane_id() == __ffs(act) - 1 && sum) atomicAdd(&ctl->next_needs, sum);
+    }
+
 }
 
 __global__ void k_scatter(int n, int64_t base, const int32_t *__restrict__ posnode, const int32_t *__restrict__ perm,
@@ -444,7 +460,19 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= count_lvl) return;
     int64_t nid = base + j;
-    int32_t start = nd.start[nid], cnt = nd.count[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
+    int32_t cnt = nd.count[nid];
+    if (cnt == 0) {
+        // empty child: never visited by the walk (its parent's child mask is 0
+        // there) and never on a particle's path; only the zero moments matter
+        nd.mass[nid] = 0.0;
+        nd.comx[nid] = nd.comy[nid] = nd.comz[nid] = 0.0;
+        nd.gas[nid] = 0.0;
+        nd.mvx[nid] = nd.mvy[nid] = nd.mvz[nid] = 0.0;
+        nd.ngas[nid] = 0;
+        nd.childmask[nid] = 0;
+        return;
+    }
+    int32_t start = nd.start[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
     uint8_t mode = nd.mode[nid];
     int level = nd.level[nid];
     Sums tot, own;  // tot: whole routed range; own: the reference's mass set
@@ -454,6 +482,7 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     if (first >= 0) {
         for (int o = 0; o < 8; o++) {
             int64_t c = first + o;
+            if (nd.count[c] == 0) continue;
             own.add_node(nd, c);
             if (nd.mass[c] != 0.0) cmask |= (uint8_t)(1u << o);
         }
@@ -493,31 +522,36 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
             cz = P.pz[lp];
             gas = isgas ? mp : 0.0;
         } else {
-            // one serial insertion into an empty leaf (Node.cpp:678-698)
-            mass = __dadd_rn(0.0, mp);
+            // one serial insertion into an empty leaf (Node.cpp:678-698): the
+            // running mean (0*(m-m) + x*m)/m, rounded as the reference rounds it
+            mass = mp;
             if (mass != 0.0) {
-                cx = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(P.px[lp], mp)), mass);
-                cy = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(P.py[lp], mp)), mass);
-                cz = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(P.pz[lp], mp)), mass);
+                cx = __ddiv_rn(__dmul_rn(P.px[lp], mp), mass);
+                cy = __ddiv_rn(__dmul_rn(P.py[lp], mp), mass);
+                cz = __ddiv_rn(__dmul_rn(P.pz[lp], mp), mass);
             }
-            gas = isgas ? __dadd_rn(0.0, mp) : 0.0;
+            gas = isgas ? mp : 0.0;
             if (isgas && gas > 0) {
-                mvx = __ddiv_rn(__dmul_rn(P.vx[lp], mp), gas);
-                mvy = __ddiv_rn(__dmul_rn(P.vy[lp], mp), gas);
-                mvz = __ddiv_rn(__dmul_rn(P.vz[lp], mp), gas);
+                // gas velocity of a leaf is only ever read for export (the walk
+                // uses the leaf particle's own velocity, Node.cpp:111-113)
+                mvx = P.vx[lp];
+                mvy = P.vy[lp];
+                mvz = P.vz[lp];
             }
         }
     } else {
         if (mass > 0.0) {
-            cx = own.mx / mass;
-            cy = own.my / mass;
-            cz = own.mz / mass;
+            double im = 1.0 / mass;  // one FP64 division per node
+            cx = own.mx * im;
+            cy = own.my * im;
+            cz = own.mz * im;
         }
         if (gas_uniform) gas = gas_prefix[own.ng];
         if (own.g > 0) {
-            mvx = own.gvx / own.g;
-            mvy = own.gvy / own.g;
-            mvz = own.gvz / own.g;
+            double ig = 1.0 / own.g;
+            mvx = own.gvx * ig;
+            mvy = own.gvy * ig;
+            mvz = own.gvz * ig;
         }
     }
     nd.mass[nid] = mass;
@@ -548,36 +582,37 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
         nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)gas);
 }
 
+// count, min and max mass of the gas particles (grid-wide, order-preserving
+// integer atomics on the positive masses)
 __global__ void k_gas_stats(int n, const double *m, const uint8_t *type, Ctx::Ctl *ctl)
 {
-    __shared__ double smin[kBlock], smax[kBlock];
-    __shared__ int scnt[kBlock];
-    double lo = 1e308, hi = -1e308;
+    long long lo = LLONG_MAX, hi = LLONG_MIN;
     int cnt = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (type[i] == 2) {
-            lo = fmin(lo, m[i]);
-            hi = fmax(hi, m[i]);
+            long long k = okey(m[i]);
+            lo = min(lo, k);
+            hi = max(hi, k);
             cnt++;
         }
     }
-    smin[threadIdx.x] = lo;
-    smax[threadIdx.x] = hi;
-    scnt[threadIdx.x] = cnt;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
-            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
-            scnt[threadIdx.x] += scnt[threadIdx.x + w];
-        }
-        __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
-    if (threadIdx.x == 0) {
-        ctl->gas_mass_min = smin[0];
-        ctl->gas_mass_max = smax[0];
-        ctl->ngas_total = scnt[0];
+    if ((threadIdx.x & 31) == 0 && cnt) {
+        atomicMin((long long *)&ctl->gas_key_min, lo);
+        atomicMax((long long *)&ctl->gas_key_max, hi);
+        atomicAdd(&ctl->ngas_total, cnt);
     }
+}
+
+__global__ void k_gas_stats_init(Ctx::Ctl *ctl)
+{
+    ctl->gas_key_min = LLONG_MAX;
+    ctl->gas_key_max = LLONG_MIN;
+    ctl->ngas_total = 0;
 }
 
 // gasMass of a node whose gas particles all weigh mg: the reference adds them
@@ -644,15 +679,35 @@ static int ensure_hist(Ctx *c, size_t nodes_in_level)
     return AG2_OK;
 }
 
+static double key_to_double(long long k)
+{
+    long long b = k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFLL);
+    double x;
+    std::memcpy(&x, &b, 8);
+    return x;
+}
+
+// Gas statistics depend only on masses and types, so they are refreshed when
+// those change (upload, ag2_set_field of the mass), not every build.
 static int prepare_gas_table(Ctx *c, int n, bool *uniform)
 {
-    Particles &S = c->S();
-    AG2_LAUNCH(c, k_gas_stats, 1, kBlock, 0, n, S.m, S.type, c->ctl);
-    int rc = sync_ctl(c);
-    if (rc) return rc;
-    const Ctx::Ctl &h = *c->ctl_host;
-    *uniform = h.ngas_total > 0 && h.gas_mass_min == h.gas_mass_max;
-    size_t need = (size_t)h.ngas_total + 1;
+    if (c->gas_stats_dirty) {
+        Particles &S = c->S();
+        AG2_LAUNCH(c, k_gas_stats_init, 1, 1, 0, c->ctl);
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        unsigned blocks = std::min(grid_for(n, kBlock), (unsigned)(4 * sms));
+        AG2_LAUNCH(c, k_gas_stats, blocks, kBlock, 0, n, S.m, S.type, c->ctl);
+        int rc = sync_ctl(c);
+        if (rc) return rc;
+        const Ctx::Ctl &h = *c->ctl_host;
+        c->ngas = h.ngas_total;
+        c->gas_mass_min = h.ngas_total ? key_to_double(h.gas_key_min) : 0.0;
+        c->gas_mass_max = h.ngas_total ? key_to_double(h.gas_key_max) : 0.0;
+        c->gas_stats_dirty = false;
+    }
+    *uniform = c->ngas > 0 && c->gas_mass_min == c->gas_mass_max;
+    size_t need = (size_t)c->ngas + 1;
     if (need > c->gas_prefix_cap) {
         if (c->gas_prefix) cudaFree(c->gas_prefix);
         c->gas_prefix = nullptr;
@@ -661,10 +716,10 @@ static int prepare_gas_table(Ctx *c, int n, bool *uniform)
         c->gas_prefix_cap = need;
         c->gas_table_mass = -1.0;
     }
-    if (*uniform && (c->gas_table_mass != h.gas_mass_min || c->gas_table_n != h.ngas_total)) {
-        AG2_LAUNCH(c, k_gas_prefix, 1, 1, 0, h.ngas_total, h.gas_mass_min, c->gas_prefix);
-        c->gas_table_mass = h.gas_mass_min;
-        c->gas_table_n = h.ngas_total;
+    if (*uniform && (c->gas_table_mass != c->gas_mass_min || c->gas_table_n != c->ngas)) {
+        AG2_LAUNCH(c, k_gas_prefix, 1, 1, 0, c->ngas, c->gas_mass_min, c->gas_prefix);
+        c->gas_table_mass = c->gas_mass_min;
+        c->gas_table_n = c->ngas;
     }
     return AG2_OK;
 }

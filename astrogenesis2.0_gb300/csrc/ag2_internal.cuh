@@ -103,7 +103,11 @@ struct Ctx {
     double gas_table_mass = -1.0; // gas particle mass the gasMass table was built for
     int32_t gas_table_n = -1;
     bool gas_uniform = false;
+    bool gas_stats_dirty = true;  // masses or types changed since the last statistics
+    int32_t ngas = 0;
+    double gas_mass_min = 0.0, gas_mass_max = 0.0;
     double tree_theta = 0.0;      // opening angle baked into the walk records
+    int walk_variant = 1;         // FP32 walk register-budget variant (ag2_autotune)
 
     // small device control block
     struct Ctl {
@@ -115,7 +119,7 @@ struct Ctx {
         int32_t any_drop;
         int32_t gas_uniform;
         int32_t ngas_total;
-        double gas_mass_min, gas_mass_max;
+        long long gas_key_min, gas_key_max;
         unsigned long long inter_grav, inter_sph;
         int32_t list_count;
         int32_t pad;
@@ -179,6 +183,7 @@ int sync_ctl(Ctx *c);  // copy ctl to host (synchronises the stream)
 int run_direct_sum(Ctx *c, size_t ns, const int64_t *ids_host, double *out_host);
 int run_diagnostics(Ctx *c, double *out8);
 int run_fma_probe(Ctx *c, double *gflops);
+int run_autotune(Ctx *c, int *chosen);
 
 // physical constants of the reference (Constants.h:14-15, Particle.h:40)
 constexpr double kGamma = 5.0 / 3.0;

@@ -226,7 +226,7 @@ int run_sph_density(Ctx *c)
 {
     if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_sph_density needs a tree (call ag2_build_tree)");
     const int n = (int)c->n;
-    if (n == 0 || c->ctl_host->ngas_total == 0) return AG2_OK;
+    if (n == 0 || c->ngas == 0) return AG2_OK;
     Particles &S = c->S();
     TreeView t = view(c);
     AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
@@ -234,7 +234,7 @@ int run_sph_density(Ctx *c)
     AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->prm.massInH, c->nd.flag);
     AG2_LAUNCH(c, k_final, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->nd.flag, c->finalnode, c->nodelist,
                c->ctl);
-    const int ngas = c->ctl_host->ngas_total;
+    const int ngas = c->ngas;
     AG2_LAUNCH(c, k_rho, grid_for((size_t)ngas * 32, kBlock), kBlock, 0, t, S.px, S.py, S.pz, S.m, S.type,
                c->nodelist, c->ctl, c->root_radius, c->nd.rho);
     AG2_LAUNCH(c, k_assign, grid_for(n, kBlock), kBlock, 0, n, t, c->finalnode, S.type, S.U, c->nd.rho,

@@ -36,6 +36,7 @@ namespace {
 constexpr int kWalkBlock = 128;  // 4 warps
 constexpr int kStack = 512;      // entries per warp
 constexpr float kGuard = 1e-5f;
+constexpr int kWalkVariants = 3;
 
 struct WalkArgs {
     int n;
@@ -301,12 +302,52 @@ __device__ __forceinline__ double warp_max(double v)
     return v;
 }
 
-template <bool kGeneral, bool kGas>
-__global__ void __launch_bounds__(kWalkBlock) k_walk32(WalkArgs a)
+// Rare path of the FP32 walk: an opening test within the guard band of the
+// threshold, or a distance too small for the float offsets, is decided again
+// exactly as the FP64 walk decides it (and such a tiny-distance interaction is
+// evaluated in FP64).  Returns 0 skip, 1 interact in FP32, 2 open, 3 done.
+template <bool kGeneral>
+__device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, double xi, double yi, double zi,
+                                         bool tiny, Vec3<float> &bs, unsigned long long &cnt_g)
 {
-    __shared__ int2 stk_all[(kWalkBlock / 32) * kStack];
+    double ddx = a.comx[c] - xi, ddy = a.comy[c] - yi, ddz = a.comz[c] - zi;
+    double r = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    if (r == 0.0) return 0;
+    int decision = (leaf || ldexp(a.R, -(int)a.level[c]) / r < a.theta) ? 1 : 2;
+    if (decision == 1 && tiny) {
+        double e2 = a.e0 * a.e0;
+        if (!kGeneral || general_eps2(r, a.e0, &e2)) {
+            double sc = a.G * a.mass[c] / (r * r + e2);
+            bs.x += (float)((ddx / r) * sc);
+            bs.y += (float)((ddy / r) * sc);
+            bs.z += (float)((ddz / r) * sc);
+            cnt_g++;
+        }
+        return 3;
+    }
+    return decision;
+}
+
+// Shared-memory layout per warp: the stack, and the staged records of the
+// children being evaluated (relative centre of mass + mass, opening radius^2,
+// first grandchild + child mask, and the SPH record).
+struct alignas(16) WarpSmem {
+    float4 cpos[8];  // com - group centre (lane-invariant part), mass
+    float4 cgas[8];  // gas velocity, gasMass
+    float cmac[8];   // (radius/theta)^2, or -1 for a leaf
+    int cfirst[8];   // first child of the child (-1 leaf)
+    int ccm[8];      // child mask of the child
+    unsigned om[8];  // lanes that open each child
+    int2 stk[kStack];  // (first child of the node to open, lane mask)
+    unsigned char stkcm[kStack];
+};
+
+template <bool kGeneral, bool kGas, int kMinBlocks>
+__global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
+{
+    __shared__ WarpSmem sm_all[kWalkBlock / 32];
     const int lane = threadIdx.x & 31;
-    int2 *stk = stk_all + (threadIdx.x >> 5) * kStack;
+    WarpSmem &W = sm_all[threadIdx.x >> 5];
     const int ngroups = (a.n + 31) >> 5;
     const float G = (float)a.G;
     const float eps02 = (float)(a.e0 * a.e0);
@@ -368,120 +409,110 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk32(WalkArgs a)
         const unsigned all = __ballot_sync(0xffffffffu, valid);
         int sp = 0;
         bool overflow = false;
-
-        // evaluate one node for this lane: returns 0 skip, 1 accepted, 2 open
-        auto eval = [&](int c, const float4 &A, const float4 &B, Vec3<float> &bs, bool in) -> int {
-            if (!in) return 0;
-            const bool leaf = B.w < 0.0f;
-            if (leaf && c == myleaf) return 0;
-            float dx = ((A.x - ghx) + (B.x - glx)) - ox;
-            float dy = ((A.y - ghy) + (B.y - gly)) - oy;
-            float dz = ((A.z - ghz) + (B.z - glz)) - oz;
-            float r2 = dx * dx + dy * dy + dz * dz;
-            int decision;
-            const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * B.w;
-            if (r2 <= tiny || (!leaf && fabsf(r2 - B.w) <= kGuard * B.w)) {
-                // re-decide exactly as the FP64 walk
-                double ddx = a.comx[c] - xi, ddy = a.comy[c] - yi, ddz = a.comz[c] - zi;
-                double r = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
-                if (r == 0.0) return 0;
-                if (leaf)
-                    decision = 1;
-                else
-                    decision = (ldexp(a.R, -(int)a.level[c]) / r < a.theta) ? 1 : 2;
-                if (decision == 2) return 2;
-                if (r2 <= tiny) {
-                    // distance too small for the float offsets: FP64 force
-                    double e2 = a.e0 * a.e0;
-                    if (kGeneral && !general_eps2(r, a.e0, &e2)) return 1;
-                    double s = a.G * a.mass[c] / (r * r + e2);
-                    bs.x += (float)((ddx / r) * s);
-                    bs.y += (float)((ddy / r) * s);
-                    bs.z += (float)((ddz / r) * s);
-                    cnt_g++;
-                    return 1;
-                }
-            } else {
-                decision = (leaf || r2 > B.w) ? 1 : 2;
-                if (decision == 2) return 2;
+        // the root is the only child of a virtual parent (evaluated like any child)
+        if (all && a.mass[0] != 0.0) {
+            if (lane == 0) {
+                W.stk[0] = make_int2(0, (int)all);
+                W.stkcm[0] = 1;
             }
-            const float ir = rsqrtf(r2);
-            float e2 = eps02;
-            if (kGeneral) {
-                double de2;
-                if (!general_eps2((double)(r2 * ir), a.e0, &de2)) return 1;
-                e2 = (float)de2;
-            }
-            const float s = __fdividef(G * A.w * ir, r2 + e2);
-            bs.x += dx * s;
-            bs.y += dy * s;
-            bs.z += dz * s;
-            cnt_g++;
-            if (kGas && gas_i && r2 < h2x4) {
-                const float4 D = a.wD[c];
-                if (D.w > 0.0f) {
-                    sph_pair<float>(D.w, -dx, -dy, -dz, r2 * ir, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs, bs,
-                                    du);
-                    cnt_s++;
-                }
-            }
-            return 1;
-        };
-
-        if (all) {
-            // the root on its own
-            Vec3<float> bs = {0, 0, 0};
-            const float4 A = a.wA[0], B = a.wB[0];
-            int d = (a.mass[0] != 0.0) ? eval(0, A, B, bs, valid) : 0;
-            kahan_add(sx, kx, bs.x);
-            kahan_add(sy, ky, bs.y);
-            kahan_add(sz, kz, bs.z);
-            const unsigned om = __ballot_sync(0xffffffffu, d == 2);
-            if (om) {
-                if (lane == 0) stk[0] = make_int2(0, (int)om);
-                sp = 1;
-            }
+            sp = 1;
         }
         __syncwarp();
-        // stack entries: (parent, lanes) -- evaluate the non-empty children of parent
         while (sp > 0) {
             sp--;
-            const int2 e = stk[sp];
-            __syncwarp();
-            const int p = e.x;
+            const int2 e = W.stk[sp];
+            const unsigned cm = W.stkcm[sp];
+            const int fc = e.x;
             const unsigned msk = (unsigned)e.y;
             const bool in = (msk >> lane) & 1u;
-            const int32_t fc = a.first[p];
-            const unsigned cm = a.childmask[p];
-            Vec3<float> bs = {0, 0, 0};
-            unsigned om[8];
-#pragma unroll
-            for (int o = 0; o < 8; o++) {
-                om[o] = 0;
-                if ((cm >> o) & 1u) {
-                    const int c = fc + o;
-                    const float4 A = a.wA[c];
-                    const float4 B = a.wB[c];
-                    int d = eval(c, A, B, bs, in);
-                    om[o] = __ballot_sync(0xffffffffu, d == 2);
-                }
+            __syncwarp();
+            // stage the children: lane o loads child o (one coalesced 128-byte read per array)
+            if (lane < 8 && ((cm >> lane) & 1u)) {
+                const int c = fc + lane;
+                const float4 A = a.wA[c];
+                const float4 B = a.wB[c];
+                W.cpos[lane] = make_float4((A.x - ghx) + (B.x - glx), (A.y - ghy) + (B.y - gly),
+                                           (A.z - ghz) + (B.z - glz), A.w);
+                W.cmac[lane] = B.w;
+                W.cfirst[lane] = a.first[c];
+                W.ccm[lane] = a.childmask[c];
+            } else if (kGas && lane >= 8 && lane < 16 && ((cm >> (lane - 8)) & 1u)) {
+                W.cgas[lane - 8] = a.wD[fc + lane - 8];
             }
+            __syncwarp();
+            Vec3<float> bs = {0, 0, 0};
+#pragma unroll 1
+            for (int o = 0; o < 8; o++) {
+                if (!((cm >> o) & 1u)) {
+                    if (lane == 0) W.om[o] = 0u;
+                    continue;
+                }
+                const int c = fc + o;
+                bool open = false;
+                if (in) {
+                    const float4 Pc = W.cpos[o];
+                    const float mac = W.cmac[o];
+                    const bool leaf = mac < 0.0f;
+                    const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    int decision = 0;  // 0 skip, 1 interact, 2 open, 3 interacted in FP64
+                    if (!(leaf && c == myleaf)) {
+                        const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
+                        if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
+                            decision = recheck_fp64<kGeneral>(a, c, leaf, xi, yi, zi, r2 <= tiny, bs, cnt_g);
+                        else
+                            decision = (leaf || r2 > mac) ? 1 : 2;
+                    }
+                    if (decision == 2) {
+                        open = true;
+                    } else if (decision == 1) {
+                        const float ir = rsqrtf(r2);
+                        float e2 = eps02;
+                        bool ok = true;
+                        if (kGeneral) {
+                            double de2;
+                            ok = general_eps2((double)(r2 * ir), a.e0, &de2);
+                            e2 = (float)de2;
+                        }
+                        if (ok) {
+                            const float sc = __fdividef(G * Pc.w * ir, r2 + e2);
+                            bs.x += dx * sc;
+                            bs.y += dy * sc;
+                            bs.z += dz * sc;
+                            cnt_g++;
+                            if (kGas && gas_i && r2 < h2x4) {
+                                const float4 D = W.cgas[o];
+                                if (D.w > 0.0f) {
+                                    sph_pair<float>(D.w, -dx, -dy, -dz, r2 * ir, vxi - D.x, vyi - D.y, vzi - D.z,
+                                                    hi_, pr, cs, bs, du);
+                                    cnt_s++;
+                                }
+                            }
+                        }
+                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, open);
+                if (lane == 0) W.om[o] = b;
+            }
+            __syncwarp();
             kahan_add(sx, kx, bs.x);
             kahan_add(sy, ky, bs.y);
             kahan_add(sz, kz, bs.z);
             int npush = 0;
-#pragma unroll
-            for (int o = 0; o < 8; o++) npush += om[o] ? 1 : 0;
+            for (int o = 0; o < 8; o++) npush += W.om[o] ? 1 : 0;
             if (sp + npush > kStack) {
                 overflow = true;
                 break;
             }
-#pragma unroll
-            for (int o = 7; o >= 0; o--)
-                if (om[o]) {
-                    if (lane == 0) stk[sp] = make_int2(fc + o, (int)om[o]);
-                    sp++;
-                }
+            if (lane == 0) {
+                for (int o = 7; o >= 0; o--)
+                    if (W.om[o]) {
+                        W.stk[sp] = make_int2(W.cfirst[o], (int)W.om[o]);
+                        W.stkcm[sp] = (unsigned char)W.ccm[o];
+                        sp++;
+                    }
+            }
+            sp = __shfl_sync(0xffffffffu, sp, 0);
             __syncwarp();
         }
         if (overflow && lane == 0) {
@@ -548,7 +579,7 @@ int run_forces(Ctx *c)
     // The softening law reduces to Plummer softening with e0 whenever the
     // truncated |e| of Node.cpp:302 is 0 for every distance, i.e. e0 < 0.66.
     const bool general = !(c->prm.e0 > 0.0 && c->prm.e0 < 0.6);
-    const bool gas = c->ctl_host->ngas_total > 0;
+    const bool gas = c->ngas > 0;
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->inter_grav, 0, 2 * sizeof(unsigned long long), c->stream));
     int dev_sms = 152;
@@ -564,13 +595,57 @@ int run_forces(Ctx *c)
             if (gas) WALK((k_walk64<false, true>)); else WALK((k_walk64<false, false>));
         }
     } else {
+        // register budget variant (autotuned): 0 = compiler's choice, 1 = 80, 2 = 64
+        const int v = c->walk_variant;
+#define W32(G, S)                                          \
+    do {                                                   \
+        if (v == 1) WALK((k_walk32<G, S, 6>));             \
+        else if (v == 2) WALK((k_walk32<G, S, 8>));        \
+        else WALK((k_walk32<G, S, 1>));                    \
+    } while (0)
         if (general) {
-            if (gas) WALK((k_walk32<true, true>)); else WALK((k_walk32<true, false>));
+            if (gas) W32(true, true); else W32(true, false);
         } else {
-            if (gas) WALK((k_walk32<false, true>)); else WALK((k_walk32<false, false>));
+            if (gas) W32(false, true); else W32(false, false);
         }
+#undef W32
     }
 #undef WALK
+    return AG2_OK;
+}
+
+int run_autotune(Ctx *c, int *chosen)
+{
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_autotune needs a tree (call ag2_build_tree)");
+    if (c->prm.precision != AG2_PREC_FP32 || c->n == 0) {
+        *chosen = c->walk_variant;
+        return AG2_OK;
+    }
+    cudaEvent_t e0, e1;
+    AG2_CUDA(c, cudaEventCreate(&e0));
+    AG2_CUDA(c, cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_v = 0;
+    for (int v = 0; v < kWalkVariants; v++) {
+        c->walk_variant = v;
+        float ms = 0;
+        for (int rep = 0; rep < 2; rep++) {  // first run warms caches
+            AG2_CUDA(c, cudaEventRecord(e0, c->stream));
+            int rc = run_forces(c);
+            if (rc) return rc;
+            AG2_CUDA(c, cudaEventRecord(e1, c->stream));
+            AG2_CUDA(c, cudaEventSynchronize(e1));
+            cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (ms < best) {
+            best = ms;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->walk_variant = best_v;
+    *chosen = best_v;
     return AG2_OK;
 }
 

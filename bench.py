@@ -57,40 +57,62 @@ CLOCK_Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,
            "clocks_event_reasons.sw_power_cap")
 
 
-def clocks_start(gpu: int):
-    try:
-        return subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={CLOCK_Q}", "--format=csv,noheader,nounits",
-                                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-    except OSError:
-        return None
+class ClockSampler:
+    """nvidia-smi sampling every 200 ms, started before the warm-up so that its
+    start-up never overlaps the timed window; only samples taken inside the
+    window [mark_start, mark_stop] are reported."""
 
+    def __init__(self, gpu: int):
+        import threading
 
-def clocks_stop(p) -> dict:
-    if p is None:
-        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-    time.sleep(0.25)
-    p.terminate()
-    try:
-        out, _ = p.communicate(timeout=5)
-    except subprocess.TimeoutExpired:
-        p.kill()
-        out, _ = p.communicate()
-    sm, smax, reasons = [], [], set()
-    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-    for line in out.splitlines():
-        f = [x.strip() for x in line.split(",")]
-        if len(f) < 7:
-            continue
+        self.lines = []
+        self.t0 = self.t1 = None
         try:
-            sm.append(float(f[0]))
-            smax.append(float(f[1]))
-        except ValueError:
-            continue
-        for name, v in zip(names, f[3:7]):
-            if v.lower().startswith("active"):
-                reasons.add(name)
-    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-            "reasons": sorted(reasons), "samples": len(sm)}
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={CLOCK_Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append((time.time(), line))
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time()
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        inside = [l for t, l in self.lines if self.t0 is not None and self.t0 - 0.2 <= t <= (self.t1 or t) + 0.2]
+        for line in inside:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 # ---------------------------------------------------------------------------
@@ -201,6 +223,9 @@ def our_arm(args, wl, d):
     ctx.build_tree()
     ctx.sph_density()
     ctx.forces()
+    variant = ctx.autotune() if args.precision == "fp32" else None
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+    clk = ClockSampler(int(vis) if vis.isdigit() else D.local_rank)
 
     walk_ev = []
 
@@ -220,8 +245,7 @@ def our_arm(args, wl, d):
         step()
     torch.cuda.synchronize()
     barrier(D)
-    clk = clocks_start(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(D.local_rank)).split(",")[0])
-                       if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else D.local_rank)
+    clk.mark_start()
     flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device="cuda") if needs_flush(n) else None
     l0 = ctx.launches()
     inter_g = inter_s = 0
@@ -240,8 +264,9 @@ def our_arm(args, wl, d):
         inter_g += g
         inter_s += s
     torch.cuda.synchronize()
+    clk.mark_stop()
     barrier(D)
-    clocks = clocks_stop(clk)
+    clocks = clk.stop()
     launches = ctx.launches() - l0
     t = sum(a.elapsed_time(b) for a, b in step_ev) / 1e3
     tmax = max_over_ranks(t, D)
@@ -339,6 +364,7 @@ def our_arm(args, wl, d):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic", "config": config_block(args, wl, d), "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks,
+            "walk_variant": variant,
             "roofline": {"bound": "fp32", "kernel": "k_walk32" if args.precision == "fp32" else "k_walk64",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": "measured FP32 FMA throughput (ag2_fp32_peak_probe, "

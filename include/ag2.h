@@ -128,6 +128,11 @@ int ag2_scale_positions(ag2_ctx *ctx, double factor);
 int ag2_step(ag2_ctx *ctx, double dt, double hubble_factor, int with_visual_density,
              double visualDensityRadius);
 
+/* Time the FP32 walk's compiled variants (register budget per thread, hence
+ * warps resident per SM) on the current tree and keep the fastest for later
+ * ag2_forces calls of this context; *variant receives its index. */
+int ag2_autotune(ag2_ctx *ctx, int *variant);
+
 /* Tree introspection (synchronises). */
 int ag2_root_radius(ag2_ctx *ctx, double *radius);
 int ag2_node_count(ag2_ctx *ctx, int64_t *nodes, int64_t *internal, int32_t *max_depth);

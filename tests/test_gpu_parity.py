@@ -229,8 +229,19 @@ def test_edge_cases():
         c.forces()
         if n:
             np.testing.assert_allclose(c.download("acc"), w.get("acc"), rtol=1e-12, atol=0)
-    # coincident particles: the reference recurses without end; here an error
+    # coincident particles off the centre planes: the reference separates nothing
+    # but drops them once the half-width falls below their ulp (depth ~58)
     pos = np.concatenate([[[0.1, 0.2, 0.3]] * 3, ics.plummer(40, seed=2)["pos"]])
+    d = {"pos": pos, "mass": np.ones(len(pos)), "type": np.ones(len(pos), np.uint8)}
+    w = port_world(d)
+    c = ctx_for(d)
+    c.build_tree()
+    assert c.node_count()[0] == w.node_count()
+    assert np.array_equal(c.topology()["cp_hash"], w.topology()["cp_hash"])
+    np.testing.assert_array_equal(c.particle_node(), w.leaf_index())
+    # coincident particles on every centre plane (the origin): the reference's
+    # chain only ends when the half-width underflows (~1075 levels); here an error
+    pos = np.concatenate([[[0.0, 0.0, 0.0]] * 3, ics.plummer(40, seed=2)["pos"]])
     d = {"pos": pos, "mass": np.ones(len(pos)), "type": np.ones(len(pos), np.uint8)}
     c = ctx_for(d)
     with pytest.raises(ag2.AG2Error) as ei:
