@@ -60,12 +60,23 @@ __device__ __forceinline__ double dist0(double x, double y, double z)
 
 // ---- Tree::calcTreeWidth ---------------------------------------------------
 
-// Small N: the reference's sequential sums, bit for bit (Tree.cpp:99-103).
-__global__ void k_width_seq(const double *px, const double *py, const double *pz, int n, Ctx::Ctl *ctl)
+// slot of each particle in the caller's (upload) order: the state is kept in
+// tree order, but the reference sums distances in its particle array order
+__global__ void k_slot_of(int n, const int32_t *__restrict__ id, int32_t *__restrict__ slot_of)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) slot_of[id[i]] = i;
+}
+
+// Small N: the reference's sequential sums in its particle order, bit for bit
+// (Tree.cpp:99-103).
+__global__ void k_width_seq(const double *px, const double *py, const double *pz, const int32_t *slot_of, int n,
+                            Ctx::Ctl *ctl)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double s = 0.0, s2 = 0.0;
-    for (int i = 0; i < n; i++) {
+    for (int k = 0; k < n; k++) {
+        int i = slot_of[k];
         double d = dist0(px[i], py[i], pz[i]);
         s = __dadd_rn(s, d);
         s2 = __dadd_rn(s2, __dmul_rn(d, d));
@@ -74,12 +85,14 @@ __global__ void k_width_seq(const double *px, const double *py, const double *pz
     ctl->sum_d2 = s2;
 }
 
-// Large N: deterministic two-stage FP64 sums.
-__global__ void k_width_partial(const double *px, const double *py, const double *pz, int n, double *part)
+// Large N: deterministic two-stage FP64 sums, also in the caller's order.
+__global__ void k_width_partial(const double *px, const double *py, const double *pz, const int32_t *slot_of, int n,
+                                double *part)
 {
     __shared__ double sh[2][kBlock];
     double s = 0.0, s2 = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int i = slot_of[k];
         double d = dist0(px[i], py[i], pz[i]);
         s += d;
         s2 += d * d;
@@ -735,10 +748,11 @@ int build_tree(Ctx *c)
 
     // root half-width
     if (n > 0) {
+        AG2_LAUNCH(c, k_slot_of, grid_for(n, kBlock), kBlock, 0, n, S.id, c->slot_of);
         if (n <= kSeqWidthMax) {
-            AG2_LAUNCH(c, k_width_seq, 1, 1, 0, S.px, S.py, S.pz, n, c->ctl);
+            AG2_LAUNCH(c, k_width_seq, 1, 1, 0, S.px, S.py, S.pz, c->slot_of, n, c->ctl);
         } else {
-            AG2_LAUNCH(c, k_width_partial, kWidthBlocks, kBlock, 0, S.px, S.py, S.pz, n, c->width_part);
+            AG2_LAUNCH(c, k_width_partial, kWidthBlocks, kBlock, 0, S.px, S.py, S.pz, c->slot_of, n, c->width_part);
             AG2_LAUNCH(c, k_width_final, 1, 32, 0, c->width_part, kWidthBlocks, c->ctl);
         }
         AG2_LAUNCH(c, k_width_thr, 1, 32, 0, n, c->ctl);

@@ -89,6 +89,7 @@ struct Ctx {
     int32_t *perm = nullptr, *perm2 = nullptr, *posnode = nullptr, *posnode2 = nullptr;
     int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
     int32_t *refnode = nullptr;   // the reference's Particle::node per slot (-1 = null)
+    int32_t *slot_of = nullptr;   // tree-order slot of each upload index
     int32_t *finalnode = nullptr; // SPH / visual density result node per slot
     int32_t *nodelist = nullptr;  // compacted node list (SPH density nodes)
     uint8_t *digit = nullptr;

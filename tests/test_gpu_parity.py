@@ -190,6 +190,30 @@ def test_full_steps_match_port():
         assert np.max(np.abs(a - b)) <= tol * scale, k
 
 
+def test_root_radius_after_reordering_builds():
+    """The state is kept in tree order between builds; the root half-width must
+    still be summed in the caller's particle order (Tree.cpp:99-103)."""
+    for n in (3000, 70000):
+        d = ics.plummer(n, seed=12)
+        c = ctx_for(d)
+        w = oracle.World(d["pos"], d["mass"], d["type"], d["vel"], kind="port")
+        for _ in range(3):
+            c.build_tree()
+            c.forces()
+            c.kick_drift(1e-3)
+            w.build(1)
+            w.forces(0.01, 0.5, os.cpu_count() or 1)
+            w.kick(1e-3)
+            w.drift(1e-3)
+        c.set_field("pos", w.get("pos"))
+        c.build_tree()
+        w.build(1)
+        if n <= 32768:
+            assert c.root_radius() == w.root_radius()
+        else:
+            assert c.root_radius() == pytest.approx(w.root_radius(), rel=1e-15)
+
+
 def test_large_properties():
     """1M Plummer sphere: node-count identity, one leaf per particle, FP32 walk
     against FP64 walk."""
