@@ -437,10 +437,22 @@ __global__ void k_refnode(int n, Nodes nd, const int32_t *__restrict__ pnode, co
 struct Sums {
     double m, mx, my, mz, g, gvx, gvy, gvz;
     int32_t ng;
-    __device__ void zero() { m = mx = my = mz = g = gvx = gvy = gvz = 0.0; ng = 0; }
+    int32_t first_id;     // lowest upload index in the set (the first one serial insertion sees)
+    double first_m;       // its mass
+    __device__ void zero()
+    {
+        m = mx = my = mz = g = gvx = gvy = gvz = 0.0;
+        ng = 0;
+        first_id = INT32_MAX;
+        first_m = 1.0;
+    }
     __device__ void add_particle(const Particles &P, int i)
     {
         double mi = P.m[i];
+        if (P.id[i] < first_id) {
+            first_id = P.id[i];
+            first_m = mi;
+        }
         m += mi;
         mx += P.px[i] * mi;
         my += P.py[i] * mi;
@@ -455,6 +467,10 @@ struct Sums {
     }
     __device__ void add_node(const Nodes &nd, int64_t c)
     {
+        if (nd.tfirst[c] < first_id) {
+            first_id = nd.tfirst[c];
+            first_m = nd.tfirstm[c];
+        }
         m += nd.tm[c];
         mx += nd.tmx[c];
         my += nd.tmy[c];
@@ -519,6 +535,8 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     nd.tgvy[nid] = tot.gvy;
     nd.tgvz[nid] = tot.gvz;
     nd.tng[nid] = tot.ng;
+    nd.tfirst[nid] = tot.first_id;
+    nd.tfirstm[nid] = tot.first_m;
     nd.childmask[nid] = cmask;
 
     double mass = own.m, cx = 0.0, cy = 0.0, cz = 0.0, gas = own.g, mvx = 0.0, mvy = 0.0, mvz = 0.0;
@@ -553,7 +571,13 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
             }
         }
     } else {
-        if (mass > 0.0) {
+        const bool serial = (mode == MODE_SER || mode == MODE_SER_ENTRY);
+        if (serial && own.first_m == 0.0 && own.first_id != INT32_MAX) {
+            // serial insertion's running mean starts with (0*0 + x*0)/0 when the
+            // first particle to arrive is massless (Node.cpp:698): the centre of
+            // mass is NaN from then on, so the node is always opened
+            cx = cy = cz = __longlong_as_double(0x7ff8000000000000LL);
+        } else if (mass > 0.0) {
             double im = 1.0 / mass;  // one FP64 division per node
             cx = own.mx * im;
             cy = own.my * im;
@@ -670,7 +694,8 @@ int ensure_node_capacity(Ctx *c, size_t need)
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
     G(cx) G(cy) G(cz) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
-    G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(wA) G(wB) G(wD) G(flag) G(rho)
+    G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(tfirst) G(tfirstm) G(wA) G(wB) G(wD) G(flag)
+    G(rho)
 #undef G
     if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;
     c->node_cap = nc;

@@ -55,6 +55,8 @@ struct Nodes {
     // sums over the whole routed range (bottom-up helper)
     double *tm, *tmx, *tmy, *tmz, *tg, *tgvx, *tgvy, *tgvz;
     int32_t *tng;
+    int32_t *tfirst;     // lowest upload index in the routed range
+    double *tfirstm;     // its mass
     // walk records (FP32 view)
     float4 *wA;  // com_hi.xyz, mass
     float4 *wB;  // com_lo.xyz, mac radius^2 (leaf: -1)
