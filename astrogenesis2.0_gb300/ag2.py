@@ -32,7 +32,7 @@ EXPORTS = [
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
-    "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune",
+    "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc",
 ]
 
 
@@ -94,6 +94,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_diagnostics.argtypes = [P, P]
     L.ag2_fp32_peak_probe.argtypes = [P, dp]
     L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
+    L.ag2_root_radius_noalloc.argtypes = [P, ctypes.c_int64, P, P]
     L.ag2_launch_count.argtypes = [P]
     L.ag2_launch_count.restype = ctypes.c_int64
     _lib = L

@@ -159,6 +159,22 @@ int ag2_direct_sum(ag2_ctx *ctx, size_t ns, const int64_t *ids, double *out);
 int ag2_diagnostics(ag2_ctx *ctx, double *out8);
 /* FP32 FMA throughput of this GPU in GFLOP/s (roofline denominator of the walk). */
 int ag2_fp32_peak_probe(ag2_ctx *ctx, double *gflops);
+/* Allocation-free root half-width.  No counterpart in the reference: it computes
+ * the same quantity as ag2_root_radius (Tree::calcTreeWidth) for callers that
+ * cannot allocate device memory, such as a host code that has reserved the
+ * GPU's memory for its own pools or code in the middle of capturing a CUDA
+ * stream into a graph.  The caller passes device buffers: pos holds n
+ * xyz-interleaved doubles, radius receives one double; the work is enqueued on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) and nothing is
+ * allocated.  Scratch space is a fixed 16 KiB array inside this library on each
+ * device that uses it, kept until the process exits.  The first call on a
+ * device looks up that array's address (make it before any stream capture).
+ * Calls that overlap on the GPU share the array and race.  n must lie in
+ * 1..AG2_NOALLOC_MAX_PARTICLES; larger n returns AG2_E_CAPACITY and launches
+ * nothing. */
+#define AG2_NOALLOC_MAX_PARTICLES 2147483647
+int ag2_root_radius_noalloc(const double *pos, int64_t n, double *radius, void *stream);
+
 /* Number of kernels this library launched since the context was created. */
 int64_t ag2_launch_count(const ag2_ctx *ctx);
 
