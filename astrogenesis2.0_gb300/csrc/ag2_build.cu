@@ -359,24 +359,54 @@ __global__ void k_scatter(int n, int64_t base, const int32_t *__restrict__ posno
 }
 
 // Out-of-bounds tails are the only ranges whose order the partition leaves
-// open; put them in upload order so the build is deterministic.
-__global__ void k_sort_drops(int64_t nnodes, Nodes nd, int32_t *perm, const int32_t *id)
+// open; put them in upload order so the build is deterministic.  One block per
+// node with a tail of two or more: bitonic sort of (upload index, slot) pairs in
+// shared memory (tails up to kDropSort), or a block-strided rank sort for longer
+// tails.
+constexpr int kDropSort = 4096;
+
+__global__ void k_sort_drops(int64_t nnodes, Nodes nd, int32_t *perm, const int32_t *id, int32_t *scratch)
 {
-    int64_t nid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (nid >= nnodes) return;
-    int32_t nd8 = nd.ndrop[nid];
-    if (nd8 < 2) return;
-    int32_t e = nd.start[nid] + nd.count[nid];
-    int32_t b = e - nd8;
-    for (int32_t i = b + 1; i < e; i++) {
-        int32_t v = perm[i];
-        int32_t key = id[v];
-        int32_t j = i - 1;
-        while (j >= b && id[perm[j]] > key) {
-            perm[j + 1] = perm[j];
-            j--;
+    __shared__ long long key[kDropSort];
+    for (int64_t nid = blockIdx.x; nid < nnodes; nid += gridDim.x) {
+        const int32_t nd8 = nd.ndrop[nid];
+        if (nd8 < 2) continue;
+        const int32_t e = nd.start[nid] + nd.count[nid];
+        const int32_t b = e - nd8;
+        if (nd8 <= kDropSort) {
+            int m = 1;
+            while (m < nd8) m <<= 1;
+            for (int t = threadIdx.x; t < m; t += blockDim.x)
+                key[t] = t < nd8 ? (((long long)id[perm[b + t]]) << 32) | (unsigned)perm[b + t] : LLONG_MAX;
+            __syncthreads();
+            for (int k = 2; k <= m; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+                        int u = t ^ j;
+                        if (u > t) {
+                            bool up = (t & k) == 0;
+                            long long x = key[t], y = key[u];
+                            if ((x > y) == up) {
+                                key[t] = y;
+                                key[u] = x;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (int t = threadIdx.x; t < nd8; t += blockDim.x) perm[b + t] = (int32_t)(key[t] & 0xffffffffLL);
+            __syncthreads();
+        } else {
+            // rank of each element by its upload index (all distinct), O(k^2 / threads)
+            for (int t = threadIdx.x; t < nd8; t += blockDim.x) {
+                int32_t v = perm[b + t], kv = id[v], r = 0;
+                for (int u = 0; u < nd8; u++) r += id[perm[b + u]] < kv ? 1 : 0;
+                scratch[b + r] = v;
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < nd8; t += blockDim.x) perm[b + t] = scratch[b + t];
+            __syncthreads();
         }
-        perm[j + 1] = v;
     }
 }
 
@@ -830,8 +860,11 @@ int build_tree(Ctx *c)
     c->max_level = (int)c->level_base.size() - 2;
     c->nnodes = c->level_base.back();
     c->ninternal = (c->nnodes - 1) / 8;
-    if (c->ctl_host->any_drop)
-        AG2_LAUNCH(c, k_sort_drops, grid_for((size_t)c->nnodes, kBlock), kBlock, 0, c->nnodes, c->nd, c->perm, S.id);
+    if (c->ctl_host->any_drop) {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        AG2_LAUNCH(c, k_sort_drops, (unsigned)(4 * sms), kBlock, 0, c->nnodes, c->nd, c->perm, S.id, c->perm2);
+    }
 
     // particle state into tree order
     Particles &src = c->st[c->cur];

@@ -302,6 +302,61 @@ __device__ __forceinline__ double warp_max(double v)
     return v;
 }
 
+// Shared-memory layout per warp: the stack, the batch of up to 32 children
+// being decided (staged one per lane), and the interaction list (accepted node
+// + the lanes that accepted it) that the force loop consumes.
+constexpr int kBatch = 32;
+constexpr int kList = 96;
+struct alignas(16) WarpSmem {
+    float4 cpos[kBatch];     // com - group centre (lane-invariant part), mass
+    float4 cgas[kBatch];     // gas velocity, gasMass
+    float cmac[kBatch];      // (radius/theta)^2, or -1 for a leaf
+    int cfirst[kBatch];      // first child of the child (-1 leaf)
+    int bchild[kBatch];      // node index of batch slot j
+    unsigned bmask[kBatch];  // lanes that evaluate batch slot j
+    unsigned char ccm[kBatch];  // child mask of the child
+    float4 lpos[kList];      // accepted nodes: relative com, mass
+    unsigned lmask[kList];   // lanes that accepted them
+    int2 stk[kStack];        // (first child of a node to open, lane mask)
+    unsigned char stkcm[kStack];
+};
+
+// Force loop over the interaction list: every lane evaluates every entry and
+// keeps it when its bit is set (predicated, no branches), summing into a batch
+// that is added to the compensated accumulator once per flush.
+template <bool kGeneral>
+__device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane, float ox, float oy, float oz,
+                                           float G, float eps02, double e0, float &sx, float &sy, float &sz, float &kx,
+                                           float &ky, float &kz, unsigned long long &cnt_g)
+{
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    int mine = 0;
+#pragma unroll 4
+    for (int j = 0; j < cnt; j++) {
+        const float4 P = W.lpos[j];
+        const bool take = (W.lmask[j] >> lane) & 1u;
+        const float dx = P.x - ox, dy = P.y - oy, dz = P.z - oz;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float ir = rsqrtf(r2);
+        float e2 = eps02;
+        if (kGeneral) {
+            double de2 = 0.0;
+            if (take && general_eps2((double)(r2 * ir), e0, &de2))
+                e2 = (float)de2;
+        }
+        float sc = __fdividef(G * P.w * ir, r2 + e2);
+        sc = take ? sc : 0.f;
+        bx = fmaf(dx, sc, bx);
+        by = fmaf(dy, sc, by);
+        bz = fmaf(dz, sc, bz);
+        mine += take ? 1 : 0;
+    }
+    kahan_add(sx, kx, bx);
+    kahan_add(sy, ky, by);
+    kahan_add(sz, kz, bz);
+    cnt_g += (unsigned long long)mine;
+}
+
 // Rare path of the FP32 walk: an opening test within the guard band of the
 // threshold, or a distance too small for the float offsets, is decided again
 // exactly as the FP64 walk decides it (and such a tiny-distance interaction is
@@ -327,20 +382,6 @@ __device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, do
     }
     return decision;
 }
-
-// Shared-memory layout per warp: the stack, and the staged records of the
-// children being evaluated (relative centre of mass + mass, opening radius^2,
-// first grandchild + child mask, and the SPH record).
-struct alignas(16) WarpSmem {
-    float4 cpos[8];  // com - group centre (lane-invariant part), mass
-    float4 cgas[8];  // gas velocity, gasMass
-    float cmac[8];   // (radius/theta)^2, or -1 for a leaf
-    int cfirst[8];   // first child of the child (-1 leaf)
-    int ccm[8];      // child mask of the child
-    unsigned om[8];  // lanes that open each child
-    int2 stk[kStack];  // (first child of the node to open, lane mask)
-    unsigned char stkcm[kStack];
-};
 
 template <bool kGeneral, bool kGas, int kMinBlocks>
 __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
@@ -405,11 +446,12 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         }
         const float h2x4 = 4.0f * hi_ * hi_;
         float sx = 0, sy = 0, sz = 0, kx = 0, ky = 0, kz = 0;  // Kahan sums
+        Vec3<float> side = {0, 0, 0};  // SPH and FP64-path contributions
         float du = 0;
         const unsigned all = __ballot_sync(0xffffffffu, valid);
-        int sp = 0;
+        int sp = 0, nl = 0;
         bool overflow = false;
-        // the root is the only child of a virtual parent (evaluated like any child)
+        // the root is the only child of a virtual parent (decided like any child)
         if (all && a.mass[0] != 0.0) {
             if (lane == 0) {
                 W.stk[0] = make_int2(0, (int)all);
@@ -419,102 +461,97 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         }
         __syncwarp();
         while (sp > 0) {
-            sp--;
-            const int2 e = W.stk[sp];
-            const unsigned cm = W.stkcm[sp];
-            const int fc = e.x;
-            const unsigned msk = (unsigned)e.y;
-            const bool in = (msk >> lane) & 1u;
+            // gather up to 32 children from the top stack entries
+            int nc = 0;
+            if (lane == 0) {
+                while (sp > 0) {
+                    const unsigned cm = W.stkcm[sp - 1];
+                    const int k = __popc(cm);
+                    if (nc + k > kBatch) break;
+                    sp--;
+                    const int2 e = W.stk[sp];
+                    for (int o = 0; o < 8; o++)
+                        if ((cm >> o) & 1u) {
+                            W.bchild[nc] = e.x + o;
+                            W.bmask[nc] = (unsigned)e.y;
+                            nc++;
+                        }
+                }
+            }
+            nc = __shfl_sync(0xffffffffu, nc, 0);
+            sp = __shfl_sync(0xffffffffu, sp, 0);
             __syncwarp();
-            // stage the children: lane o loads child o (one coalesced 128-byte read per array)
-            if (lane < 8 && ((cm >> lane) & 1u)) {
-                const int c = fc + lane;
+            // stage: lane j loads batch slot j (one round trip for the batch)
+            if (lane < nc) {
+                const int c = W.bchild[lane];
                 const float4 A = a.wA[c];
                 const float4 B = a.wB[c];
+                const int f = a.first[c];
+                const unsigned char ccm = a.childmask[c];
+                float4 D;
+                if (kGas) D = a.wD[c];
                 W.cpos[lane] = make_float4((A.x - ghx) + (B.x - glx), (A.y - ghy) + (B.y - gly),
                                            (A.z - ghz) + (B.z - glz), A.w);
                 W.cmac[lane] = B.w;
-                W.cfirst[lane] = a.first[c];
-                W.ccm[lane] = a.childmask[c];
-            } else if (kGas && lane >= 8 && lane < 16 && ((cm >> (lane - 8)) & 1u)) {
-                W.cgas[lane - 8] = a.wD[fc + lane - 8];
+                W.cfirst[lane] = f;
+                W.ccm[lane] = ccm;
+                if (kGas) W.cgas[lane] = D;
             }
             __syncwarp();
-            Vec3<float> bs = {0, 0, 0};
 #pragma unroll 1
-            for (int o = 0; o < 8; o++) {
-                if (!((cm >> o) & 1u)) {
-                    if (lane == 0) W.om[o] = 0u;
-                    continue;
-                }
-                const int c = fc + o;
-                bool open = false;
-                if (in) {
-                    const float4 Pc = W.cpos[o];
-                    const float mac = W.cmac[o];
+            for (int j = 0; j < nc; j++) {
+                const int c = W.bchild[j];
+                const bool in = (W.bmask[j] >> lane) & 1u;
+                int decision = 0;  // 0 skip, 1 accept (FP32 list), 2 open, 3 done in FP64
+                const float4 Pc = W.cpos[j];
+                if (in && c != myleaf) {
+                    const float mac = W.cmac[j];
                     const bool leaf = mac < 0.0f;
                     const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
                     const float r2 = dx * dx + dy * dy + dz * dz;
-                    int decision = 0;  // 0 skip, 1 interact, 2 open, 3 interacted in FP64
-                    if (!(leaf && c == myleaf)) {
-                        const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
-                        if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
-                            decision = recheck_fp64<kGeneral>(a, c, leaf, xi, yi, zi, r2 <= tiny, bs, cnt_g);
-                        else
-                            decision = (leaf || r2 > mac) ? 1 : 2;
-                    }
-                    if (decision == 2) {
-                        open = true;
-                    } else if (decision == 1) {
-                        const float ir = rsqrtf(r2);
-                        float e2 = eps02;
-                        bool ok = true;
-                        if (kGeneral) {
-                            double de2;
-                            ok = general_eps2((double)(r2 * ir), a.e0, &de2);
-                            e2 = (float)de2;
-                        }
-                        if (ok) {
-                            const float sc = __fdividef(G * Pc.w * ir, r2 + e2);
-                            bs.x += dx * sc;
-                            bs.y += dy * sc;
-                            bs.z += dz * sc;
-                            cnt_g++;
-                            if (kGas && gas_i && r2 < h2x4) {
-                                const float4 D = W.cgas[o];
-                                if (D.w > 0.0f) {
-                                    sph_pair<float>(D.w, -dx, -dy, -dz, r2 * ir, vxi - D.x, vyi - D.y, vzi - D.z,
-                                                    hi_, pr, cs, bs, du);
-                                    cnt_s++;
-                                }
-                            }
+                    const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
+                    if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
+                        decision = recheck_fp64<kGeneral>(a, c, leaf, xi, yi, zi, r2 <= tiny, side, cnt_g);
+                    else
+                        decision = (leaf || r2 > mac) ? 1 : 2;
+                    if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) {
+                        const float4 D = W.cgas[j];
+                        if (D.w > 0.0f) {
+                            const float r = sqrtf(r2);
+                            sph_pair<float>(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs, side,
+                                            du);
+                            cnt_s++;
                         }
                     }
                 }
-                const unsigned b = __ballot_sync(0xffffffffu, open);
-                if (lane == 0) W.om[o] = b;
-            }
-            __syncwarp();
-            kahan_add(sx, kx, bs.x);
-            kahan_add(sy, ky, bs.y);
-            kahan_add(sz, kz, bs.z);
-            int npush = 0;
-            for (int o = 0; o < 8; o++) npush += W.om[o] ? 1 : 0;
-            if (sp + npush > kStack) {
-                overflow = true;
-                break;
-            }
-            if (lane == 0) {
-                for (int o = 7; o >= 0; o--)
-                    if (W.om[o]) {
-                        W.stk[sp] = make_int2(W.cfirst[o], (int)W.om[o]);
-                        W.stkcm[sp] = (unsigned char)W.ccm[o];
-                        sp++;
+                const unsigned am = __ballot_sync(0xffffffffu, decision == 1);
+                const unsigned om = __ballot_sync(0xffffffffu, decision == 2);
+                if (om && sp >= kStack) overflow = true;
+                if (lane == 0) {
+                    if (am) {
+                        W.lpos[nl] = Pc;
+                        W.lmask[nl] = am;
                     }
+                    if (om && sp < kStack) {
+                        W.stk[sp] = make_int2(W.cfirst[j], (int)om);
+                        W.stkcm[sp] = W.ccm[j];
+                    }
+                }
+                nl += am ? 1 : 0;
+                sp += (om && sp < kStack) ? 1 : 0;
             }
-            sp = __shfl_sync(0xffffffffu, sp, 0);
             __syncwarp();
+            if (overflow) break;
+            if (nl > kList - kBatch) {
+                flush_list<kGeneral>(W, nl, lane, ox, oy, oz, G, eps02, a.e0, sx, sy, sz, kx, ky, kz, cnt_g);
+                nl = 0;
+                __syncwarp();
+            }
         }
+        if (nl > 0) flush_list<kGeneral>(W, nl, lane, ox, oy, oz, G, eps02, a.e0, sx, sy, sz, kx, ky, kz, cnt_g);
+        kahan_add(sx, kx, side.x);
+        kahan_add(sy, ky, side.y);
+        kahan_add(sz, kz, side.z);
         if (overflow && lane == 0) {
             atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
             atomicExch(&a.ctl->err_info, grp);
