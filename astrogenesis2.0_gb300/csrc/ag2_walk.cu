@@ -315,8 +315,11 @@ struct alignas(16) WarpSmem {
     int bchild[kBatch];      // node index of batch slot j
     unsigned bmask[kBatch];  // lanes that evaluate batch slot j
     unsigned char ccm[kBatch];  // child mask of the child
+    unsigned char ccls[kBatch]; // group-level class: 0 per-lane, 1 every lane opens, 2 every lane accepts
+    unsigned cself[kBatch];     // lane whose own leaf this child is (bit), else 0
     float4 lpos[kList];      // accepted nodes: relative com, mass
     unsigned lmask[kList];   // lanes that accepted them
+    double xd[3][32];        // FP64 positions of the group (read only by the exact re-check)
     int2 stk[kStack];        // (first child of a node to open, lane mask)
     unsigned char stkcm[kStack];
 };
@@ -362,9 +365,10 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
 // exactly as the FP64 walk decides it (and such a tiny-distance interaction is
 // evaluated in FP64).  Returns 0 skip, 1 interact in FP32, 2 open, 3 done.
 template <bool kGeneral>
-__device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, double xi, double yi, double zi,
+__device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, const double (*xd)[32], int lane,
                                          bool tiny, Vec3<float> &bs, unsigned long long &cnt_g)
 {
+    const double xi = xd[0][lane], yi = xd[1][lane], zi = xd[2][lane];
     double ddx = a.comx[c] - xi, ddy = a.comy[c] - yi, ddz = a.comz[c] - zi;
     double r = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
     if (r == 0.0) return 0;
@@ -400,15 +404,22 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         if (grp >= ngroups) break;
         const int i = grp * 32 + lane;
         const bool valid = i < a.n && a.m[i] != 0.0;
-        double xi = 0, yi = 0, zi = 0;
-        if (i < a.n) {
-            xi = a.px[i];
-            yi = a.py[i];
-            zi = a.pz[i];
-        }
-        // group centre: middle of the bounding box of the valid lanes
-        double gx = 0, gy = 0, gz = 0;
+        // Group set-up in FP64 (positions, group centre, float offsets).  No FP64
+        // value stays live past this block: on this part FP64 instructions issue
+        // at 1/64 of the FP32 rate, so the compiler must not be able to
+        // re-derive the float offsets from doubles inside the walk.
+        float ghx, ghy, ghz, glx, gly, glz, ox, oy, oz;
         {
+            double xi = 0, yi = 0, zi = 0;
+            if (i < a.n) {
+                xi = a.px[i];
+                yi = a.py[i];
+                zi = a.pz[i];
+            }
+            W.xd[0][lane] = xi;
+            W.xd[1][lane] = yi;
+            W.xd[2][lane] = zi;
+            double gx = 0, gy = 0, gz = 0;
             double lx = valid ? xi : 1e300, ly = valid ? yi : 1e300, lz = valid ? zi : 1e300;
             double ux = valid ? xi : -1e300, uy = valid ? yi : -1e300, uz = valid ? zi : -1e300;
             lx = warp_min(lx);
@@ -422,11 +433,19 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 gy = 0.5 * (ly + uy);
                 gz = 0.5 * (lz + uz);
             }
+            ghx = (float)gx;
+            ghy = (float)gy;
+            ghz = (float)gz;
+            glx = (float)(gx - (double)ghx);
+            gly = (float)(gy - (double)ghy);
+            glz = (float)(gz - (double)ghz);
+            ox = (float)(xi - gx);
+            oy = (float)(yi - gy);
+            oz = (float)(zi - gz);
+            // opaque copies: the walk below sees plain floats
+            asm volatile("" : "+f"(ghx), "+f"(ghy), "+f"(ghz), "+f"(glx), "+f"(gly), "+f"(glz));
+            asm volatile("" : "+f"(ox), "+f"(oy), "+f"(oz));
         }
-        const float ghx = (float)gx, ghy = (float)gy, ghz = (float)gz;
-        const float glx = (float)(gx - (double)ghx), gly = (float)(gy - (double)ghy),
-                    glz = (float)(gz - (double)ghz);
-        const float ox = (float)(xi - gx), oy = (float)(yi - gy), oz = (float)(zi - gz);
         int myleaf = -1;
         float hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
         bool gas_i = false;
@@ -444,7 +463,17 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 vzi = (float)a.vz[i];
             }
         }
+        asm volatile("" : "+f"(hi_), "+f"(pr), "+f"(cs), "+f"(vxi), "+f"(vyi), "+f"(vzi));
         const float h2x4 = 4.0f * hi_ * hi_;
+        // group bounding sphere (radius about the group centre, with slack for
+        // rounding) and the largest SPH reach of its gas lanes
+        float Rg = valid ? sqrtf(ox * ox + oy * oy + oz * oz) : 0.f;
+        float gas_reach2 = (kGas && gas_i && valid) ? h2x4 : 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            Rg = fmaxf(Rg, __shfl_xor_sync(0xffffffffu, Rg, o));
+            gas_reach2 = fmaxf(gas_reach2, __shfl_xor_sync(0xffffffffu, gas_reach2, o));
+        }
+        Rg = Rg * (1.0f + 1e-6f) + 1e-30f;
         float sx = 0, sy = 0, sz = 0, kx = 0, ky = 0, kz = 0;  // Kahan sums
         Vec3<float> side = {0, 0, 0};  // SPH and FP64-path contributions
         float du = 0;
@@ -461,25 +490,39 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         }
         __syncwarp();
         while (sp > 0) {
-            // gather up to 32 children from the top stack entries
+            // gather up to 32 children from the top stack entries: lane k looks at
+            // entry sp-1-k; an inclusive scan of their child counts decides how
+            // many entries fit, and each taking lane expands its own entry
             int nc = 0;
-            if (lane == 0) {
-                while (sp > 0) {
-                    const unsigned cm = W.stkcm[sp - 1];
-                    const int k = __popc(cm);
-                    if (nc + k > kBatch) break;
-                    sp--;
-                    const int2 e = W.stk[sp];
+            {
+                const int idx = sp - 1 - lane;
+                unsigned cmk = 0;
+                int2 ek = make_int2(0, 0);
+                if (idx >= 0) {
+                    cmk = W.stkcm[idx];
+                    ek = W.stk[idx];
+                }
+                const int k = __popc(cmk);
+                int incl = k;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const bool take = idx >= 0 && incl <= kBatch;
+                const unsigned tm = __ballot_sync(0xffffffffu, take);
+                const int t = __popc(tm);
+                nc = t ? __shfl_sync(0xffffffffu, incl, t - 1) : 0;
+                if (take) {
+                    int q = incl - k;
                     for (int o = 0; o < 8; o++)
-                        if ((cm >> o) & 1u) {
-                            W.bchild[nc] = e.x + o;
-                            W.bmask[nc] = (unsigned)e.y;
-                            nc++;
+                        if ((cmk >> o) & 1u) {
+                            W.bchild[q] = ek.x + o;
+                            W.bmask[q] = (unsigned)ek.y;
+                            q++;
                         }
                 }
+                sp -= t;
             }
-            nc = __shfl_sync(0xffffffffu, nc, 0);
-            sp = __shfl_sync(0xffffffffu, sp, 0);
             __syncwarp();
             // stage: lane j loads batch slot j (one round trip for the batch)
             if (lane < nc) {
@@ -490,18 +533,77 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 const unsigned char ccm = a.childmask[c];
                 float4 D;
                 if (kGas) D = a.wD[c];
-                W.cpos[lane] = make_float4((A.x - ghx) + (B.x - glx), (A.y - ghy) + (B.y - gly),
-                                           (A.z - ghz) + (B.z - glz), A.w);
+                const float cx = (A.x - ghx) + (B.x - glx), cy = (A.y - ghy) + (B.y - gly),
+                            cz = (A.z - ghz) + (B.z - glz);
+                W.cpos[lane] = make_float4(cx, cy, cz, A.w);
                 W.cmac[lane] = B.w;
                 W.cfirst[lane] = f;
                 W.ccm[lane] = ccm;
                 if (kGas) W.cgas[lane] = D;
+                // Every lane's distance lies in [dc - Rg, dc + Rg].  When the whole
+                // interval is clear of the opening threshold (outside the guard
+                // band) and of the near-zero and SPH cases, all lanes decide alike
+                // and no per-lane test is needed.  NaN centres fall through.
+                unsigned selfm = 0u;
+                if (B.w < 0.0f) {
+                    const int lp = a.leafpos[c] - grp * 32;
+                    if (lp >= 0 && lp < 32) selfm = 1u << lp;
+                }
+                W.cself[lane] = selfm;
+                const float dc = sqrtf(cx * cx + cy * cy + cz * cz);
+                const float lo = dc - Rg, hi = dc + Rg;
+                const float mac = B.w;
+                unsigned char cls = 0;
+                const bool no_sph = !kGas || !(D.w > 0.0f) || lo * lo > gas_reach2;
+                if (mac >= 0.0f) {
+                    if (lo > 0.0f && hi * hi < mac * (1.0f - 4.0f * kGuard))
+                        cls = 1;
+                    else if (lo > 0.0f && lo * lo > mac * (1.0f + 4.0f * kGuard) && no_sph)
+                        cls = 2;
+                } else if (lo > 0.0f && lo * lo > 4e-12f * eps02 && no_sph) {
+                    cls = 2;
+                }
+                W.ccls[lane] = cls;
+            }
+            __syncwarp();
+            // children every lane decides alike: lane j places child j at once
+            unsigned mixed;
+            {
+                const int j = lane;
+                const unsigned char cls = j < nc ? W.ccls[j] : (unsigned char)255;
+                const unsigned bm = j < nc ? W.bmask[j] : 0u;
+                const unsigned keep = bm & ~(j < nc ? W.cself[j] : 0u);
+                const bool opn = cls == 1;
+                const bool acc = cls == 2 && keep != 0u;
+                const unsigned om = __ballot_sync(0xffffffffu, opn);
+                const unsigned am = __ballot_sync(0xffffffffu, acc);
+                mixed = __ballot_sync(0xffffffffu, cls == 0);
+                const unsigned below = (1u << lane) - 1u;
+                if (sp + __popc(om) > kStack) {
+                    overflow = true;
+                } else {
+                    if (opn) {
+                        const int q = sp + __popc(om & below);
+                        W.stk[q] = make_int2(W.cfirst[j], (int)bm);
+                        W.stkcm[q] = W.ccm[j];
+                    }
+                    sp += __popc(om);
+                }
+                if (acc) {
+                    const int q = nl + __popc(am & below);
+                    W.lpos[q] = W.cpos[j];
+                    W.lmask[q] = keep;
+                }
+                nl += __popc(am);
             }
             __syncwarp();
 #pragma unroll 1
-            for (int j = 0; j < nc; j++) {
+            while (mixed) {
+                const int j = __ffs(mixed) - 1;
+                mixed &= mixed - 1u;
                 const int c = W.bchild[j];
-                const bool in = (W.bmask[j] >> lane) & 1u;
+                const unsigned bm = W.bmask[j];
+                const bool in = (bm >> lane) & 1u;
                 int decision = 0;  // 0 skip, 1 accept (FP32 list), 2 open, 3 done in FP64
                 const float4 Pc = W.cpos[j];
                 if (in && c != myleaf) {
@@ -511,7 +613,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
                     if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
-                        decision = recheck_fp64<kGeneral>(a, c, leaf, xi, yi, zi, r2 <= tiny, side, cnt_g);
+                        decision = recheck_fp64<kGeneral>(a, c, leaf, W.xd, lane, r2 <= tiny, side, cnt_g);
                     else
                         decision = (leaf || r2 > mac) ? 1 : 2;
                     if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) {
