@@ -32,7 +32,8 @@ EXPORTS = [
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
-    "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc",
+    "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
+    "ag2_phase_times",
 ]
 
 
@@ -95,6 +96,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_fp32_peak_probe.argtypes = [P, dp]
     L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.ag2_root_radius_noalloc.argtypes = [P, ctypes.c_int64, P, P]
+    L.ag2_phase_timing.argtypes = [P, I]
+    L.ag2_phase_times.argtypes = [P, I, P, P]
     L.ag2_launch_count.argtypes = [P]
     L.ag2_launch_count.restype = ctypes.c_int64
     _lib = L
@@ -254,6 +257,15 @@ class Context:
         g = ctypes.c_double()
         self._check(self.L.ag2_fp32_peak_probe(self.h, ctypes.byref(g)))
         return g.value
+
+    def phase_timing(self, enable: bool = True):
+        self._check(self.L.ag2_phase_timing(self.h, 1 if enable else 0))
+
+    def phase_times(self) -> list:
+        names = (ctypes.c_char_p * 16)()
+        ms = (ctypes.c_float * 16)()
+        k = self.L.ag2_phase_times(self.h, 16, names, ms)
+        return [(names[i].decode(), ms[i]) for i in range(min(k, 16))]
 
     def autotune(self) -> int:
         v = ctypes.c_int()

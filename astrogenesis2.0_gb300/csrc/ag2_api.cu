@@ -24,6 +24,33 @@ int cuda_check(Ctx *c, cudaError_t e, const char *what)
     return set_err(c, e == cudaErrorMemoryAllocation ? AG2_E_NOMEM : AG2_E_CUDA, m);
 }
 
+void phase_reset(Ctx *c)
+{
+    if (!c->timing) return;
+    c->nphase = 0;
+    cudaEventRecord(c->ev[0], c->stream);
+}
+
+void phase_mark(Ctx *c, const char *name)
+{
+    if (!c->timing || c->nphase >= Ctx::kMaxPhases) return;
+    c->phase_name[c->nphase] = name;
+    cudaEventRecord(c->ev[c->nphase + 1], c->stream);
+    c->nphase++;
+}
+
+void phase_finish(Ctx *c)
+{
+    if (!c->timing || c->nphase == 0) return;
+    cudaEventSynchronize(c->ev[c->nphase]);
+    for (int k = 0; k < c->nphase; k++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
+        c->phase_ms[k] = ms;
+    }
+    c->phase_count = c->nphase;
+}
+
 int sync_ctl(Ctx *c)
 {
     AG2_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(Ctx::Ctl), cudaMemcpyDeviceToHost, c->stream));
@@ -240,6 +267,8 @@ int ag2_destroy(ag2_ctx *c)
                   c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8, c->width_part, c->ctl};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return AG2_OK;
@@ -342,7 +371,10 @@ size_t ag2_count(const ag2_ctx *c) { return c ? c->n : 0; }
 int ag2_build_tree(ag2_ctx *c)
 {
     if (!c) return AG2_E_INVALID;
-    return build_tree(c);
+    phase_reset(c);
+    int rc = build_tree(c);
+    phase_finish(c);
+    return rc;
 }
 
 int ag2_visual_density(ag2_ctx *c, double R)
@@ -387,14 +419,48 @@ int ag2_step(ag2_ctx *c, double dt, double hubble_factor, int with_visual, doubl
 {
     if (!c) return AG2_E_INVALID;
     int rc;
+    // phase names follow the reference's Log::startProcess calls (Simulation.cpp:256-351)
+    phase_reset(c);
     if ((rc = run_kick_drift(c, dt))) return rc;
-    if ((rc = build_tree(c))) return rc;
+    phase_mark(c, "first kick");
+    const bool t = c->timing;
+    c->timing = false;  // the build's own sub-phases are not split inside a step
+    rc = build_tree(c);
+    c->timing = t;
+    if (rc) return rc;
+    phase_mark(c, "build tree");
     if (with_visual && (rc = run_visual_density(c, Rv))) return rc;
+    phase_mark(c, "Visual Density");
     if ((rc = run_sph_density(c))) return rc;
+    phase_mark(c, "SPH density and update");
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
     if ((rc = run_forces(c))) return rc;
+    phase_mark(c, "Force Calculation");
     if ((rc = run_close_step(c, dt, hubble_factor))) return rc;
-    return check_walk(c);
+    phase_mark(c, "second kick");
+    rc = check_walk(c);
+    phase_finish(c);
+    return rc;
+}
+
+int ag2_phase_timing(ag2_ctx *c, int enable)
+{
+    if (!c) return AG2_E_INVALID;
+    if (enable && !c->ev[0])
+        for (auto &e : c->ev) AG2_CUDA(c, cudaEventCreate(&e));
+    c->timing = enable != 0;
+    return AG2_OK;
+}
+
+int ag2_phase_times(const ag2_ctx *c, int max, const char **names, float *ms)
+{
+    if (!c || max < 0) return AG2_E_INVALID;
+    int k = c->phase_count < max ? c->phase_count : max;
+    for (int i = 0; i < k; i++) {
+        if (names) names[i] = c->phase_name[i];
+        if (ms) ms[i] = c->phase_ms[i];
+    }
+    return c->phase_count;
 }
 
 int ag2_root_radius(ag2_ctx *c, double *r)
@@ -558,10 +624,19 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
         if (particle) particle[k] = leafpos[v] >= 0 ? id[leafpos[v]] : -1;
         if (cp_count) cp_count[k] = cc;
         if (cp_hash) cp_hash[k] = ch;
-        if (mass) mass[k] = m[v];
-        if (com3) { com3[3 * k] = cx[v]; com3[3 * k + 1] = cy[v]; com3[3 * k + 2] = cz[v]; }
-        if (gas_mass) gas_mass[k] = g[v];
-        if (mvel3) { mvel3[3 * k] = vx[v]; mvel3[3 * k + 1] = vy[v]; mvel3[3 * k + 2] = vz[v]; }
+        const bool empty = count[v] == 0;  // the build leaves empty children's moments unwritten
+        if (mass) mass[k] = empty ? 0.0 : m[v];
+        if (com3) {
+            com3[3 * k] = empty ? 0.0 : cx[v];
+            com3[3 * k + 1] = empty ? 0.0 : cy[v];
+            com3[3 * k + 2] = empty ? 0.0 : cz[v];
+        }
+        if (gas_mass) gas_mass[k] = empty ? 0.0 : g[v];
+        if (mvel3) {
+            mvel3[3 * k] = empty ? 0.0 : vx[v];
+            mvel3[3 * k + 1] = empty ? 0.0 : vy[v];
+            mvel3[3 * k + 2] = empty ? 0.0 : vz[v];
+        }
         if (center3) { center3[3 * k] = ccx[v]; center3[3 * k + 1] = ccy[v]; center3[3 * k + 2] = ccz[v]; }
         if (radius) radius[k] = std::ldexp(c->root_radius, -(int)level[v]);
         k++;

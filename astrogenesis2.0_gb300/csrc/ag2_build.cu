@@ -232,104 +232,118 @@ __global__ void k_digit(int n, int64_t base, const int32_t *__restrict__ posnode
     agg_inc(hist, (int)((int64_t)nid - base) * 9 + d);
 }
 
-// split decisions and children of the nodes of one level
+// Split decisions and children of the nodes of one level.  Eight threads per
+// node (one per child octant) so that the children's fields are written with
+// coalesced stores; the first thread of each group of eight decides the split,
+// allocates the 8-child block (one atomic per warp) and writes the parent.
 __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, int64_t node_cap, Nodes nd,
                         Ctx::Ctl *ctl, const int32_t *__restrict__ hist, int32_t *__restrict__ cursor,
                         int max_depth)
 {
-    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (j >= count_lvl) return;
-    int64_t nid = base + j;
-    if (!nd.needs[nid]) return;
-    const int32_t *h = hist + 9 * j;
-    int32_t cnt = nd.count[nid];
-    int32_t start = nd.start[nid];
-    int32_t ndrop = h[8];
-    int32_t reached = cnt - ndrop;
-    uint8_t mode = nd.mode[nid];
-    nd.ndrop[nid] = ndrop;
-    if (ndrop) ctl->any_drop = 1;
-    int32_t acc = start;
-    for (int d = 0; d < 9; d++) {
-        cursor[9 * j + d] = acc;
-        acc += h[d];
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = lane_id();
+    const int o = lane & 7;
+    const int64_t j = t >> 3;
+    const unsigned gmask = 0xffu << (lane & ~7);  // the 8 lanes of this node
+    const bool exists = j < count_lvl;
+    const int64_t nid = base + (exists ? j : 0);
+    const bool needs = exists && nd.needs[nid];
+    // split decision (every lane of the group computes the same values)
+    int32_t cnt = 0, start = 0, ndrop = 0, reached = 0;
+    uint8_t mode = 0;
+    bool internal = false;
+    const int32_t *h = hist + 9 * (exists ? j : 0);
+    if (needs) {
+        cnt = nd.count[nid];
+        start = nd.start[nid];
+        ndrop = h[8];
+        reached = cnt - ndrop;
+        mode = nd.mode[nid];
+        internal = (mode == MODE_PAR) || (reached >= 2);
     }
-    bool internal = (mode == MODE_PAR) || (reached >= 2);
-    if (!internal) {
-        nd.first[nid] = -1;
-        nd.leafpos[nid] = (reached == 1) ? start : -1;
-        return;
+    if (needs && o == 0) {
+        nd.ndrop[nid] = ndrop;
+        if (ndrop) ctl->any_drop = 1;
+        int32_t acc = start;
+        for (int d = 0; d < 9; d++) {
+            cursor[9 * j + d] = acc;
+            acc += h[d];
+        }
+        if (!internal) {
+            nd.first[nid] = -1;
+            nd.leafpos[nid] = (reached == 1) ? start : -1;
+        }
     }
-    if (level + 1 >= max_depth) {
-        atomicExch(&ctl->err_code, (int)AG2_E_COINCIDENT);
-        atomicExch(&ctl->err_info, (int)nid);
-        nd.first[nid] = -1;
-        nd.leafpos[nid] = -1;
-        return;
+    bool split = needs && internal;
+    if (split && level + 1 >= max_depth) {
+        if (o == 0) {
+            atomicExch(&ctl->err_code, (int)AG2_E_COINCIDENT);
+            atomicExch(&ctl->err_info, (int)nid);
+            nd.first[nid] = -1;
+            nd.leafpos[nid] = -1;
+        }
+        split = false;
     }
-    // one atomic per warp for the 8-child blocks of all splitting lanes
-    unsigned long long cb;
-    {
-        unsigned act = __activemask();
-        int lane = lane_id();
-        int leader = __ffs(act) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd((unsigned long long *)&ctl->node_count, 8ull * __popc(act));
-        base = __shfl_sync(act, base, leader);
-        cb = base + 8ull * __popc(act & ((1u << lane) - 1u));
+    // one atomic per warp for the 8-child blocks of all splitting nodes
+    const unsigned leaders = __ballot_sync(0xffffffffu, split && o == 0);
+    unsigned long long wbase = 0;
+    if (leaders) {
+        if (lane == __ffs(leaders) - 1)
+            wbase = atomicAdd((unsigned long long *)&ctl->node_count, 8ull * __popc(leaders));
+        wbase = __shfl_sync(0xffffffffu, wbase, __ffs(leaders) - 1);
     }
-    if ((int64_t)cb + 8 > node_cap) {
-        atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
-        nd.first[nid] = -1;
-        return;
-    }
-    int64_t c0 = (int64_t)cb;
-    nd.first[nid] = (int32_t)c0;
-    nd.leafpos[nid] = -1;
-    // child centres c + r*(+-0.5) and radius r/2 (Node.cpp:433-443, 630-642)
-    double r = ldexp(ctl->R, -level);
-    double rc = ldexp(ctl->R, -(level + 1));
-    double cx = nd.cx[nid], cy = nd.cy[nid], cz = nd.cz[nid];
-    bool par = (mode == MODE_PAR);
     int nneeds = 0;
-    int32_t s = start;
-    for (int o = 0; o < 8; o++) {
-        int64_t c = c0 + o;
-        int32_t cc = h[o];
-        nd.cx[c] = __dadd_rn(cx, __dmul_rn(r, (o & 1) ? 0.5 : -0.5));
-        nd.cy[c] = __dadd_rn(cy, __dmul_rn(r, (o & 2) ? 0.5 : -0.5));
-        nd.cz[c] = __dadd_rn(cz, __dmul_rn(r, (o & 4) ? 0.5 : -0.5));
-        nd.start[c] = s;
-        nd.count[c] = cc;
-        nd.ndrop[c] = 0;
-        nd.first[c] = -1;
-        nd.parent[c] = (int32_t)nid;
-        nd.level[c] = (int8_t)(level + 1);
-        uint8_t cm;
-        if (cc == 0)
-            cm = MODE_EMPTY;
-        else if (!par)
-            cm = MODE_SER;
-        else if (cc == 1)
-            cm = MODE_VEC1;
-        else if (cc < thresh)
-            cm = MODE_SER_ENTRY;
-        else
-            cm = MODE_PAR;
-        nd.mode[c] = cm;
-        uint8_t needs = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER) ? 1 : 0;
-        nd.needs[c] = needs;
-        nd.leafpos[c] = (cm == MODE_VEC1) ? s : -1;
-        if (needs) set_bounds(nd, c, rc);
-        nneeds += needs;
-        s += cc;
+    if (split) {
+        const unsigned long long cb = wbase + 8ull * __popc(leaders & ((1u << (lane & ~7)) - 1u));
+        if ((int64_t)cb + 8 > node_cap) {
+            if (o == 0) {
+                atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+                nd.first[nid] = -1;
+            }
+        } else {
+            const int64_t c0 = (int64_t)cb;
+            if (o == 0) {
+                nd.first[nid] = (int32_t)c0;
+                nd.leafpos[nid] = -1;
+            }
+            // child o: centre c + r*(+-0.5), radius r/2 (Node.cpp:433-443, 630-642)
+            const double r = ldexp(ctl->R, -level);
+            const double rc = ldexp(ctl->R, -(level + 1));
+            const int64_t c = c0 + o;
+            int32_t s = start;
+            for (int d = 0; d < o; d++) s += h[d];
+            const int32_t cc = h[o];
+            nd.cx[c] = __dadd_rn(nd.cx[nid], __dmul_rn(r, (o & 1) ? 0.5 : -0.5));
+            nd.cy[c] = __dadd_rn(nd.cy[nid], __dmul_rn(r, (o & 2) ? 0.5 : -0.5));
+            nd.cz[c] = __dadd_rn(nd.cz[nid], __dmul_rn(r, (o & 4) ? 0.5 : -0.5));
+            nd.start[c] = s;
+            nd.count[c] = cc;
+            nd.ndrop[c] = 0;
+            nd.first[c] = -1;
+            nd.parent[c] = (int32_t)nid;
+            nd.level[c] = (int8_t)(level + 1);
+            uint8_t cm;
+            if (cc == 0)
+                cm = MODE_EMPTY;
+            else if (mode != MODE_PAR)
+                cm = MODE_SER;
+            else if (cc == 1)
+                cm = MODE_VEC1;
+            else if (cc < thresh)
+                cm = MODE_SER_ENTRY;
+            else
+                cm = MODE_PAR;
+            nd.mode[c] = cm;
+            const uint8_t cneeds = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER) ? 1 : 0;
+            nd.needs[c] = cneeds;
+            nd.leafpos[c] = (cm == MODE_VEC1) ? s : -1;
+            if (cneeds) set_bounds(nd, c, rc);
+            nneeds = cneeds;
+        }
     }
-    {
-        unsigned act = __activemask();
-        int sum = (int)__reduce_add_sync(act, (unsigned)nneeds);
-        if (lane_id() == __ffs(act) - 1 && sum) atomicAdd(&ctl->next_needs, sum);
-    }
-
+    const int sum = (int)__reduce_add_sync(0xffffffffu, (unsigned)nneeds);
+    if (lane == 0 && sum) atomicAdd(&ctl->next_needs, sum);
+    (void)gmask;
 }
 
 __global__ void k_scatter(int n, int64_t base, const int32_t *__restrict__ posnode, const int32_t *__restrict__ perm,
@@ -520,17 +534,7 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     if (j >= count_lvl) return;
     int64_t nid = base + j;
     int32_t cnt = nd.count[nid];
-    if (cnt == 0) {
-        // empty child: never visited by the walk (its parent's child mask is 0
-        // there) and never on a particle's path; only the zero moments matter
-        nd.mass[nid] = 0.0;
-        nd.comx[nid] = nd.comy[nid] = nd.comz[nid] = 0.0;
-        nd.gas[nid] = 0.0;
-        nd.mvx[nid] = nd.mvy[nid] = nd.mvz[nid] = 0.0;
-        nd.ngas[nid] = 0;
-        nd.childmask[nid] = 0;
-        return;
-    }
+    if (cnt == 0) return;  // empty child: no kernel reads it (parents test the count first)
     int32_t start = nd.start[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
     uint8_t mode = nd.mode[nid];
     int level = nd.level[nid];
@@ -815,6 +819,7 @@ int build_tree(Ctx *c)
     } else {
         AG2_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream));
     }
+    phase_mark(c, "build: root width");
     if ((rc = ensure_node_capacity(c, 1024)) != AG2_OK) return rc;
     const int thresh = c->prm.split_threshold;
     AG2_LAUNCH(c, k_root_init, 1, 32, 0, c->nd, c->ctl, n, thresh, c->pnode);
@@ -836,7 +841,7 @@ int build_tree(Ctx *c)
         Particles &Sp = c->S();
         AG2_LAUNCH(c, k_digit, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, Sp.px, Sp.py, Sp.pz,
                    c->nd, c->digit, c->hist);
-        AG2_LAUNCH(c, k_nodes, grid_for((size_t)cnt_lvl, kBlock), kBlock, 0, base, cnt_lvl, level, thresh,
+        AG2_LAUNCH(c, k_nodes, grid_for((size_t)cnt_lvl * 8, kBlock), kBlock, 0, base, cnt_lvl, level, thresh,
                    (int64_t)c->node_cap, c->nd, c->ctl, c->hist, c->cursor, (int)AG2_MAX_DEPTH);
         AG2_CUDA(c, cudaMemcpyAsync(c->perm2, c->perm, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
         AG2_CUDA(c, cudaMemsetAsync(c->posnode2, 0xFF, n * sizeof(int32_t), c->stream));
@@ -857,6 +862,7 @@ int build_tree(Ctx *c)
         needs = h.next_needs;
         level++;
     }
+    phase_mark(c, "build: levels");
     c->max_level = (int)c->level_base.size() - 2;
     c->nnodes = c->level_base.back();
     c->ninternal = (c->nnodes - 1) / 8;
@@ -872,6 +878,7 @@ int build_tree(Ctx *c)
     AG2_LAUNCH(c, k_reorder, grid_for(n, kBlock), kBlock, 0, n, c->perm, src, dst);
     c->cur ^= 1;
     AG2_LAUNCH(c, k_refnode, grid_for(n, kBlock), kBlock, 0, n, c->nd, c->pnode, c->S().id, c->refnode);
+    phase_mark(c, "build: reorder");
 
     // moments, deepest level first
     for (int L = c->max_level; L >= 0; L--) {
@@ -880,6 +887,7 @@ int build_tree(Ctx *c)
         AG2_LAUNCH(c, k_moments, grid_for((size_t)cnt, kBlock), kBlock, 0, base, cnt, c->nd, c->S(),
                    c->gas_prefix, gas_uniform ? 1 : 0, c->prm.theta, c->root_radius);
     }
+    phase_mark(c, "build: moments");
     c->have_tree = true;
     c->tree_theta = c->prm.theta;
     return AG2_OK;

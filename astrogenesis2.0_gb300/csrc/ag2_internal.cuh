@@ -132,8 +132,23 @@ struct Ctx {
 
     Nodes nd = {};
 
+    // phase timers (CUDA events), enabled by ag2_phase_timing
+    static constexpr int kMaxPhases = 16;
+    bool timing = false;
+    cudaEvent_t ev[kMaxPhases + 1] = {};
+    const char *phase_name[kMaxPhases] = {};
+    int nphase = 0;          // phases recorded since the last reset
+    float phase_ms[kMaxPhases] = {};
+    int phase_count = 0;     // phases of the last completed measurement
+
     Particles &S() { return st[cur]; }
 };
+
+// Phase timing helpers: reset at the start of a measured call, mark after each
+// phase, finish (synchronises) at the end.
+void phase_reset(Ctx *c);
+void phase_mark(Ctx *c, const char *name);
+void phase_finish(Ctx *c);
 
 // ordered 64-bit integer key of a double: a < b (as doubles, -0 == +0 mapped
 // to +0) iff key(a) < key(b)

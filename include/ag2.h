@@ -133,6 +133,15 @@ int ag2_step(ag2_ctx *ctx, double dt, double hubble_factor, int with_visual_dens
  * ag2_forces calls of this context; *variant receives its index. */
 int ag2_autotune(ag2_ctx *ctx, int *variant);
 
+/* Phase timers (CUDA events on the context's stream).  When enabled,
+ * ag2_build_tree records its sub-phases and ag2_step records the phases the
+ * reference logs with Log::startProcess (Simulation.cpp:256-351: "first kick",
+ * "build tree", "Visual Density", "SPH density and update", "Force
+ * Calculation", "second kick").  ag2_phase_times copies up to max phase names
+ * and durations (ms) of the last measured call and returns how many there are. */
+int ag2_phase_timing(ag2_ctx *ctx, int enable);
+int ag2_phase_times(const ag2_ctx *ctx, int max, const char **names, float *ms);
+
 /* Tree introspection (synchronises). */
 int ag2_root_radius(ag2_ctx *ctx, double *radius);
 int ag2_node_count(ag2_ctx *ctx, int64_t *nodes, int64_t *internal, int32_t *max_depth);

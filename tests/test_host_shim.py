@@ -1,0 +1,73 @@
+"""The C++ drop-in (astrogenesis2.0_gb300/host/ag2_tree.hpp) compiles against
+the C-ABI (CPU) and, on a GPU, drives two steps of the reference's loop to the
+same state as the C restatement."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import ics
+import oracle
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(REPO, "tests", "cpp", "shim_demo.cpp")
+
+
+def compile_demo(out):
+    import build
+
+    lib = build.build()
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"), "-I",
+           os.path.join(REPO, "astrogenesis2.0_gb300", "host"), SRC, "-o", out, "-L", os.path.dirname(lib), "-lag2",
+           "-Wl,-rpath," + os.path.dirname(lib)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+
+
+def test_shim_compiles(tmp_path):
+    compile_demo(str(tmp_path / "shim_demo"))
+
+
+@pytest.mark.gpu
+def test_shim_steps_match_port(tmp_path):
+    exe = str(tmp_path / "shim_demo")
+    compile_demo(exe)
+    d = ics.small_gas_cloud(3000, seed=31)
+    n = len(d["mass"])
+    e0, theta, dt, steps = 0.01, 0.5, 1e-3, 2
+    rec = np.concatenate([d["pos"], d["vel"], d["mass"][:, None], d["U"][:, None]], axis=1)
+    with open(tmp_path / "in.bin", "wb") as f:
+        f.write(np.int64(n).tobytes())
+        f.write(np.ascontiguousarray(rec, np.float64).tobytes())
+        f.write(np.ascontiguousarray(d["type"], np.uint8).tobytes())
+        f.write(np.array([e0, theta, d["massInH"], dt], np.float64).tobytes())
+    r = subprocess.run([exe, str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), str(steps)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    out = np.fromfile(tmp_path / "out.bin", np.float64).reshape(n, 12)
+    w = oracle.World(d["pos"], d["mass"], d["type"], d["vel"], d["U"], kind="port")
+    w.build(1)
+    w.gas_density(d["massInH"])
+    w.forces(e0, theta, os.cpu_count() or 1)
+    for _ in range(steps):
+        w.kick(dt)
+        w.drift(dt)
+        w.build(1)
+        w.gas_density(d["massInH"])
+        w.forces(e0, theta, os.cpu_count() or 1)
+        g = d["type"] == 2
+        du = w.get("dUdt")
+        U = w.get("U")
+        U[g] = U[g] + du[g] * dt
+        du[g] = 0
+        w.set("U", U)
+        w.set("dUdt", du)
+        w.kick(dt)
+    pos = w.get("pos")
+    assert np.max(np.abs(out[:, 0:3] - pos)) <= 1e-6 * np.max(np.abs(pos))
+    # the shim runs the FP32 walk: positions agree to rounding, so a node-level
+    # smoothing length may differ only where a particle sits on a cell wall
+    assert np.mean(out[:, 9] == w.get("h")) >= 0.999
+    a = w.get("acc")
+    rel = np.linalg.norm(out[:, 6:9] - a, axis=1) / np.maximum(np.linalg.norm(a, axis=1), 1e-300)
+    assert np.median(rel) <= 1e-5 and np.quantile(rel, 0.999) <= 1e-3
