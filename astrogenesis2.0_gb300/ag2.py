@@ -33,7 +33,7 @@ EXPORTS = [
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
     "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
-    "ag2_phase_times",
+    "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius",
 ]
 
 
@@ -97,6 +97,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.ag2_root_radius_noalloc.argtypes = [P, ctypes.c_int64, P, P]
     L.ag2_phase_timing.argtypes = [P, I]
+    L.ag2_set_instances.argtypes = [P, ctypes.c_int32, P, P]
+    L.ag2_instance_radius.argtypes = [P, ctypes.c_int32, dp]
     L.ag2_phase_times.argtypes = [P, I, P, P]
     L.ag2_launch_count.argtypes = [P]
     L.ag2_launch_count.restype = ctypes.c_int64
@@ -257,6 +259,19 @@ class Context:
         g = ctypes.c_double()
         self._check(self.L.ag2_fp32_peak_probe(self.h, ctypes.byref(g)))
         return g.value
+
+    def set_instances(self, first, massInH=None):
+        """Split the uploaded particles into independent simulations:
+        instance k = upload indices [first[k], first[k+1])."""
+        first = np.ascontiguousarray(first, np.int64)
+        mih = None if massInH is None else np.ascontiguousarray(massInH, np.float64)
+        self._keep_inst = (first, mih)
+        self._check(self.L.ag2_set_instances(self.h, first.size - 1, _ptr(first), _ptr(mih)))
+
+    def instance_radius(self, k: int) -> float:
+        r = ctypes.c_double()
+        self._check(self.L.ag2_instance_radius(self.h, k, ctypes.byref(r)))
+        return r.value
 
     def phase_timing(self, enable: bool = True):
         self._check(self.L.ag2_phase_timing(self.h, 1 if enable else 0))

@@ -43,10 +43,18 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+# Per-file flags.  The walk is compiled without multiply-add contraction: its
+# results must not depend on which variant (with or without SPH, register
+# budget) the compiler contracted differently, and the reference (x86-64
+# without -march) does not contract either.  Intended FMAs are written as fmaf.
+FILE_FLAGS = {"ag2_walk.cu": ["-fmad=false"]}
+
+
 def _compile(src: str, headers: list[str]) -> str:
     obj = os.path.join(OBJ, os.path.basename(src).replace(".cu", ".o"))
-    if _stale(obj, [src] + headers):
-        cmd = [_nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+    extra = FILE_FLAGS.get(os.path.basename(src), [])
+    if _stale(obj, [src] + headers + [os.path.abspath(__file__)]):
+        cmd = [_nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

@@ -2,6 +2,7 @@
 // download in the caller's order, the step driver and tree introspection.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -178,6 +179,20 @@ bool valid_params(const ag2_params *p)
            p->theta > 0.0;
 }
 
+__global__ void k_pinst(const int64_t *first, int32_t *pinst)
+{
+    const int k = blockIdx.x;
+    for (int64_t i = first[k] + threadIdx.x; i < first[k + 1]; i += blockDim.x) pinst[i] = k;
+}
+
+template <class T>
+bool realloc_dev(T *&p, size_t n)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    return cudaMalloc((void **)&p, (n ? n : 1) * sizeof(T)) == cudaSuccess;
+}
+
 int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const double *mass, const double *U,
                   const uint8_t *type)
 {
@@ -187,6 +202,8 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
     c->n = n;
     c->have_tree = false;
     c->gas_stats_dirty = true;
+    c->n_inst = 1;
+    c->inst_dirty = true;
     int rc = sync_ctl(c);
     if (rc) return rc;
     if (c->ctl_host->err_code == AG2_E_NAN) return set_err(c, AG2_E_NAN, "non-finite particle position");
@@ -194,6 +211,98 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
 }
 
 }  // namespace
+
+// Upload the instance tables and walk groups when the instance layout changed.
+int ensure_instance_tables(Ctx *c)
+{
+    if (!c->inst_dirty) return AG2_OK;
+    const int K = c->n_inst;
+    if ((size_t)K > c->inst_cap) {
+        bool ok = realloc_dev(c->inst_first, K + 1) && realloc_dev(c->inst_R, K) && realloc_dev(c->inst_massInH, K) &&
+                  realloc_dev(c->gas_off, K) && realloc_dev(c->gas_uni, K) && realloc_dev(c->gas_cnt, K) &&
+                  realloc_dev(c->gas_kmin, K) && realloc_dev(c->gas_kmax, K) && realloc_dev(c->width_thr, K) &&
+                  realloc_dev(c->wsum_final, K);
+        if (!ok) return set_err(c, AG2_E_NOMEM, "instance table allocation failed");
+        c->inst_cap = K;
+    }
+    if (K == 1) {
+        c->inst_first_h = {0, (int64_t)c->n};
+        c->inst_massInH_h = {c->prm.massInH};
+    }
+    AG2_CUDA(c, cudaMemcpyAsync(c->inst_first, c->inst_first_h.data(), (K + 1) * sizeof(int64_t),
+                                cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(c->inst_massInH, c->inst_massInH_h.data(), K * sizeof(double), cudaMemcpyHostToDevice,
+                                c->stream));
+    // root-width summation tasks (ag2_build.cu): one sequential task per instance
+    // up to 4096 particles, a 64-ary tree of sequential runs above
+    {
+        std::vector<std::vector<int4>> lv(1);
+        std::vector<int32_t> fin(K);
+        int32_t nbuf = 0;
+        // level 0 tasks read particles; a task's z is its destination pair
+        std::vector<std::pair<int32_t, int32_t>> cur(K);  // per instance: (first pair, count) of its current level
+        for (int k = 0; k < K; k++) {
+            const int64_t b = c->inst_first_h[k], n = c->inst_first_h[k + 1] - b;
+            const int64_t run = n <= 4096 ? std::max<int64_t>(n, 1) : 64;
+            const int32_t cnt = (int32_t)((n + run - 1) / run);
+            cur[k] = {nbuf, std::max(cnt, 1)};
+            for (int64_t j = 0; j < std::max<int64_t>(n, 1); j += run)
+                lv[0].push_back(make_int4((int)(b + j), (int)std::min(run, n - j), nbuf++, k));
+            if (n == 0) {
+                lv[0].back().y = 0;
+            }
+        }
+        for (;;) {
+            std::vector<int4> next;
+            bool any = false;
+            for (int k = 0; k < K; k++) {
+                auto [p0, cnt] = cur[k];
+                if (cnt <= 1) {
+                    fin[k] = p0;
+                    continue;
+                }
+                any = true;
+                const int32_t nn = (cnt + 63) / 64;
+                const int32_t q0 = nbuf;
+                for (int32_t j = 0; j < cnt; j += 64) next.push_back(make_int4(p0 + j, std::min(64, cnt - j), nbuf++, k));
+                cur[k] = {q0, nn};
+            }
+            if (!any) break;
+            lv.push_back(std::move(next));
+        }
+        std::vector<int4> all;
+        c->wsum_level.assign(1, 0);
+        for (auto &l : lv) {
+            all.insert(all.end(), l.begin(), l.end());
+            c->wsum_level.push_back((int32_t)all.size());
+        }
+        if (!realloc_dev(c->wsum_task, all.size()) || !realloc_dev(c->width_part, 2 * (size_t)std::max(nbuf, 1)))
+            return set_err(c, AG2_E_NOMEM, "root width table allocation failed");
+        AG2_CUDA(c, cudaMemcpyAsync(c->wsum_task, all.data(), all.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                    c->stream));
+        AG2_CUDA(c, cudaMemcpyAsync(c->wsum_final, fin.data(), K * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                    c->stream));
+        AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    std::vector<int4> g;
+    for (int k = 0; k < K; k++) {
+        const int64_t b = c->inst_first_h[k], e = c->inst_first_h[k + 1];
+        for (int64_t s = b; s < e; s += 32) g.push_back(make_int4((int)s, (int)std::min<int64_t>(32, e - s), k, 0));
+    }
+    if (g.size() > c->groups_cap) {
+        if (!realloc_dev(c->groups, g.size())) return set_err(c, AG2_E_NOMEM, "group table allocation failed");
+        c->groups_cap = g.size();
+    }
+    if (!g.empty())
+        AG2_CUDA(c, cudaMemcpyAsync(c->groups, g.data(), g.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    c->ngroups = (int32_t)g.size();
+    if (c->n) AG2_LAUNCH(c, k_pinst, K, 256, 0, c->inst_first, c->pinst);
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors above go out of scope
+    c->inst_dirty = false;
+    c->gas_stats_dirty = true;
+    return AG2_OK;
+}
+
 }  // namespace ag2
 
 using namespace ag2;
@@ -224,6 +333,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     if (!c) return AG2_E_NOMEM;
     c->prm = *params;
     cudaGetDevice(&c->device);
+    if (const char *dbg = std::getenv("AG2_DEBUG_SYNC")) c->debug_sync = dbg[0] == '1';
     size_t cap = std::max(capacity, (size_t)1);
     c->cap = cap;
     int rc = AG2_OK;
@@ -238,10 +348,10 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->refnode, cap * 4) == cudaSuccess && cudaMalloc(&c->slot_of, cap * 4) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->digit, cap) == cudaSuccess &&
+         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->drop_list, 65536 * 4) == cudaSuccess && cudaMalloc(&c->digit, cap) == cudaSuccess &&
          cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&
-         cudaMalloc(&c->width_part, 2 * 1024 * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&c->pinst, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->ctl, sizeof(Ctx::Ctl)) == cudaSuccess &&
          cudaMallocHost(&c->ctl_host, sizeof(Ctx::Ctl)) == cudaSuccess;
     if (ok) ok = ensure_node_capacity(c, 4 * cap + 1024) == AG2_OK;
@@ -263,8 +373,10 @@ int ag2_destroy(ag2_ctx *c)
     free_particles(c->st[0]);
     free_particles(c->st[1]);
     free_nodes(c->nd);
-    void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->slot_of, c->finalnode, c->nodelist, c->digit,
-                  c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8, c->width_part, c->ctl};
+    void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->slot_of, c->finalnode,
+                  c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
+                  c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->inst_first, c->inst_R,
+                  c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     for (auto &e : c->ev)
@@ -280,6 +392,7 @@ int ag2_set_params(ag2_ctx *c, const ag2_params *p)
     bool retree = p->split_threshold != c->prm.split_threshold;
     c->prm = *p;
     if (retree) c->have_tree = false;
+    if (c->n_inst == 1) c->inst_massInH_h = {p->massInH};
     return AG2_OK;
 }
 
@@ -463,6 +576,31 @@ int ag2_phase_times(const ag2_ctx *c, int max, const char **names, float *ms)
     return c->phase_count;
 }
 
+int ag2_set_instances(ag2_ctx *c, int32_t n_inst, const int64_t *first, const double *massInH)
+{
+    if (!c || n_inst < 1 || !first) return set_err(c, AG2_E_INVALID, "bad instance layout");
+    if (first[0] != 0 || first[n_inst] != (int64_t)c->n)
+        return set_err(c, AG2_E_INVALID, "instances must cover the uploaded particles: first[0] = 0, first[k] = n");
+    for (int k = 0; k < n_inst; k++)
+        if (first[k + 1] < first[k]) return set_err(c, AG2_E_INVALID, "instance offsets must not decrease");
+    c->n_inst = n_inst;
+    c->inst_first_h.assign(first, first + n_inst + 1);
+    c->inst_massInH_h.assign(n_inst, c->prm.massInH);
+    if (massInH) c->inst_massInH_h.assign(massInH, massInH + n_inst);
+    c->inst_dirty = true;
+    c->have_tree = false;
+    return AG2_OK;
+}
+
+int ag2_instance_radius(ag2_ctx *c, int32_t k, double *r)
+{
+    if (!c || !r) return AG2_E_INVALID;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
+    if (k < 0 || k >= c->n_inst) return set_err(c, AG2_E_INVALID, "no such instance");
+    *r = c->inst_R_h[k];
+    return AG2_OK;
+}
+
 int ag2_root_radius(ag2_ctx *c, double *r)
 {
     if (!c || !r) return AG2_E_INVALID;
@@ -539,7 +677,8 @@ int ag2_particle_node(ag2_ctx *c, int64_t *out)
         AG2_CUDA(c, cudaMemcpyAsync(id.data(), c->S().id, n * 4, cudaMemcpyDeviceToHost, c->stream));
     }
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));
-    std::vector<int64_t> pre(nn, -1), stack{0};
+    std::vector<int64_t> pre(nn, -1), stack;
+    for (int r = c->n_inst - 1; r >= 0; r--) stack.push_back(r);
     int64_t k = 0;
     while (!stack.empty()) {
         int64_t v = stack.back();
@@ -564,6 +703,7 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
     std::vector<int8_t> level(nn);
     std::vector<uint8_t> mode(nn);
     std::vector<double> m(nn), cx(nn), cy(nn), cz(nn), g(nn), vx(nn), vy(nn), vz(nn), ccx(nn), ccy(nn), ccz(nn);
+    std::vector<int32_t> inst_of(nn);
     auto cp = [&](void *dst, const void *src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
     };
@@ -586,15 +726,16 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
     AG2_CUDA(c, cp(ccx.data(), d.cx, nn * 8));
     AG2_CUDA(c, cp(ccy.data(), d.cy, nn * 8));
     AG2_CUDA(c, cp(ccz.data(), d.cz, nn * 8));
+    AG2_CUDA(c, cp(inst_of.data(), d.inst, nn * 4));
     if (n) AG2_CUDA(c, cp(id.data(), c->S().id, n * 4));
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));
     // prefix sums of member hashes over tree-order slots
     std::vector<uint64_t> hp(n + 1, 0);
     for (size_t i = 0; i < n; i++) hp[i + 1] = hp[i] + id_hash((uint64_t)id[i]);
     auto hsum = [&](int32_t a, int32_t b) { return hp[b] - hp[a]; };
-    // depth-first preorder, children 0..7
+    // depth-first preorder, children 0..7, instance after instance
     std::vector<int64_t> stack;
-    stack.push_back(0);
+    for (int r = c->n_inst - 1; r >= 0; r--) stack.push_back(r);
     int64_t k = 0;
     while (!stack.empty()) {
         int64_t v = stack.back();
@@ -602,7 +743,7 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
         int32_t s = start[v], e = s + count[v], re = e - ndrop[v];
         int64_t cc = 0;
         uint64_t ch = 0;
-        bool root = (v == 0);
+        bool root = (v < c->n_inst);
         switch (mode[v]) {
         case MODE_PAR:
         case MODE_VEC1:
@@ -638,7 +779,7 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
             mvel3[3 * k + 2] = empty ? 0.0 : vz[v];
         }
         if (center3) { center3[3 * k] = ccx[v]; center3[3 * k + 1] = ccy[v]; center3[3 * k + 2] = ccz[v]; }
-        if (radius) radius[k] = std::ldexp(c->root_radius, -(int)level[v]);
+        if (radius) radius[k] = std::ldexp(c->inst_R_h[c->n_inst == 1 ? 0 : inst_of[v]], -(int)level[v]);
         k++;
         if (first[v] >= 0)
             for (int o = 7; o >= 0; o--) stack.push_back(first[v] + o);

@@ -33,7 +33,8 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWidthBlocks = 608;  // 4 x 152 SMs
-constexpr int kSeqWidthMax = 32768;
+constexpr int kSeqWidthMax = 4096;
+constexpr int kMaxDropNodes = 1 << 16;  // nodes with out-of-bounds tails tracked for the ordering pass
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
@@ -52,13 +53,38 @@ __device__ __forceinline__ int agg_inc(int32_t *arr, int slot)
     return v + rank;
 }
 
+// Reduce v over the lanes of `peers` (this lane's group from __match_any_sync,
+// any bit pattern); every lane of the group gets the result.  The lanes of one
+// group run the loop together (same mask, same trip count), 32 shuffles per
+// warp in total whatever the grouping.
+template <class T, class Op>
+__device__ __forceinline__ T group_reduce(unsigned peers, T v, Op op)
+{
+    unsigned rest = peers;
+    T r = __shfl_sync(peers, v, __ffs(rest) - 1);
+    rest &= rest - 1u;
+    while (rest) {
+        const int l = __ffs(rest) - 1;
+        rest &= rest - 1u;
+        r = op(r, __shfl_sync(peers, v, l));
+    }
+    return r;
+}
+
 __device__ __forceinline__ double dist0(double x, double y, double z)
 {
     // vec3::length(): sqrt(x*x + y*y + z*z), evaluated left to right, no FMA
     return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
 }
 
-// ---- Tree::calcTreeWidth ---------------------------------------------------
+// ---- Tree::calcTreeWidth, per instance -------------------------------------
+//
+// Sums of |x| and |x|^2 in the caller's particle order (Tree.cpp:99-103).  Up to
+// kSeqWidthMax particles they are the reference's sequential sums, bit for bit.
+// Above that the sums follow a fixed 64-ary tree over the instance's particles:
+// runs of 64 consecutive values are added sequentially, then runs of 64 of
+// those sums, and so on.  The rule depends only on the instance's own particles,
+// so an instance gets the same half-width alone or sharing the context.
 
 // slot of each particle in the caller's (upload) order: the state is kept in
 // tree order, but the reference sums distances in its particle array order
@@ -68,92 +94,72 @@ __global__ void k_slot_of(int n, const int32_t *__restrict__ id, int32_t *__rest
     if (i < n) slot_of[id[i]] = i;
 }
 
-// Small N: the reference's sequential sums in its particle order, bit for bit
-// (Tree.cpp:99-103).
-__global__ void k_width_seq(const double *px, const double *py, const double *pz, const int32_t *slot_of, int n,
-                            Ctx::Ctl *ctl)
+// first level: task (first caller index, count, destination) over particles
+__global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const double *px, const double *py,
+                                 const double *pz, const int32_t *slot_of, double *buf)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntask) return;
+    const int4 q = task[t];
     double s = 0.0, s2 = 0.0;
-    for (int k = 0; k < n; k++) {
-        int i = slot_of[k];
-        double d = dist0(px[i], py[i], pz[i]);
+    for (int j = 0; j < q.y; j++) {
+        const int i = slot_of[q.x + j];
+        const double d = dist0(px[i], py[i], pz[i]);
         s = __dadd_rn(s, d);
         s2 = __dadd_rn(s2, __dmul_rn(d, d));
     }
-    ctl->sum_d = s;
-    ctl->sum_d2 = s2;
+    buf[2 * (int64_t)q.z] = s;
+    buf[2 * (int64_t)q.z + 1] = s2;
 }
 
-// Large N: deterministic two-stage FP64 sums, also in the caller's order.
-__global__ void k_width_partial(const double *px, const double *py, const double *pz, const int32_t *slot_of, int n,
-                                double *part)
+// higher levels: task (first source sum, count, destination)
+__global__ void k_wsum_sums(int ntask, const int4 *__restrict__ task, double *buf)
 {
-    __shared__ double sh[2][kBlock];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntask) return;
+    const int4 q = task[t];
     double s = 0.0, s2 = 0.0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        int i = slot_of[k];
-        double d = dist0(px[i], py[i], pz[i]);
-        s += d;
-        s2 += d * d;
+    for (int j = 0; j < q.y; j++) {
+        s = __dadd_rn(s, buf[2 * ((int64_t)q.x + j)]);
+        s2 = __dadd_rn(s2, buf[2 * ((int64_t)q.x + j) + 1]);
     }
-    sh[0][threadIdx.x] = s;
-    sh[1][threadIdx.x] = s2;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
-            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = sh[0][0];
-        part[2 * blockIdx.x + 1] = sh[1][0];
-    }
+    buf[2 * (int64_t)q.z] = s;
+    buf[2 * (int64_t)q.z + 1] = s2;
 }
 
-__global__ void k_width_final(const double *part, int nparts, Ctx::Ctl *ctl)
+// one thread per instance: threshold mean + 10 sigma from the instance's sums
+__global__ void k_width_thr(int n_inst, const int64_t *first, const int32_t *final_pos, const double *buf,
+                            double *thr, double *R)
 {
-    if (threadIdx.x != 0) return;
-    double s = 0.0, s2 = 0.0;
-    for (int b = 0; b < nparts; b++) {
-        s += part[2 * b];
-        s2 += part[2 * b + 1];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_inst) return;
+    const int64_t n = first[k + 1] - first[k];
+    R[k] = 0.0;
+    if (n == 0) {
+        thr[k] = 0.0;
+        return;
     }
-    ctl->sum_d = s;
-    ctl->sum_d2 = s2;
+    const double s = buf[2 * (int64_t)final_pos[k]], s2 = buf[2 * (int64_t)final_pos[k] + 1];
+    const double mean = s / (double)n;
+    const double sd = sqrt(__dsub_rn(s2 / (double)n, __dmul_rn(mean, mean)));
+    thr[k] = __dadd_rn(mean, __dmul_rn(10.0, sd));  // mean + acceptanceRatio*stdev (Tree.cpp:89,105)
 }
 
-__global__ void k_width_thr(int n, Ctx::Ctl *ctl)
+// R = max |x| over |x| <= thr (Tree.cpp:107-116); a NaN threshold keeps R = 0
+__global__ void k_width_max(int n, const double *px, const double *py, const double *pz, const int32_t *pinst,
+                            const double *thr, double *R)
 {
-    if (threadIdx.x != 0) return;
-    double mean = ctl->sum_d / (double)n;
-    double sd = sqrt(__dsub_rn(ctl->sum_d2 / (double)n, __dmul_rn(mean, mean)));
-    ctl->thr = __dadd_rn(mean, __dmul_rn(10.0, sd));  // mean + acceptanceRatio*stdev (Tree.cpp:89,105)
-    ctl->R = 0.0;
-}
-
-__global__ void k_width_max(const double *px, const double *py, const double *pz, int n, Ctx::Ctl *ctl)
-{
-    // R = max |x| over |x| <= thr (Tree.cpp:107-116); a NaN threshold keeps R = 0
-    __shared__ unsigned long long sh[kBlock];
-    double thr = ctl->thr;
-    unsigned long long best = 0ull;  // key of +0.0
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double d = dist0(px[i], py[i], pz[i]);
-        if (d <= thr && d > 0.0) {
-            unsigned long long k = (unsigned long long)__double_as_longlong(d);
-            best = k > best ? k : best;
-        }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = i < n ? pinst[i] : -1;
+    unsigned long long best = 0ull;
+    if (i < n) {
+        const double d = dist0(px[i], py[i], pz[i]);
+        if (d <= thr[k] && d > 0.0) best = (unsigned long long)__double_as_longlong(d);
     }
-    sh[threadIdx.x] = best;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) sh[threadIdx.x] = max(sh[threadIdx.x], sh[threadIdx.x + w]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0 && sh[0] != 0ull) atomicMax((unsigned long long *)&ctl->R, sh[0]);
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    best = group_reduce(peers, best, [](unsigned long long a, unsigned long long b) { return a > b ? a : b; });
+    if (k >= 0 && best != 0ull && (threadIdx.x & 31) == __ffs(peers) - 1)
+        atomicMax((unsigned long long *)&R[k], best);
 }
 
 // ---- level-wise partition --------------------------------------------------
@@ -173,39 +179,55 @@ __device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
     k[8] = okey(cz);
 }
 
-__global__ void k_root_init(Nodes nd, Ctx::Ctl *ctl, int n, int thresh, int32_t *pnode)
+// root of instance k is node k (Tree.cpp:28-33: centre at the origin, half-width
+// from calcTreeWidth, depth 0)
+__global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *first, const double *R, int thresh,
+                            int32_t *pnode)
 {
-    if (threadIdx.x != 0) return;
-    double R = ctl->R;
-    nd.start[0] = 0;
-    nd.count[0] = n;
-    nd.ndrop[0] = 0;
-    nd.first[0] = -1;
-    nd.parent[0] = -1;
-    nd.level[0] = 0;
-    nd.cx[0] = 0.0;
-    nd.cy[0] = 0.0;
-    nd.cz[0] = 0.0;
-    uint8_t mode = n == 0 ? MODE_EMPTY : n == 1 ? MODE_VEC1 : n < thresh ? MODE_SER_ENTRY : MODE_PAR;
-    nd.mode[0] = mode;
-    uint8_t needs = (mode == MODE_PAR || mode == MODE_SER_ENTRY) ? 1 : 0;
-    nd.needs[0] = needs;
-    nd.leafpos[0] = (mode == MODE_VEC1) ? 0 : -1;
-    if (mode == MODE_VEC1) pnode[0] = 0;
-    if (needs) set_bounds(nd, 0, R);
-    ctl->node_count = 1;
-    ctl->next_needs = needs;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_inst) return;
+    const int32_t start = (int32_t)first[k];
+    const int32_t n = (int32_t)(first[k + 1] - first[k]);
+    nd.start[k] = start;
+    nd.count[k] = n;
+    nd.ndrop[k] = 0;
+    nd.first[k] = -1;
+    nd.parent[k] = -1;
+    nd.level[k] = 0;
+    nd.cx[k] = 0.0;
+    nd.cy[k] = 0.0;
+    nd.cz[k] = 0.0;
+    nd.radius[k] = R[k];
+    nd.inst[k] = k;
+    const uint8_t mode = n == 0 ? MODE_EMPTY : n == 1 ? MODE_VEC1 : n < thresh ? MODE_SER_ENTRY : MODE_PAR;
+    nd.mode[k] = mode;
+    const uint8_t needs = (mode == MODE_PAR || mode == MODE_SER_ENTRY) ? 1 : 0;
+    nd.needs[k] = needs;
+    nd.leafpos[k] = (mode == MODE_VEC1) ? start : -1;
+    if (mode == MODE_VEC1) pnode[start] = k;
+    if (needs) {
+        set_bounds(nd, k, R[k]);
+        atomicAdd(&ctl->next_needs, 1);
+    }
+}
+
+__global__ void k_ctl_reset(Ctx::Ctl *ctl, int n_inst)
+{
+    ctl->node_count = n_inst;
+    ctl->next_needs = 0;
     ctl->err_code = 0;
     ctl->err_info = 0;
     ctl->any_drop = 0;
+    ctl->ndrop_nodes = 0;
 }
 
-__global__ void k_init_positions(int n, int root_needs, int32_t *perm, int32_t *posnode)
+__global__ void k_init_positions(int n, const int32_t *pinst, const uint8_t *needs, int32_t *perm, int32_t *posnode)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     perm[i] = i;
-    posnode[i] = root_needs ? 0 : -1;
+    const int k = pinst[i];
+    posnode[i] = needs[k] ? k : -1;
 }
 
 // digit of every particle of a node being split at this level
@@ -238,7 +260,7 @@ __global__ void k_digit(int n, int64_t base, const int32_t *__restrict__ posnode
 // allocates the 8-child block (one atomic per warp) and writes the parent.
 __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, int64_t node_cap, Nodes nd,
                         Ctx::Ctl *ctl, const int32_t *__restrict__ hist, int32_t *__restrict__ cursor,
-                        int max_depth)
+                        int max_depth, int32_t *__restrict__ drop_list)
 {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int lane = lane_id();
@@ -264,6 +286,10 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
     if (needs && o == 0) {
         nd.ndrop[nid] = ndrop;
         if (ndrop) ctl->any_drop = 1;
+        if (ndrop >= 2) {  // tails to put in upload order after the partition
+            int k = atomicAdd(&ctl->ndrop_nodes, 1);
+            if (k < kMaxDropNodes) drop_list[k] = (int32_t)nid;
+        }
         int32_t acc = start;
         for (int d = 0; d < 9; d++) {
             cursor[9 * j + d] = acc;
@@ -307,8 +333,8 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
                 nd.leafpos[nid] = -1;
             }
             // child o: centre c + r*(+-0.5), radius r/2 (Node.cpp:433-443, 630-642)
-            const double r = ldexp(ctl->R, -level);
-            const double rc = ldexp(ctl->R, -(level + 1));
+            const double r = nd.radius[nid];
+            const double rc = r / 2;  // Node.cpp:440
             const int64_t c = c0 + o;
             int32_t s = start;
             for (int d = 0; d < o; d++) s += h[d];
@@ -322,6 +348,8 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
             nd.first[c] = -1;
             nd.parent[c] = (int32_t)nid;
             nd.level[c] = (int8_t)(level + 1);
+            nd.radius[c] = rc;
+            nd.inst[c] = nd.inst[nid];
             uint8_t cm;
             if (cc == 0)
                 cm = MODE_EMPTY;
@@ -379,10 +407,12 @@ __global__ void k_scatter(int n, int64_t base, const int32_t *__restrict__ posno
 // tails.
 constexpr int kDropSort = 4096;
 
-__global__ void k_sort_drops(int64_t nnodes, Nodes nd, int32_t *perm, const int32_t *id, int32_t *scratch)
+__global__ void k_sort_drops(int ndn, const int32_t *drop_list, Nodes nd, int32_t *perm, const int32_t *id,
+                             int32_t *scratch)
 {
     __shared__ long long key[kDropSort];
-    for (int64_t nid = blockIdx.x; nid < nnodes; nid += gridDim.x) {
+    for (int q = blockIdx.x; q < ndn; q += gridDim.x) {
+        const int64_t nid = drop_list[q];
         const int32_t nd8 = nd.ndrop[nid];
         if (nd8 < 2) continue;
         const int32_t e = nd.start[nid] + nd.count[nid];
@@ -528,7 +558,7 @@ struct Sums {
 };
 
 __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P, const double *gas_prefix,
-                          int gas_uniform, double theta, double R)
+                          const int32_t *gas_off, const uint8_t *gas_uni, double theta)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= count_lvl) return;
@@ -537,7 +567,6 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     if (cnt == 0) return;  // empty child: no kernel reads it (parents test the count first)
     int32_t start = nd.start[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
     uint8_t mode = nd.mode[nid];
-    int level = nd.level[nid];
     Sums tot, own;  // tot: whole routed range; own: the reference's mass set
     tot.zero();
     own.zero();
@@ -617,7 +646,8 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
             cy = own.my * im;
             cz = own.mz * im;
         }
-        if (gas_uniform) gas = gas_prefix[own.ng];
+        const int k = nd.inst[nid];
+        if (gas_uni[k]) gas = gas_prefix[gas_off[k] + own.ng];
         if (own.g > 0) {
             double ig = 1.0 / own.g;
             mvx = own.gvx * ig;
@@ -643,7 +673,7 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     if (leaf) {
         mac = -1.0f;
     } else {
-        double q = ldexp(R, -level) / theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
+        double q = nd.radius[nid] / theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
         mac = (float)(q * q);
     }
     nd.wB[nid] = make_float4(lx, ly, lz, mac);
@@ -653,49 +683,52 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
         nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)gas);
 }
 
-// count, min and max mass of the gas particles (grid-wide, order-preserving
-// integer atomics on the positive masses)
-__global__ void k_gas_stats(int n, const double *m, const uint8_t *type, Ctx::Ctl *ctl)
+// count, min and max mass of each instance's gas particles (order-preserving
+// integer atomics; peers of one instance in a warp combine first)
+__global__ void k_gas_stats(int n, const double *m, const uint8_t *type, const int32_t *pinst, int32_t *cnt,
+                            long long *kmin, long long *kmax)
 {
-    long long lo = LLONG_MAX, hi = LLONG_MIN;
-    int cnt = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (type[i] == 2) {
-            long long k = okey(m[i]);
-            lo = min(lo, k);
-            hi = max(hi, k);
-            cnt++;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    }
-    if ((threadIdx.x & 31) == 0 && cnt) {
-        atomicMin((long long *)&ctl->gas_key_min, lo);
-        atomicMax((long long *)&ctl->gas_key_max, hi);
-        atomicAdd(&ctl->ngas_total, cnt);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool g = i < n && type[i] == 2;
+    const int k = g ? pinst[i] : -1;
+    long long lo = g ? okey(m[i]) : LLONG_MAX, hi = g ? okey(m[i]) : LLONG_MIN;
+    int c = g ? 1 : 0;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    lo = group_reduce(peers, lo, [](long long a, long long b) { return a < b ? a : b; });
+    hi = group_reduce(peers, hi, [](long long a, long long b) { return a > b ? a : b; });
+    c = group_reduce(peers, c, [](int a, int b) { return a + b; });
+    if (g &&(threadIdx.x & 31) == __ffs(peers) - 1) {
+        atomicMin(&kmin[k], lo);
+        atomicMax(&kmax[k], hi);
+        atomicAdd(&cnt[k], c);
     }
 }
 
-__global__ void k_gas_stats_init(Ctx::Ctl *ctl)
+__global__ void k_gas_stats_init(int n_inst, int32_t *cnt, long long *kmin, long long *kmax)
 {
-    ctl->gas_key_min = LLONG_MAX;
-    ctl->gas_key_max = LLONG_MIN;
-    ctl->ngas_total = 0;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_inst) return;
+    cnt[k] = 0;
+    kmin[k] = LLONG_MAX;
+    kmax[k] = LLONG_MIN;
 }
 
 // gasMass of a node whose gas particles all weigh mg: the reference adds them
-// one at a time (Node.cpp:479-480, 681), so its value is the k-th partial sum
-__global__ void k_gas_prefix(int ngas, double mg, double *out)
+// one at a time (Node.cpp:479-480, 681), so its value is the k-th partial sum.
+// One thread per instance with a uniform gas mass.
+__global__ void k_gas_prefix(int n_inst, const int32_t *cnt, const long long *kmin, const uint8_t *uni,
+                             const int32_t *off, double *out)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_inst || !uni[k]) return;
+    const long long key = kmin[k];
+    const double mg = __longlong_as_double(key >= 0 ? key : (key ^ 0x7FFFFFFFFFFFFFFFLL));
     double s = 0.0;
-    out[0] = 0.0;
-    for (int k = 1; k <= ngas; k++) {
+    double *t = out + off[k];
+    t[0] = 0.0;
+    for (int j = 1; j <= cnt[k]; j++) {
         s = __dadd_rn(s, mg);
-        out[k] = s;
+        t[j] = s;
     }
 }
 
@@ -727,7 +760,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
 #define G(x) \
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
-    G(cx) G(cy) G(cz) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
+    G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
     G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(tfirst) G(tfirstm) G(wA) G(wB) G(wD) G(flag)
     G(rho)
 #undef G
@@ -751,48 +784,46 @@ static int ensure_hist(Ctx *c, size_t nodes_in_level)
     return AG2_OK;
 }
 
-static double key_to_double(long long k)
+// Gas statistics depend only on masses, types and instances, so they are
+// refreshed when those change (upload, ag2_set_field of the mass,
+// ag2_set_instances), not every build.
+static int prepare_gas_tables(Ctx *c, int n)
 {
-    long long b = k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFLL);
-    double x;
-    std::memcpy(&x, &b, 8);
-    return x;
-}
-
-// Gas statistics depend only on masses and types, so they are refreshed when
-// those change (upload, ag2_set_field of the mass), not every build.
-static int prepare_gas_table(Ctx *c, int n, bool *uniform)
-{
-    if (c->gas_stats_dirty) {
-        Particles &S = c->S();
-        AG2_LAUNCH(c, k_gas_stats_init, 1, 1, 0, c->ctl);
-        int sms = 152;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-        unsigned blocks = std::min(grid_for(n, kBlock), (unsigned)(4 * sms));
-        AG2_LAUNCH(c, k_gas_stats, blocks, kBlock, 0, n, S.m, S.type, c->ctl);
-        int rc = sync_ctl(c);
-        if (rc) return rc;
-        const Ctx::Ctl &h = *c->ctl_host;
-        c->ngas = h.ngas_total;
-        c->gas_mass_min = h.ngas_total ? key_to_double(h.gas_key_min) : 0.0;
-        c->gas_mass_max = h.ngas_total ? key_to_double(h.gas_key_max) : 0.0;
-        c->gas_stats_dirty = false;
+    if (!c->gas_stats_dirty) return AG2_OK;
+    const int K = c->n_inst;
+    Particles &S = c->S();
+    AG2_LAUNCH(c, k_gas_stats_init, grid_for(K, kBlock), kBlock, 0, K, c->gas_cnt, c->gas_kmin, c->gas_kmax);
+    AG2_LAUNCH(c, k_gas_stats, grid_for(n, kBlock), kBlock, 0, n, S.m, S.type, c->pinst, c->gas_cnt, c->gas_kmin,
+               c->gas_kmax);
+    std::vector<int32_t> cnt(K);
+    std::vector<long long> lo(K), hi(K);
+    AG2_CUDA(c, cudaMemcpyAsync(cnt.data(), c->gas_cnt, K * 4, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(lo.data(), c->gas_kmin, K * 8, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(hi.data(), c->gas_kmax, K * 8, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<int32_t> off(K);
+    std::vector<uint8_t> uni(K);
+    size_t total = 0;
+    c->ngas = 0;
+    for (int k = 0; k < K; k++) {
+        off[k] = (int32_t)total;
+        uni[k] = cnt[k] > 0 && lo[k] == hi[k];
+        total += (size_t)cnt[k] + 1;
+        c->ngas += cnt[k];
     }
-    *uniform = c->ngas > 0 && c->gas_mass_min == c->gas_mass_max;
-    size_t need = (size_t)c->ngas + 1;
-    if (need > c->gas_prefix_cap) {
+    if (total > c->gas_prefix_cap) {
         if (c->gas_prefix) cudaFree(c->gas_prefix);
         c->gas_prefix = nullptr;
-        if (cudaMalloc(&c->gas_prefix, need * sizeof(double)) != cudaSuccess)
+        if (cudaMalloc(&c->gas_prefix, total * sizeof(double)) != cudaSuccess)
             return set_err(c, AG2_E_NOMEM, "gas table allocation failed");
-        c->gas_prefix_cap = need;
-        c->gas_table_mass = -1.0;
+        c->gas_prefix_cap = total;
     }
-    if (*uniform && (c->gas_table_mass != c->gas_mass_min || c->gas_table_n != c->ngas)) {
-        AG2_LAUNCH(c, k_gas_prefix, 1, 1, 0, c->ngas, c->gas_mass_min, c->gas_prefix);
-        c->gas_table_mass = c->gas_mass_min;
-        c->gas_table_n = c->ngas;
-    }
+    AG2_CUDA(c, cudaMemcpyAsync(c->gas_off, off.data(), K * 4, cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(c->gas_uni, uni.data(), K, cudaMemcpyHostToDevice, c->stream));
+    AG2_LAUNCH(c, k_gas_prefix, grid_for(K, kBlock), kBlock, 0, K, c->gas_cnt, c->gas_kmin, c->gas_uni, c->gas_off,
+               c->gas_prefix);
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors above go out of scope
+    c->gas_stats_dirty = false;
     return AG2_OK;
 }
 
@@ -800,35 +831,45 @@ int build_tree(Ctx *c)
 {
     const int n = (int)c->n;
     c->have_tree = false;
-    Particles &S = c->S();
     int rc;
-    bool gas_uniform = false;
-    if ((rc = prepare_gas_table(c, n, &gas_uniform)) != AG2_OK) return rc;
+    if ((rc = ensure_instance_tables(c)) != AG2_OK) return rc;
+    const int K = c->n_inst;
+    Particles &S = c->S();
+    if ((rc = prepare_gas_tables(c, n)) != AG2_OK) return rc;
 
-    // root half-width
+    // root half-width of every instance
+    AG2_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream));
     if (n > 0) {
         AG2_LAUNCH(c, k_slot_of, grid_for(n, kBlock), kBlock, 0, n, S.id, c->slot_of);
-        if (n <= kSeqWidthMax) {
-            AG2_LAUNCH(c, k_width_seq, 1, 1, 0, S.px, S.py, S.pz, c->slot_of, n, c->ctl);
-        } else {
-            AG2_LAUNCH(c, k_width_partial, kWidthBlocks, kBlock, 0, S.px, S.py, S.pz, c->slot_of, n, c->width_part);
-            AG2_LAUNCH(c, k_width_final, 1, 32, 0, c->width_part, kWidthBlocks, c->ctl);
+        for (size_t l = 0; l + 1 < c->wsum_level.size(); l++) {
+            const int nt = c->wsum_level[l + 1] - c->wsum_level[l];
+            const int4 *tk = c->wsum_task + c->wsum_level[l];
+            if (l == 0)
+                AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, S.px, S.py, S.pz, c->slot_of,
+                           c->width_part);
+            else
+                AG2_LAUNCH(c, k_wsum_sums, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->width_part);
         }
-        AG2_LAUNCH(c, k_width_thr, 1, 32, 0, n, c->ctl);
-        AG2_LAUNCH(c, k_width_max, kWidthBlocks, kBlock, 0, S.px, S.py, S.pz, n, c->ctl);
-    } else {
-        AG2_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream));
     }
+    AG2_LAUNCH(c, k_width_thr, grid_for(K, kBlock), kBlock, 0, K, c->inst_first, c->wsum_final, c->width_part,
+               c->width_thr, c->inst_R);
+    if (n > 0)
+        AG2_LAUNCH(c, k_width_max, grid_for(n, kBlock), kBlock, 0, n, S.px, S.py, S.pz, c->pinst, c->width_thr,
+                   c->inst_R);
     phase_mark(c, "build: root width");
-    if ((rc = ensure_node_capacity(c, 1024)) != AG2_OK) return rc;
+    if ((rc = ensure_node_capacity(c, (size_t)K + 1024)) != AG2_OK) return rc;
     const int thresh = c->prm.split_threshold;
-    AG2_LAUNCH(c, k_root_init, 1, 32, 0, c->nd, c->ctl, n, thresh, c->pnode);
+    AG2_LAUNCH(c, k_ctl_reset, 1, 1, 0, c->ctl, K);
+    AG2_LAUNCH(c, k_root_init, grid_for(K, kBlock), kBlock, 0, K, c->nd, c->ctl, c->inst_first, c->inst_R, thresh,
+               c->pnode);
+    c->inst_R_h.resize(K);
+    AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-    c->root_radius = c->ctl_host->R;
+    c->root_radius = c->inst_R_h[0];
     int root_needs = c->ctl_host->next_needs;
-    AG2_LAUNCH(c, k_init_positions, grid_for(n, kBlock), kBlock, 0, n, root_needs, c->perm, c->posnode);
+    AG2_LAUNCH(c, k_init_positions, grid_for(n, kBlock), kBlock, 0, n, c->pinst, c->nd.needs, c->perm, c->posnode);
 
-    c->level_base.assign({0, 1});
+    c->level_base.assign({0, (int64_t)K});
     int level = 0;
     int needs = root_needs;
     while (needs > 0) {
@@ -842,7 +883,7 @@ int build_tree(Ctx *c)
         AG2_LAUNCH(c, k_digit, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, Sp.px, Sp.py, Sp.pz,
                    c->nd, c->digit, c->hist);
         AG2_LAUNCH(c, k_nodes, grid_for((size_t)cnt_lvl * 8, kBlock), kBlock, 0, base, cnt_lvl, level, thresh,
-                   (int64_t)c->node_cap, c->nd, c->ctl, c->hist, c->cursor, (int)AG2_MAX_DEPTH);
+                   (int64_t)c->node_cap, c->nd, c->ctl, c->hist, c->cursor, (int)AG2_MAX_DEPTH, c->drop_list);
         AG2_CUDA(c, cudaMemcpyAsync(c->perm2, c->perm, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
         AG2_CUDA(c, cudaMemsetAsync(c->posnode2, 0xFF, n * sizeof(int32_t), c->stream));
         AG2_LAUNCH(c, k_scatter, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, c->digit, c->nd,
@@ -865,12 +906,12 @@ int build_tree(Ctx *c)
     phase_mark(c, "build: levels");
     c->max_level = (int)c->level_base.size() - 2;
     c->nnodes = c->level_base.back();
-    c->ninternal = (c->nnodes - 1) / 8;
-    if (c->ctl_host->any_drop) {
-        int sms = 152;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-        AG2_LAUNCH(c, k_sort_drops, (unsigned)(4 * sms), kBlock, 0, c->nnodes, c->nd, c->perm, S.id, c->perm2);
-    }
+    c->ninternal = (c->nnodes - K) / 8;
+    if (c->ctl_host->ndrop_nodes > kMaxDropNodes)
+        return set_err(c, AG2_E_CAPACITY, "more than 65536 nodes with out-of-bounds particles");
+    if (c->ctl_host->ndrop_nodes > 0)
+        AG2_LAUNCH(c, k_sort_drops, (unsigned)c->ctl_host->ndrop_nodes, kBlock, 0, c->ctl_host->ndrop_nodes,
+                   c->drop_list, c->nd, c->perm, S.id, c->perm2);
 
     // particle state into tree order
     Particles &src = c->st[c->cur];
@@ -885,7 +926,7 @@ int build_tree(Ctx *c)
         int64_t base = c->level_base[L];
         int64_t cnt = c->level_base[L + 1] - base;
         AG2_LAUNCH(c, k_moments, grid_for((size_t)cnt, kBlock), kBlock, 0, base, cnt, c->nd, c->S(),
-                   c->gas_prefix, gas_uniform ? 1 : 0, c->prm.theta, c->root_radius);
+                   c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
     }
     phase_mark(c, "build: moments");
     c->have_tree = true;

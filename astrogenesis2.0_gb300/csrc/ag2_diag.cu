@@ -29,18 +29,21 @@ __device__ double softening_kernel_d(double u)
 
 // One block per sample: threads stride over all sources, FP64 throughout.
 template <bool kGeneral>
-__global__ void __launch_bounds__(kDirectBlock) k_direct(int n, const double *__restrict__ px,
-                                                         const double *__restrict__ py, const double *__restrict__ pz,
-                                                         const double *__restrict__ m, const int32_t *__restrict__ slot,
-                                                         double e0, double G, double *__restrict__ out)
+__global__ void __launch_bounds__(kDirectBlock) k_direct(const double *__restrict__ px, const double *__restrict__ py,
+                                                         const double *__restrict__ pz, const double *__restrict__ m,
+                                                         const int32_t *__restrict__ slot, const int32_t *pinst,
+                                                         const int64_t *first, double e0, double G,
+                                                         double *__restrict__ out)
 {
     __shared__ double red[3][kDirectBlock / 32];
     const int s = blockIdx.x;
     const int i = slot[s];
+    const int k = pinst[i];
+    const int j0 = (int)first[k], n = (int)first[k + 1];  // sources: the sample's own simulation
     const double xi = px[i], yi = py[i], zi = pz[i];
     const double e02 = e0 * e0;
     double ax = 0, ay = 0, az = 0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int j = j0 + threadIdx.x; j < n; j += blockDim.x) {
         if (j == i) continue;
         double mj = m[j];
         if (mj == 0.0) continue;
@@ -156,6 +159,8 @@ int run_direct_sum(Ctx *c, size_t ns, const int64_t *ids_host, double *out_host)
 {
     const int n = (int)c->n;
     if (ns == 0) return AG2_OK;
+    int rc = ensure_instance_tables(c);
+    if (rc) return rc;
     if (ns > c->cap) return set_err(c, AG2_E_INVALID, "more samples than particles");
     std::vector<std::pair<int32_t, size_t>> order(ns);
     for (size_t k = 0; k < ns; k++) {
@@ -172,11 +177,11 @@ int run_direct_sum(Ctx *c, size_t ns, const int64_t *ids_host, double *out_host)
     AG2_LAUNCH(c, k_id_to_slot, grid_for(n, 256), 256, 0, n, S.id, d_want, (int)ns, d_slot);
     const bool general = !(c->prm.e0 > 0.0 && c->prm.e0 < 0.6);
     if (general)
-        AG2_LAUNCH(c, k_direct<true>, (unsigned)ns, kDirectBlock, 0, n, S.px, S.py, S.pz, S.m, d_slot, c->prm.e0,
-                   c->prm.G, d_out);
+        AG2_LAUNCH(c, k_direct<true>, (unsigned)ns, kDirectBlock, 0, S.px, S.py, S.pz, S.m, d_slot, c->pinst,
+                   c->inst_first, c->prm.e0, c->prm.G, d_out);
     else
-        AG2_LAUNCH(c, k_direct<false>, (unsigned)ns, kDirectBlock, 0, n, S.px, S.py, S.pz, S.m, d_slot, c->prm.e0,
-                   c->prm.G, d_out);
+        AG2_LAUNCH(c, k_direct<false>, (unsigned)ns, kDirectBlock, 0, S.px, S.py, S.pz, S.m, d_slot, c->pinst,
+                   c->inst_first, c->prm.e0, c->prm.G, d_out);
     std::vector<double> tmp(3 * ns);
     AG2_CUDA(c, cudaMemcpyAsync(tmp.data(), d_out, 3 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));

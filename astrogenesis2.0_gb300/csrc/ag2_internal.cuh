@@ -48,6 +48,8 @@ struct Nodes {
     uint8_t *needs;      // node gets a digit pass at its level
     uint8_t *childmask;  // bit o: child o has mass != 0
     double *cx, *cy, *cz;
+    double *radius;      // half-width (the root's R halved per level, exactly as Node.cpp:440)
+    int32_t *inst;       // simulation instance the node belongs to
     int64_t *bkey;       // 9 ordered-integer keys per node: lo xyz, hi xyz, centre xyz
     // moments (reference semantics, FP64)
     double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz;
@@ -81,6 +83,7 @@ struct Ctx {
     bool have_tree = false;
     double root_radius = 0.0;
     int64_t launches = 0;
+    bool debug_sync = false;  // AG2_DEBUG_SYNC=1: synchronise and check after every launch
     int64_t inter_grav = 0, inter_sph = 0;
     std::string err;
 
@@ -94,6 +97,7 @@ struct Ctx {
     int32_t *slot_of = nullptr;   // tree-order slot of each upload index
     int32_t *finalnode = nullptr; // SPH / visual density result node per slot
     int32_t *nodelist = nullptr;  // compacted node list (SPH density nodes)
+    int32_t *drop_list = nullptr; // nodes with out-of-bounds tails (65536 entries)
     uint8_t *digit = nullptr;
     int32_t *hist = nullptr;      // 9 per node of a level
     int32_t *cursor = nullptr;
@@ -102,7 +106,11 @@ struct Ctx {
     size_t gas_prefix_cap = 0;
     double *staging = nullptr;    // 6n doubles for upload/download
     uint8_t *staging_u8 = nullptr;
-    double *width_part = nullptr; // per-block partial sums of the root width
+    double *width_part = nullptr; // partial sums of the root width (pairs), laid out by the task table
+    int4 *wsum_task = nullptr;    // root-width summation tasks, level after level
+    int32_t *wsum_final = nullptr; // per instance: position of its final pair
+    std::vector<int32_t> wsum_level;  // task offsets of each level
+    double *width_thr = nullptr;  // mean + 10 sigma per instance
     double gas_table_mass = -1.0; // gas particle mass the gasMass table was built for
     int32_t gas_table_n = -1;
     bool gas_uniform = false;
@@ -111,6 +119,30 @@ struct Ctx {
     double gas_mass_min = 0.0, gas_mass_max = 0.0;
     double tree_theta = 0.0;      // opening angle baked into the walk records
     int walk_variant = 1;         // FP32 walk register-budget variant (ag2_autotune)
+
+    // Independent simulations ("instances") sharing this context: instance k
+    // owns upload indices [inst_first[k], inst_first[k+1]); in tree order it
+    // owns the same slot range (every build only permutes inside each root's
+    // range), its tree's root is node k, and its walk groups never mix with
+    // another instance's.
+    int32_t n_inst = 1;
+    std::vector<int64_t> inst_first_h{0, 0};
+    std::vector<double> inst_massInH_h{0.0};
+    size_t inst_cap = 0;
+    int64_t *inst_first = nullptr;  // device, n_inst + 1
+    double *inst_R = nullptr;       // device, root half-width per instance
+    double *inst_massInH = nullptr; // device
+    int32_t *pinst = nullptr;       // device, instance of each slot
+    int4 *groups = nullptr;         // device walk groups: (first slot, lanes, instance, 0)
+    int32_t ngroups = 0;
+    size_t groups_cap = 0;
+    bool inst_dirty = true;         // instance tables need uploading
+    // gasMass tables: instance k's sequential partial sums start at gas_off[k]
+    int32_t *gas_off = nullptr;     // device
+    uint8_t *gas_uni = nullptr;     // device: instance's gas particles share one mass
+    int32_t *gas_cnt = nullptr;     // device scratch: gas count per instance
+    long long *gas_kmin = nullptr, *gas_kmax = nullptr;  // device scratch
+    std::vector<double> inst_R_h;   // host copy after a build
 
     // small device control block
     struct Ctl {
@@ -125,7 +157,7 @@ struct Ctx {
         long long gas_key_min, gas_key_max;
         unsigned long long inter_grav, inter_sph;
         int32_t list_count;
-        int32_t pad;
+        int32_t ndrop_nodes;
     };
     Ctl *ctl = nullptr;      // device
     Ctl *ctl_host = nullptr; // pinned mirror
@@ -174,20 +206,25 @@ int cuda_check(Ctx *c, cudaError_t e, const char *what);
     } while (0)
 
 inline unsigned grid_for(size_t n, int block) { return (unsigned)((n + block - 1) / block); }
+inline bool launch_ok(unsigned long long g) { return g > 0; }
+inline bool launch_ok(const dim3 &g) { return g.x > 0 && g.y > 0 && g.z > 0; }
 
 // launch accounting: every kernel launch goes through this
 #define AG2_LAUNCH(c, kern, grid, block, smem, ...)                          \
     do {                                                                     \
-        if ((grid) > 0) {                                                    \
+        if (launch_ok(grid)) {                                               \
             kern<<<(grid), (block), (smem), (c)->stream>>>(__VA_ARGS__);     \
             (c)->launches++;                                                 \
             cudaError_t _le = cudaGetLastError();                            \
+            if (_le == cudaSuccess && (c)->debug_sync)                       \
+                _le = cudaStreamSynchronize((c)->stream);                    \
             if (_le != cudaSuccess) return cuda_check(c, _le, #kern);        \
         }                                                                    \
     } while (0)
 
 // entry points implemented per translation unit
 int build_tree(Ctx *c);
+int ensure_instance_tables(Ctx *c);
 int ensure_node_capacity(Ctx *c, size_t need);
 int run_forces(Ctx *c);
 int run_sph_density(Ctx *c);

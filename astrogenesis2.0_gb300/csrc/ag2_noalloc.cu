@@ -8,14 +8,17 @@
 // would break the capture.  Such callers hand in their own device buffers for
 // the positions and the result; the per-block partial sums this computation
 // needs live in a fixed array in this file instead of in memory allocated by a
-// context.  The kernels are copies of the context path's width kernels reading
+// context.  The kernels follow the context path's width rule (sequential sums
+// up to 4096 particles, a 64-ary tree of sequential runs above) reading
 // xyz-interleaved positions, and give bit-identical results to ag2_build_tree's
-// root half-width (ag2_root_radius).
+// root half-width (ag2_root_radius).  The scratch holds the tree's second level
+// (one pair per 4096 particles), which bounds n at AG2_NOALLOC_MAX_PARTICLES.
 //
-// The scratch array is 16 KiB per device, owned by this library from its first
+// The scratch array is 32 KiB per device, owned by this library from its first
 // use on a device until the process exits.  Every call shares it and leaves
 // the previous call's values in it, so calls that overlap on the GPU (on
 // different streams, or from different host threads) race; serialise them.
+#include <cstdint>
 #include <mutex>
 
 #include "ag2_internal.cuh"
@@ -25,21 +28,22 @@ namespace ag2 {
 namespace {
 
 constexpr int kNaBlock = 256;
-constexpr int kNaBlocks = 608;        // same fixed grid as the context path
-constexpr int kNaSeqMax = 32768;      // sequential sums below this, as the context path
+constexpr int kNaBlocks = 608;        // grid of the max pass
+constexpr int kNaSlots = 2040;        // second-level pairs held in the scratch (8,355,840 particles)
+constexpr int kNaSeqMax = 4096;       // sequential sums up to this, as the context path
 constexpr int kNaMaxDevices = 64;
 
 struct NoAllocScratch {
-    double part[2 * kNaBlocks];       // per-block sums of |x| and |x|^2
+    double part[2 * kNaSlots];        // second-level sums of |x| and |x|^2 (4096 particles each)
     double sum_d, sum_d2, thr;
     unsigned long long R_bits;        // running max of |x| (bit pattern of a positive double)
 };
-static_assert(sizeof(NoAllocScratch) <= 16384, "scratch larger than its stated size");
+static_assert(sizeof(NoAllocScratch) <= 32768, "scratch larger than its stated size");
 
 // The scratch itself: a file-scope device array of fixed size.  Host code must
 // not pass its name to a kernel (that is a host-side stand-in, not a device
 // address); it uses the address obtained with cudaGetSymbolAddress below.
-static __device__ __align__(256) unsigned char g_noalloc_scratch[16384];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[32768];
 
 std::mutex g_setup_mutex;
 void *g_scratch_addr[kNaMaxDevices] = {};
@@ -71,41 +75,50 @@ __global__ void k_na_seq(const double *pos, int n, NoAllocScratch *s)
     s->sum_d2 = b;
 }
 
-__global__ void k_na_partial(const double *pos, int n, NoAllocScratch *s)
+// second level of the 64-ary tree: entry e sums the 64 runs of 64 particles
+// starting at particle 4096*e, each run sequentially, the runs in order
+__global__ void k_na_level2(const double *pos, int n, int nent, NoAllocScratch *s)
 {
-    __shared__ double sh[2][kNaBlock];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nent) return;
     double a = 0.0, b = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double d = na_dist(pos, i);
-        a += d;
-        b += d * d;
-    }
-    sh[0][threadIdx.x] = a;
-    sh[1][threadIdx.x] = b;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
-            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+    for (int r = 0; r < 64; r++) {
+        const int64_t lo = (int64_t)e * 4096 + (int64_t)r * 64;
+        if (lo >= n) break;
+        const int64_t hi = min(lo + 64, (int64_t)n);
+        double ra = 0.0, rb = 0.0;
+        for (int64_t q = lo; q < hi; q++) {
+            double d = na_dist(pos, (int)q);
+            ra = __dadd_rn(ra, d);
+            rb = __dadd_rn(rb, __dmul_rn(d, d));
         }
-        __syncthreads();
+        a = __dadd_rn(a, ra);
+        b = __dadd_rn(b, rb);
     }
-    if (threadIdx.x == 0) {
-        s->part[2 * blockIdx.x] = sh[0][0];
-        s->part[2 * blockIdx.x + 1] = sh[1][0];
-    }
+    s->part[2 * e] = a;
+    s->part[2 * e + 1] = b;
 }
 
-__global__ void k_na_final(NoAllocScratch *s)
+// remaining levels: runs of 64 pairs, in place, until one pair is left
+__global__ void k_na_final(int nent, NoAllocScratch *s)
 {
     if (threadIdx.x != 0) return;
-    double a = 0.0, b = 0.0;
-    for (int k = 0; k < kNaBlocks; k++) {
-        a += s->part[2 * k];
-        b += s->part[2 * k + 1];
+    int cnt = nent;
+    while (cnt > 1) {
+        const int nn = (cnt + 63) / 64;
+        for (int j = 0; j < nn; j++) {
+            double a = 0.0, b = 0.0;
+            for (int q = 64 * j; q < min(64 * j + 64, cnt); q++) {
+                a = __dadd_rn(a, s->part[2 * q]);
+                b = __dadd_rn(b, s->part[2 * q + 1]);
+            }
+            s->part[2 * j] = a;
+            s->part[2 * j + 1] = b;
+        }
+        cnt = nn;
     }
-    s->sum_d = a;
-    s->sum_d2 = b;
+    s->sum_d = s->part[0];
+    s->sum_d2 = s->part[1];
 }
 
 __global__ void k_na_thr(int n, NoAllocScratch *s)
@@ -178,8 +191,9 @@ extern "C" int ag2_root_radius_noalloc(const double *pos, int64_t n, double *rad
     if (ni <= kNaSeqMax) {
         k_na_seq<<<1, 1, 0, st>>>(pos, ni, s);
     } else {
-        k_na_partial<<<kNaBlocks, kNaBlock, 0, st>>>(pos, ni, s);
-        k_na_final<<<1, 32, 0, st>>>(s);
+        const int nent = (ni + 4095) / 4096;
+        k_na_level2<<<(nent + kNaBlock - 1) / kNaBlock, kNaBlock, 0, st>>>(pos, ni, nent, s);
+        k_na_final<<<1, 32, 0, st>>>(nent, s);
     }
     k_na_thr<<<1, 32, 0, st>>>(ni, s);
     k_na_max<<<kNaBlocks, kNaBlock, 0, st>>>(pos, ni, s);

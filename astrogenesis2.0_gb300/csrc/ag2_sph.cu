@@ -34,7 +34,8 @@ struct TreeView {
     const int32_t *start, *count, *ndrop, *parent, *leafpos, *pnode, *refnode;
     const int8_t *level;
     const uint8_t *mode;
-    const double *mass, *comx, *comy, *comz, *gas;
+    const double *mass, *comx, *comy, *comz, *gas, *radius;
+    const int32_t *pinst;
 };
 
 TreeView view(Ctx *c)
@@ -54,6 +55,8 @@ TreeView view(Ctx *c)
     t.comy = c->nd.comy;
     t.comz = c->nd.comz;
     t.gas = c->nd.gas;
+    t.radius = c->nd.radius;
+    t.pinst = c->pinst;
     return t;
 }
 
@@ -70,10 +73,11 @@ __device__ __forceinline__ bool cp_member(const TreeView &t, int64_t n, int i)
     return md != MODE_EMPTY;
 }
 
-__global__ void k_climb(int n, TreeView t, const uint8_t *type, double M, uint8_t *flag)
+__global__ void k_climb(int n, TreeView t, const uint8_t *type, const double *inst_massInH, uint8_t *flag)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || type[i] != 2) return;
+    const double M = inst_massInH[t.pinst[i]];
     int pn = t.refnode[i];
     if (pn < 0) return;  // Particle::node is null
     int64_t nd = pn;
@@ -130,13 +134,13 @@ __device__ __forceinline__ double cubic_spline(double r, double h)
 }
 
 __global__ void k_rho(TreeView t, const double *px, const double *py, const double *pz, const double *m,
-                      const uint8_t *type, const int32_t *list, const Ctx::Ctl *ctl, double R, double *rho_node)
+                      const uint8_t *type, const int32_t *list, const Ctx::Ctl *ctl, double *rho_node)
 {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (w >= ctl->list_count) return;
     int64_t nd = list[w];
-    double h = 2.0 * ldexp(R, -(int)t.level[nd]);  // h = radius * 2 (Node.cpp:765)
+    double h = t.radius[nd] * 2;  // h = radius * 2 (Node.cpp:765)
     double cx = t.comx[nd], cy = t.comy[nd], cz = t.comz[nd];
     int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
     uint8_t md = t.mode[nd];
@@ -160,7 +164,7 @@ __global__ void k_rho(TreeView t, const double *px, const double *py, const doub
 }
 
 __global__ void k_assign(int n, TreeView t, const int32_t *finalnode, const uint8_t *type, const double *U,
-                         const double *rho_node, double R, double *h, double *rho, double *P, double *T)
+                         const double *rho_node, double *h, double *rho, double *P, double *T)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || type[i] != 2) return;
@@ -169,7 +173,7 @@ __global__ void k_assign(int n, TreeView t, const int32_t *finalnode, const uint
         h[i] = 0.0;  // Tree.cpp:123-133 resets h; rho, P, T keep their old values
         return;
     }
-    h[i] = ldexp(R, -(int)t.level[f]) * 2;
+    h[i] = t.radius[f] * 2;
     double r = rho_node[f];
     rho[i] = r;
     P[i] = (kGamma - 1.0) * U[i] * r;                           // Node.cpp:789
@@ -178,7 +182,7 @@ __global__ void k_assign(int n, TreeView t, const int32_t *finalnode, const uint
 
 // ---- visual density --------------------------------------------------------
 
-__global__ void k_vclimb(int n, TreeView t, double R, double Rv, uint8_t *flag)
+__global__ void k_vclimb(int n, TreeView t, double Rv, uint8_t *flag)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -188,8 +192,8 @@ __global__ void k_vclimb(int n, TreeView t, double R, double Rv, uint8_t *flag)
     for (;;) {
         int32_t par = t.parent[nd];
         if (par < 0) return;
-        double r = ldexp(R, -(int)t.level[nd]);
-        double rp = ldexp(R, -(int)t.level[par]);
+        double r = t.radius[nd];
+        double rp = t.radius[par];
         if (fabs(Rv - r) > fabs(Rv - rp)) {
             nd = par;
             continue;
@@ -204,7 +208,7 @@ __global__ void k_vclimb(int n, TreeView t, double R, double Rv, uint8_t *flag)
     }
 }
 
-__global__ void k_vfinal(int n, TreeView t, const uint8_t *flag, double R, double *vdens)
+__global__ void k_vfinal(int n, TreeView t, const uint8_t *flag, double *vdens)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -212,7 +216,7 @@ __global__ void k_vfinal(int n, TreeView t, const uint8_t *flag, double R, doubl
     double v = 0.0;
     while (nd >= 0) {
         if (flag[nd] && cp_member(t, nd, i)) {
-            double r = ldexp(R, -(int)t.level[nd]);
+            double r = t.radius[nd];
             v = t.mass[nd] / (r * r * r);
         }
         nd = t.parent[nd];
@@ -231,14 +235,16 @@ int run_sph_density(Ctx *c)
     TreeView t = view(c);
     AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
-    AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->prm.massInH, c->nd.flag);
+    if (c->n_inst == 1)  // a single simulation follows ag2_set_params
+        AG2_CUDA(c, cudaMemcpyAsync(c->inst_massInH, &c->prm.massInH, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->inst_massInH, c->nd.flag);
     AG2_LAUNCH(c, k_final, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->nd.flag, c->finalnode, c->nodelist,
                c->ctl);
     const int ngas = c->ngas;
     AG2_LAUNCH(c, k_rho, grid_for((size_t)ngas * 32, kBlock), kBlock, 0, t, S.px, S.py, S.pz, S.m, S.type,
-               c->nodelist, c->ctl, c->root_radius, c->nd.rho);
-    AG2_LAUNCH(c, k_assign, grid_for(n, kBlock), kBlock, 0, n, t, c->finalnode, S.type, S.U, c->nd.rho,
-               c->root_radius, S.h, S.rho, S.P, S.T);
+               c->nodelist, c->ctl, c->nd.rho);
+    AG2_LAUNCH(c, k_assign, grid_for(n, kBlock), kBlock, 0, n, t, c->finalnode, S.type, S.U, c->nd.rho, S.h, S.rho,
+               S.P, S.T);
     return AG2_OK;
 }
 
@@ -250,8 +256,8 @@ int run_visual_density(Ctx *c, double Rv)
     Particles &S = c->S();
     TreeView t = view(c);
     AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
-    AG2_LAUNCH(c, k_vclimb, grid_for(n, kBlock), kBlock, 0, n, t, c->root_radius, Rv, c->nd.flag);
-    AG2_LAUNCH(c, k_vfinal, grid_for(n, kBlock), kBlock, 0, n, t, c->nd.flag, c->root_radius, S.vdens);
+    AG2_LAUNCH(c, k_vclimb, grid_for(n, kBlock), kBlock, 0, n, t, Rv, c->nd.flag);
+    AG2_LAUNCH(c, k_vfinal, grid_for(n, kBlock), kBlock, 0, n, t, c->nd.flag, S.vdens);
     return AG2_OK;
 }
 

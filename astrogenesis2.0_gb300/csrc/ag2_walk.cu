@@ -48,8 +48,10 @@ struct WalkArgs {
     const int32_t *first, *leafpos;
     const uint8_t *childmask;
     const int8_t *level;
-    const double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz;
-    double R, theta, e0, G;
+    const double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz, *radius;
+    const int4 *groups;  // (first slot, lanes, instance = root node, 0)
+    int ngroups;
+    double theta, e0, G;
     Ctx::Ctl *ctl;
 };
 
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
     __shared__ int2 stk_all[(kWalkBlock / 32) * kStack];
     const int lane = threadIdx.x & 31;
     int2 *stk = stk_all + (threadIdx.x >> 5) * kStack;
-    const int ngroups = (a.n + 31) >> 5;
+    const int ngroups = a.ngroups;
     const double eps02 = a.e0 * a.e0;
     unsigned long long cnt_g = 0, cnt_s = 0;
     for (;;) {
@@ -159,12 +161,15 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
         if (lane == 0) grp = atomicAdd(&a.ctl->list_count, 1);
         grp = __shfl_sync(0xffffffffu, grp, 0);
         if (grp >= ngroups) break;
-        const int i = grp * 32 + lane;
-        const bool valid = i < a.n && a.m[i] != 0.0;
+        const int4 gd = a.groups[grp];
+        const int i = gd.x + lane;
+        const bool live = lane < gd.y;
+        const int root = gd.z;
+        const bool valid = live && a.m[i] != 0.0;
         double xi = 0, yi = 0, zi = 0, hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
         bool gas_i = false;
         int myleaf = -1;
-        if (i < a.n) {
+        if (live) {
             xi = a.px[i];
             yi = a.py[i];
             zi = a.pz[i];
@@ -186,8 +191,8 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
         const unsigned all = __ballot_sync(0xffffffffu, valid);
         int sp = 0;
         bool overflow = false;
-        if (all && a.mass[0] != 0.0) {
-            stk[0] = make_int2(0, (int)all);  // evaluate the root itself
+        if (all && a.mass[root] != 0.0) {
+            stk[0] = make_int2(root, (int)all);  // evaluate the root itself
             sp = 1;
         }
         __syncwarp();
@@ -208,7 +213,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
                 if (r != 0.0) {
                     bool interact = leaf;
                     if (!leaf) {
-                        double rad = ldexp(a.R, -(int)a.level[c]);
+                        double rad = a.radius[c];
                         if (rad / r < a.theta)
                             interact = true;
                         else
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
             atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
             atomicExch(&a.ctl->err_info, grp);
         }
-        if (i < a.n) {
+        if (live) {
             a.ax[i] = valid ? acc.x : 0.0;
             a.ay[i] = valid ? acc.y : 0.0;
             a.az[i] = valid ? acc.z : 0.0;
@@ -372,7 +377,7 @@ __device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, co
     double ddx = a.comx[c] - xi, ddy = a.comy[c] - yi, ddz = a.comz[c] - zi;
     double r = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
     if (r == 0.0) return 0;
-    int decision = (leaf || ldexp(a.R, -(int)a.level[c]) / r < a.theta) ? 1 : 2;
+    int decision = (leaf || a.radius[c] / r < a.theta) ? 1 : 2;
     if (decision == 1 && tiny) {
         double e2 = a.e0 * a.e0;
         if (!kGeneral || general_eps2(r, a.e0, &e2)) {
@@ -393,7 +398,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
     __shared__ WarpSmem sm_all[kWalkBlock / 32];
     const int lane = threadIdx.x & 31;
     WarpSmem &W = sm_all[threadIdx.x >> 5];
-    const int ngroups = (a.n + 31) >> 5;
+    const int ngroups = a.ngroups;
     const float G = (float)a.G;
     const float eps02 = (float)(a.e0 * a.e0);
     unsigned long long cnt_g = 0, cnt_s = 0;
@@ -402,8 +407,11 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         if (lane == 0) grp = atomicAdd(&a.ctl->list_count, 1);
         grp = __shfl_sync(0xffffffffu, grp, 0);
         if (grp >= ngroups) break;
-        const int i = grp * 32 + lane;
-        const bool valid = i < a.n && a.m[i] != 0.0;
+        const int4 gd = a.groups[grp];
+        const int i = gd.x + lane;
+        const bool live = lane < gd.y;
+        const int root = gd.z;
+        const bool valid = live && a.m[i] != 0.0;
         // Group set-up in FP64 (positions, group centre, float offsets).  No FP64
         // value stays live past this block: on this part FP64 instructions issue
         // at 1/64 of the FP32 rate, so the compiler must not be able to
@@ -411,7 +419,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         float ghx, ghy, ghz, glx, gly, glz, ox, oy, oz;
         {
             double xi = 0, yi = 0, zi = 0;
-            if (i < a.n) {
+            if (live) {
                 xi = a.px[i];
                 yi = a.py[i];
                 zi = a.pz[i];
@@ -449,7 +457,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         int myleaf = -1;
         float hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
         bool gas_i = false;
-        if (i < a.n) {
+        if (live) {
             int pn = a.pnode[i];
             myleaf = (pn >= 0 && a.leafpos[pn] == i) ? pn : -1;
             if (kGas && a.type[i] == 2) {
@@ -481,9 +489,9 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         int sp = 0, nl = 0;
         bool overflow = false;
         // the root is the only child of a virtual parent (decided like any child)
-        if (all && a.mass[0] != 0.0) {
+        if (all && a.mass[root] != 0.0) {
             if (lane == 0) {
-                W.stk[0] = make_int2(0, (int)all);
+                W.stk[0] = make_int2(root, (int)all);
                 W.stkcm[0] = 1;
             }
             sp = 1;
@@ -546,7 +554,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 // and no per-lane test is needed.  NaN centres fall through.
                 unsigned selfm = 0u;
                 if (B.w < 0.0f) {
-                    const int lp = a.leafpos[c] - grp * 32;
+                    const int lp = a.leafpos[c] - gd.x;
                     if (lp >= 0 && lp < 32) selfm = 1u << lp;
                 }
                 W.cself[lane] = selfm;
@@ -658,7 +666,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
             atomicExch(&a.ctl->err_info, grp);
         }
-        if (i < a.n) {
+        if (live) {
             a.ax[i] = valid ? (double)sx - (double)kx : 0.0;
             a.ay[i] = valid ? (double)sy - (double)ky : 0.0;
             a.az[i] = valid ? (double)sz - (double)kz : 0.0;
@@ -676,13 +684,12 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
     }
 }
 
-__global__ void k_update_mac(int64_t nnodes, const int32_t *first, const int8_t *level, float4 *wB, double R,
-                             double theta)
+__global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double *radius, float4 *wB, double theta)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     if (first[j] < 0) return;
-    double q = ldexp(R, -(int)level[j]) / theta;
+    double q = radius[j] / theta;
     wB[j].w = (float)(q * q);
 }
 
@@ -693,8 +700,8 @@ int run_forces(Ctx *c)
     if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_forces needs a tree (call ag2_build_tree)");
     if (c->n == 0) return AG2_OK;
     if (c->prm.theta != c->tree_theta) {
-        AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.level,
-                   c->nd.wB, c->root_radius, c->prm.theta);
+        AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.radius,
+                   c->nd.wB, c->prm.theta);
         c->tree_theta = c->prm.theta;
     }
     Particles &S = c->S();
@@ -710,7 +717,9 @@ int run_forces(Ctx *c)
     a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.childmask = c->nd.childmask; a.level = c->nd.level;
     a.mass = c->nd.mass; a.comx = c->nd.comx; a.comy = c->nd.comy; a.comz = c->nd.comz;
     a.gas = c->nd.gas; a.mvx = c->nd.mvx; a.mvy = c->nd.mvy; a.mvz = c->nd.mvz;
-    a.R = c->root_radius;
+    a.radius = c->nd.radius;
+    a.groups = c->groups;
+    a.ngroups = c->ngroups;
     a.theta = c->prm.theta;
     a.e0 = c->prm.e0;
     a.G = c->prm.G;
@@ -723,7 +732,7 @@ int run_forces(Ctx *c)
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->inter_grav, 0, 2 * sizeof(unsigned long long), c->stream));
     int dev_sms = 152;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device);
-    const int ngroups = (int)((c->n + 31) / 32);
+    const int ngroups = c->ngroups;
     int blocks = std::min((ngroups + 3) / 4, dev_sms * 16);
     if (blocks < 1) blocks = 1;
 #define WALK(K) AG2_LAUNCH(c, K, blocks, kWalkBlock, 0, a)

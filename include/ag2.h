@@ -112,6 +112,17 @@ int ag2_set_field(ag2_ctx *ctx, int field, const double *src, int src_is_device)
 int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
 size_t ag2_count(const ag2_ctx *ctx);
 
+/* Independent simulations in one context (the batched ensemble and the
+ * serving loop): after ag2_upload, instance k is the particles with upload
+ * indices [first[k], first[k+1]) (first[0] = 0, first[n_inst] = n).  Each
+ * instance gets its own octree (root half-width, modes, moments), its own SPH
+ * neighbour mass (massInH[k]; NULL = params.massInH) and its own walk groups, so
+ * its results do not depend on what else shares the context; every hot-path
+ * call below then processes all instances at once.  ag2_upload resets the
+ * layout to one instance. */
+int ag2_set_instances(ag2_ctx *ctx, int32_t n_inst, const int64_t *first, const double *massInH);
+int ag2_instance_radius(ag2_ctx *ctx, int32_t instance, double *radius);
+
 /* Hot path.  The tree is device resident until the next build or upload. */
 int ag2_build_tree(ag2_ctx *ctx);
 int ag2_visual_density(ag2_ctx *ctx, double visualDensityRadius);
@@ -175,13 +186,13 @@ int ag2_fp32_peak_probe(ag2_ctx *ctx, double *gflops);
  * stream into a graph.  The caller passes device buffers: pos holds n
  * xyz-interleaved doubles, radius receives one double; the work is enqueued on
  * `stream` (a cudaStream_t; NULL = the legacy default stream) and nothing is
- * allocated.  Scratch space is a fixed 16 KiB array inside this library on each
+ * allocated.  Scratch space is a fixed 32 KiB array inside this library on each
  * device that uses it, kept until the process exits.  The first call on a
  * device looks up that array's address (make it before any stream capture).
  * Calls that overlap on the GPU share the array and race.  n must lie in
  * 1..AG2_NOALLOC_MAX_PARTICLES; larger n returns AG2_E_CAPACITY and launches
  * nothing. */
-#define AG2_NOALLOC_MAX_PARTICLES 2147483647
+#define AG2_NOALLOC_MAX_PARTICLES 8355840
 int ag2_root_radius_noalloc(const double *pos, int64_t n, double *radius, void *stream);
 
 /* Number of kernels this library launched since the context was created. */

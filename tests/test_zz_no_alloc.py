@@ -39,6 +39,6 @@ def test_noalloc_root_radius_matches_context_path():
             assert rc == ag2.OK
             torch.cuda.synchronize()
             assert out.item() == want
-    rc = L.ag2_root_radius_noalloc(ctypes.c_void_p(pos.data_ptr()), 2 ** 31, ctypes.c_void_p(out.data_ptr()),
+    rc = L.ag2_root_radius_noalloc(ctypes.c_void_p(pos.data_ptr()), 8355840 + 1, ctypes.c_void_p(out.data_ptr()),
                                    stream)
     assert rc == ag2.E_CAPACITY
