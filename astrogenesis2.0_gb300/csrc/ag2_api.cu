@@ -168,7 +168,8 @@ void free_nodes(Nodes &d)
     void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs, d.childmask,
                   d.cx,    d.cy,    d.cz,    d.bkey,  d.mass,   d.comx,    d.comy, d.comz, d.gas,   d.mvx,
                   d.mvy,   d.mvz,   d.ngas,  d.tm,    d.tmx,    d.tmy,     d.tmz,  d.tg,   d.tgvx,  d.tgvy,
-                  d.tgvz,  d.tng,   d.tfirst, d.tfirstm, d.wA,   d.wB,      d.wD,   d.flag, d.rho};
+                  d.tgvz,  d.tng,   d.tfirst, d.tfirstm, d.wA,   d.wB,      d.wD,   d.flag, d.rho,
+                  d.radius, d.inst, d.nlx, d.ilist};
     for (void *q : ps) cudaFree(q);
     d = Nodes{};
 }
@@ -352,6 +353,10 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
          cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&
          cudaMalloc(&c->pinst, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->perm_final, cap * 4) == cudaSuccess && cudaMalloc(&c->ap[0], cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->ap[1], cap * 4) == cudaSuccess && cudaMalloc(&c->nl[0], cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->nl[1], cap * 4) == cudaSuccess && cudaMalloc(&c->leaves, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->pkey, 6 * cap * sizeof(int64_t)) == cudaSuccess &&
          cudaMalloc(&c->ctl, sizeof(Ctx::Ctl)) == cudaSuccess &&
          cudaMallocHost(&c->ctl_host, sizeof(Ctx::Ctl)) == cudaSuccess;
     if (ok) ok = ensure_node_capacity(c, 4 * cap + 1024) == AG2_OK;
@@ -376,7 +381,8 @@ int ag2_destroy(ag2_ctx *c)
     void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->slot_of, c->finalnode,
                   c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
                   c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->inst_first, c->inst_R,
-                  c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax};
+                  c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax,
+                  c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     for (auto &e : c->ev)
@@ -703,7 +709,8 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
     std::vector<int8_t> level(nn);
     std::vector<uint8_t> mode(nn);
     std::vector<double> m(nn), cx(nn), cy(nn), cz(nn), g(nn), vx(nn), vy(nn), vz(nn), ccx(nn), ccy(nn), ccz(nn);
-    std::vector<int32_t> inst_of(nn);
+    std::vector<int32_t> inst_of(nn), parent(nn);
+    std::vector<double> rad(nn);
     auto cp = [&](void *dst, const void *src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
     };
@@ -727,6 +734,8 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
     AG2_CUDA(c, cp(ccy.data(), d.cy, nn * 8));
     AG2_CUDA(c, cp(ccz.data(), d.cz, nn * 8));
     AG2_CUDA(c, cp(inst_of.data(), d.inst, nn * 4));
+    AG2_CUDA(c, cp(parent.data(), d.parent, nn * 4));
+    AG2_CUDA(c, cp(rad.data(), d.radius, nn * 8));
     if (n) AG2_CUDA(c, cp(id.data(), c->S().id, n * 4));
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));
     // prefix sums of member hashes over tree-order slots
@@ -766,6 +775,15 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
         if (cp_count) cp_count[k] = cc;
         if (cp_hash) cp_hash[k] = ch;
         const bool empty = count[v] == 0;  // the build leaves empty children's moments unwritten
+        if (empty && !root) {
+            // nor their centres: parent centre + r*(+-0.5), as for every child (Node.cpp:433-443)
+            const int32_t pa = parent[v];
+            const int o = (int)(v - first[pa]);
+            const double rc = rad[pa] / 2;
+            ccx[v] = ccx[pa] + ((o & 1) ? rc : -rc);
+            ccy[v] = ccy[pa] + ((o & 2) ? rc : -rc);
+            ccz[v] = ccz[pa] + ((o & 4) ? rc : -rc);
+        }
         if (mass) mass[k] = empty ? 0.0 : m[v];
         if (com3) {
             com3[3 * k] = empty ? 0.0 : cx[v];

@@ -164,10 +164,9 @@ __global__ void k_width_max(int n, const double *px, const double *py, const dou
 
 // ---- level-wise partition --------------------------------------------------
 
-__device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
+__device__ __forceinline__ void set_bounds_v(Nodes nd, int64_t c, double cx, double cy, double cz, double r)
 {
     int64_t *k = nd.bkey + 9 * c;
-    double cx = nd.cx[c], cy = nd.cy[c], cz = nd.cz[c];
     k[0] = okey(__dsub_rn(cx, r));
     k[1] = okey(__dsub_rn(cy, r));
     k[2] = okey(__dsub_rn(cz, r));
@@ -178,11 +177,15 @@ __device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
     k[7] = okey(cy);
     k[8] = okey(cz);
 }
+__device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
+{
+    set_bounds_v(nd, c, nd.cx[c], nd.cy[c], nd.cz[c], r);
+}
 
 // root of instance k is node k (Tree.cpp:28-33: centre at the origin, half-width
 // from calcTreeWidth, depth 0)
 __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *first, const double *R, int thresh,
-                            int32_t *pnode)
+                            int32_t *nl0, int32_t *leaves)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_inst) return;
@@ -204,10 +207,12 @@ __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *
     const uint8_t needs = (mode == MODE_PAR || mode == MODE_SER_ENTRY) ? 1 : 0;
     nd.needs[k] = needs;
     nd.leafpos[k] = (mode == MODE_VEC1) ? start : -1;
-    if (mode == MODE_VEC1) pnode[start] = k;
+    if (mode == MODE_VEC1) leaves[atomicAdd(&ctl->nleaf, 1)] = k;
     if (needs) {
         set_bounds(nd, k, R[k]);
-        atomicAdd(&ctl->next_needs, 1);
+        const int q = atomicAdd(&ctl->next_needs, 1);
+        nl0[q] = k;
+        nd.nlx[k] = q;
     }
 }
 
@@ -219,30 +224,97 @@ __global__ void k_ctl_reset(Ctx::Ctl *ctl, int n_inst)
     ctl->err_info = 0;
     ctl->any_drop = 0;
     ctl->ndrop_nodes = 0;
+    ctl->next_active = 0;
+    ctl->nleaf = 0;
+    ctl->nint = 0;
 }
 
-__global__ void k_init_positions(int n, const int32_t *pinst, const uint8_t *needs, int32_t *perm, int32_t *posnode)
+// Block-wide reservation in a compact list: every thread of the block calls
+// this (no early return before it).  A flagged thread gets the position of its
+// `stride` entries in the list whose length is *counter; one atomicAdd per block.
+template <class T>
+__device__ __forceinline__ T block_reserve(bool flag, T *counter, T stride, int32_t *sh, T *sbase)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    perm[i] = i;
-    const int k = pinst[i];
-    posnode[i] = needs[k] ? k : -1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned b = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0) sh[w] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = 0; k < nw; k++) {
+            const int v = sh[k];
+            sh[k] = acc;
+            acc += v;
+        }
+        *sbase = acc ? atomicAdd(counter, (T)acc * stride) : (T)0;
+    }
+    __syncthreads();
+    const T r = flag ? *sbase + (T)(sh[w] + __popc(b & ((1u << lane) - 1u))) * stride : (T)0;
+    __syncthreads();
+    return r;
 }
 
-// digit of every particle of a node being split at this level
-__global__ void k_digit(int n, int64_t base, const int32_t *__restrict__ posnode, const int32_t *__restrict__ perm,
-                        const double *__restrict__ px, const double *__restrict__ py,
-                        const double *__restrict__ pz, Nodes nd, uint8_t *__restrict__ digit,
-                        int32_t *__restrict__ hist)
+// Buffers of one level of the partition.  A slot is a position in the
+// partition; it is active while the node whose range holds it is still split.
+struct LevelBufs {
+    const int32_t *ap;       // active slots of this level
+    int32_t *ap_next;        // ... of the next level
+    const int32_t *posnode;  // per active slot: index of its node in this level's split list
+    int32_t *posnode_next;
+    const int32_t *perm;     // per active slot: index of the particle there in the state arrays
+    int32_t *perm_next;
+    const int64_t *kx, *ky, *kz;  // per active slot: ordered keys of the particle's coordinates
+    int64_t *kx_next, *ky_next, *kz_next;
+    int32_t *perm_final;     // per slot, written when the particle there settles
+    int32_t *pnode;          // per slot: node the settled particle ends in
+    uint8_t *digit;          // per active-list entry
+    int32_t *hist, *cursor;  // 9 per split-list entry
+    const int32_t *nl;       // this level's split list (node ids)
+    int32_t *nl_next;
+    int32_t *leaves;         // every non-empty leaf
+    int32_t *drop_list;      // nodes with out-of-bounds tails of two or more
+};
+
+// Level 0: the slots of an instance whose root is split are active (the
+// coordinates become ordered keys, in slot order); the slot of a one-particle
+// root is final at once.
+__global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restrict__ pinst, Nodes nd,
+                                                   const double *__restrict__ px, const double *__restrict__ py,
+                                                   const double *__restrict__ pz, LevelBufs b, Ctx::Ctl *ctl)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int nid = posnode[i];
-    if (nid < 0) return;
-    int p = perm[i];
-    int64_t kx = okey(px[p]), ky = okey(py[p]), kz = okey(pz[p]);
-    const int64_t *k = nd.bkey + 9 * (int64_t)nid;
+    __shared__ int32_t sh[kBlock / 32 + 1];
+    __shared__ int32_t sbase;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = false;
+    int32_t *perm = const_cast<int32_t *>(b.perm);
+    int32_t *posnode = const_cast<int32_t *>(b.posnode);
+    if (i < n) {
+        const int k = pinst[i];
+        if (nd.needs[k]) {
+            act = true;
+            perm[i] = i;
+            posnode[i] = nd.nlx[k];
+            const_cast<int64_t *>(b.kx)[i] = okey(px[i]);
+            const_cast<int64_t *>(b.ky)[i] = okey(py[i]);
+            const_cast<int64_t *>(b.kz)[i] = okey(pz[i]);
+        } else {
+            b.perm_final[i] = i;
+            b.pnode[i] = k;  // one-particle root
+        }
+    }
+    const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
+    if (act) const_cast<int32_t *>(b.ap)[q] = i;
+}
+
+// digit of every active slot against its node's bounds
+__global__ void __launch_bounds__(kBlock) k_digit(int nap, LevelBufs b, Nodes nd)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nap) return;
+    const int i = b.ap[t];
+    const int j = b.posnode[i];
+    const int64_t *k = nd.bkey + 9 * (int64_t)b.nl[j];
+    const int64_t kx = b.kx[i], ky = b.ky[i], kz = b.kz[i];
     int d;
     // inclusive bounds of Node::getOctant / insert(Particle*) (Node.cpp:606-608, 706-708)
     if (kx < k[0] || kx > k[3] || ky < k[1] || ky > k[4] || kz < k[2] || kz > k[5]) {
@@ -250,32 +322,32 @@ __global__ void k_digit(int n, int64_t base, const int32_t *__restrict__ posnode
     } else {
         d = (kx > k[6] ? 1 : 0) | (ky > k[7] ? 2 : 0) | (kz > k[8] ? 4 : 0);  // Node.cpp:714-716
     }
-    digit[i] = (uint8_t)d;
-    agg_inc(hist, (int)((int64_t)nid - base) * 9 + d);
+    b.digit[t] = (uint8_t)d;
+    agg_inc(b.hist, 9 * j + d);
 }
 
-// Split decisions and children of the nodes of one level.  Eight threads per
-// node (one per child octant) so that the children's fields are written with
-// coalesced stores; the first thread of each group of eight decides the split,
-// allocates the 8-child block (one atomic per warp) and writes the parent.
-__global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, int64_t node_cap, Nodes nd,
-                        Ctx::Ctl *ctl, const int32_t *__restrict__ hist, int32_t *__restrict__ cursor,
-                        int max_depth, int32_t *__restrict__ drop_list)
+// Split decisions and children of the nodes of this level's split list.  Eight
+// threads per node (one per child octant) so that the children's fields are
+// written with coalesced stores; the first thread of each group of eight
+// decides the split and writes the parent.  Child blocks, the next split list,
+// the leaf list and the internal-node list are reserved once per thread block.
+__global__ void __launch_bounds__(kBlock) k_nodes(int nnl, int level, int thresh, int64_t node_cap, Nodes nd,
+                                                  Ctx::Ctl *ctl, LevelBufs b, int max_depth)
 {
+    __shared__ int32_t sh[kBlock / 32 + 1];
+    __shared__ unsigned long long sbase64;
+    __shared__ int32_t sbase;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int lane = lane_id();
     const int o = lane & 7;
     const int64_t j = t >> 3;
-    const unsigned gmask = 0xffu << (lane & ~7);  // the 8 lanes of this node
-    const bool exists = j < count_lvl;
-    const int64_t nid = base + (exists ? j : 0);
-    const bool needs = exists && nd.needs[nid];
-    // split decision (every lane of the group computes the same values)
+    const bool exists = j < nnl;
+    const int64_t nid = exists ? b.nl[j] : 0;
     int32_t cnt = 0, start = 0, ndrop = 0, reached = 0;
     uint8_t mode = 0;
     bool internal = false;
-    const int32_t *h = hist + 9 * (exists ? j : 0);
-    if (needs) {
+    const int32_t *h = b.hist + 9 * (exists ? j : 0);
+    if (exists) {
         cnt = nd.count[nid];
         start = nd.start[nid];
         ndrop = h[8];
@@ -283,16 +355,16 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
         mode = nd.mode[nid];
         internal = (mode == MODE_PAR) || (reached >= 2);
     }
-    if (needs && o == 0) {
+    if (exists && o == 0) {
         nd.ndrop[nid] = ndrop;
         if (ndrop) ctl->any_drop = 1;
         if (ndrop >= 2) {  // tails to put in upload order after the partition
             int k = atomicAdd(&ctl->ndrop_nodes, 1);
-            if (k < kMaxDropNodes) drop_list[k] = (int32_t)nid;
+            if (k < kMaxDropNodes) b.drop_list[k] = (int32_t)nid;
         }
         int32_t acc = start;
         for (int d = 0; d < 9; d++) {
-            cursor[9 * j + d] = acc;
+            b.cursor[9 * j + d] = acc;
             acc += h[d];
         }
         if (!internal) {
@@ -300,7 +372,7 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
             nd.leafpos[nid] = (reached == 1) ? start : -1;
         }
     }
-    bool split = needs && internal;
+    bool split = exists && internal;
     if (split && level + 1 >= max_depth) {
         if (o == 0) {
             atomicExch(&ctl->err_code, (int)AG2_E_COINCIDENT);
@@ -310,93 +382,133 @@ __global__ void k_nodes(int64_t base, int64_t count_lvl, int level, int thresh, 
         }
         split = false;
     }
-    // one atomic per warp for the 8-child blocks of all splitting nodes
-    const unsigned leaders = __ballot_sync(0xffffffffu, split && o == 0);
-    unsigned long long wbase = 0;
-    if (leaders) {
-        if (lane == __ffs(leaders) - 1)
-            wbase = atomicAdd((unsigned long long *)&ctl->node_count, 8ull * __popc(leaders));
-        wbase = __shfl_sync(0xffffffffu, wbase, __ffs(leaders) - 1);
+    const unsigned long long cb0 =
+        block_reserve<unsigned long long>(split && o == 0, (unsigned long long *)&ctl->node_count, 8ull, sh, &sbase64);
+    const unsigned long long cb = __shfl_sync(0xffffffffu, cb0, lane & ~7);
+    if (split && (int64_t)cb + 8 > node_cap) {
+        if (o == 0) {
+            atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+            nd.first[nid] = -1;
+        }
+        split = false;
     }
-    int nneeds = 0;
+    int64_t c = 0;
+    uint8_t cm = MODE_EMPTY;
     if (split) {
-        const unsigned long long cb = wbase + 8ull * __popc(leaders & ((1u << (lane & ~7)) - 1u));
-        if ((int64_t)cb + 8 > node_cap) {
-            if (o == 0) {
-                atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
-                nd.first[nid] = -1;
-            }
-        } else {
-            const int64_t c0 = (int64_t)cb;
-            if (o == 0) {
-                nd.first[nid] = (int32_t)c0;
-                nd.leafpos[nid] = -1;
-            }
-            // child o: centre c + r*(+-0.5), radius r/2 (Node.cpp:433-443, 630-642)
-            const double r = nd.radius[nid];
-            const double rc = r / 2;  // Node.cpp:440
-            const int64_t c = c0 + o;
-            int32_t s = start;
-            for (int d = 0; d < o; d++) s += h[d];
-            const int32_t cc = h[o];
-            nd.cx[c] = __dadd_rn(nd.cx[nid], __dmul_rn(r, (o & 1) ? 0.5 : -0.5));
-            nd.cy[c] = __dadd_rn(nd.cy[nid], __dmul_rn(r, (o & 2) ? 0.5 : -0.5));
-            nd.cz[c] = __dadd_rn(nd.cz[nid], __dmul_rn(r, (o & 4) ? 0.5 : -0.5));
-            nd.start[c] = s;
-            nd.count[c] = cc;
-            nd.ndrop[c] = 0;
-            nd.first[c] = -1;
-            nd.parent[c] = (int32_t)nid;
-            nd.level[c] = (int8_t)(level + 1);
-            nd.radius[c] = rc;
-            nd.inst[c] = nd.inst[nid];
-            uint8_t cm;
-            if (cc == 0)
-                cm = MODE_EMPTY;
-            else if (mode != MODE_PAR)
-                cm = MODE_SER;
-            else if (cc == 1)
-                cm = MODE_VEC1;
-            else if (cc < thresh)
-                cm = MODE_SER_ENTRY;
-            else
-                cm = MODE_PAR;
-            nd.mode[c] = cm;
-            const uint8_t cneeds = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER) ? 1 : 0;
-            nd.needs[c] = cneeds;
-            nd.leafpos[c] = (cm == MODE_VEC1) ? s : -1;
-            if (cneeds) set_bounds(nd, c, rc);
-            nneeds = cneeds;
+        const int64_t c0 = (int64_t)cb;
+        if (o == 0) {
+            nd.first[nid] = (int32_t)c0;
+            nd.leafpos[nid] = -1;
+        }
+        // child o: centre c + r*(+-0.5), radius r/2 (Node.cpp:433-443, 630-642)
+        const double r = nd.radius[nid];
+        const double rc = r / 2;  // Node.cpp:440; also r*0.5 of the centre offset, exactly
+        c = c0 + o;
+        int32_t s = start;
+        for (int d = 0; d < o; d++) s += h[d];
+        const int32_t cc = h[o];
+        nd.start[c] = s;
+        nd.count[c] = cc;
+        nd.ndrop[c] = 0;
+        nd.first[c] = -1;
+        nd.parent[c] = (int32_t)nid;
+        nd.level[c] = (int8_t)(level + 1);
+        nd.radius[c] = rc;
+        nd.inst[c] = nd.inst[nid];
+        if (cc == 0)
+            cm = MODE_EMPTY;
+        else if (mode != MODE_PAR)
+            cm = MODE_SER;
+        else if (cc == 1)
+            cm = MODE_VEC1;
+        else if (cc < thresh)
+            cm = MODE_SER_ENTRY;
+        else
+            cm = MODE_PAR;
+        nd.mode[c] = cm;
+        const bool cneeds = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER);
+        nd.needs[c] = cneeds ? 1 : 0;
+        nd.leafpos[c] = (cm == MODE_VEC1) ? s : -1;
+        if (cc > 0) {  // empty children's centres are never read on the device
+            const double x = __dadd_rn(nd.cx[nid], (o & 1) ? rc : -rc);
+            const double y = __dadd_rn(nd.cy[nid], (o & 2) ? rc : -rc);
+            const double z = __dadd_rn(nd.cz[nid], (o & 4) ? rc : -rc);
+            nd.cx[c] = x;
+            nd.cy[c] = y;
+            nd.cz[c] = z;
+            if (cneeds) set_bounds_v(nd, c, x, y, z, rc);
         }
     }
-    const int sum = (int)__reduce_add_sync(0xffffffffu, (unsigned)nneeds);
-    if (lane == 0 && sum) atomicAdd(&ctl->next_needs, sum);
-    (void)gmask;
+    const bool cneeds = split && (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER);
+    const int32_t q = block_reserve<int32_t>(cneeds, &ctl->next_needs, 1, sh, &sbase);
+    if (cneeds) {
+        b.nl_next[q] = (int32_t)c;
+        nd.nlx[c] = q;
+    }
+    // leaves: one-particle children of a parallel node, and nodes of this list
+    // that stay leaves; internal nodes of this level
+    const bool leaf_self = exists && o == 0 && !internal;
+    const bool lflag = (split && cm == MODE_VEC1) || leaf_self;
+    const int32_t ql = block_reserve<int32_t>(lflag, &ctl->nleaf, 1, sh, &sbase);
+    if (lflag) b.leaves[ql] = (int32_t)(leaf_self ? nid : c);
+    const bool iflag = split && o == 0;
+    const int32_t qi = block_reserve<int32_t>(iflag, &ctl->nint, 1, sh, &sbase);
+    if (iflag) nd.ilist[qi] = (int32_t)nid;
 }
 
-__global__ void k_scatter(int n, int64_t base, const int32_t *__restrict__ posnode, const int32_t *__restrict__ perm,
-                          const uint8_t *__restrict__ digit, Nodes nd, int32_t *__restrict__ cursor,
-                          int32_t *__restrict__ perm2, int32_t *__restrict__ posnode2, int32_t *__restrict__ pnode)
+// Partition of every active slot's particle by digit; settled particles go to
+// their final slot, the others (and their keys) to the next level's buffers.
+// The next level's active slots are the slots that land in a child that is
+// split again; they are listed in slot order within each thread block.
+__global__ void __launch_bounds__(kBlock) k_scatter(int nap, LevelBufs b, Nodes nd, Ctx::Ctl *ctl)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int nid = posnode[i];
-    if (nid < 0) return;
-    int d = digit[i];
-    int np = agg_inc(cursor, (int)((int64_t)nid - base) * 9 + d);
-    perm2[np] = perm[i];
-    int32_t first = nd.first[nid];
-    if (first >= 0 && d < 8) {
-        int32_t child = first + d;
-        if (nd.needs[child]) {
-            posnode2[np] = child;
+    __shared__ int32_t sh[kBlock / 32 + 1];
+    __shared__ int32_t sbase;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = false;
+    int i = 0, nj = 0;
+    if (t < nap) {
+        i = b.ap[t];
+        const int j = b.posnode[i];
+        const int32_t nid = b.nl[j];
+        const int32_t p = b.perm[i];
+        const int d = b.digit[t];
+        const int np = agg_inc(b.cursor, 9 * j + d);
+        const int32_t first = nd.first[nid];
+        if (first >= 0 && d < 8) {
+            const int32_t child = first + d;
+            if (nd.needs[child]) {
+                b.perm_next[np] = p;
+                b.kx_next[np] = b.kx[i];
+                b.ky_next[np] = b.ky[i];
+                b.kz_next[np] = b.kz[i];
+            } else {
+                b.perm_final[np] = p;
+                b.pnode[np] = child;  // single-particle leaf
+            }
         } else {
-            posnode2[np] = -1;
-            pnode[np] = child;  // single-particle leaf
+            b.perm_final[np] = p;
+            b.pnode[np] = nid;  // leaf of a serial node, or the node's out-of-bounds tail
         }
-    } else {
-        posnode2[np] = -1;
-        pnode[np] = nid;  // leaf of a serial node, or the node's out-of-bounds tail
+        // the child whose range holds slot i from the next level on: child
+        // starts are non-decreasing in octant order, so the last one at or
+        // below i (an empty child shares its successor's start)
+        if (first >= 0 && i < nd.start[nid] + nd.count[nid] - nd.ndrop[nid]) {
+            int o = 0;
+            if (nd.start[first + 4] <= i) o = 4;
+            if (nd.start[first + o + 2] <= i) o += 2;
+            if (nd.start[first + o + 1] <= i) o += 1;
+            const int32_t cnode = first + o;
+            if (nd.needs[cnode]) {
+                act = true;
+                nj = nd.nlx[cnode];
+            }
+        }
+    }
+    const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
+    if (act) {
+        b.ap_next[q] = i;
+        b.posnode_next[i] = nj;
     }
 }
 
@@ -557,38 +669,35 @@ struct Sums {
     }
 };
 
-__global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P, const double *gas_prefix,
-                          const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+// RN(RN(x*m)/m) for m > 0 without a division.  With q = RN(x*m) = x*m*(1+e),
+// |e| <= 2^-53, the quotient q/m lies strictly within one unit in the last
+// place of x, so it rounds to x or to x's neighbour on the quotient's side.
+// The residual r = q - x*m is exact (one fma), q/m - x = r/m, and the half gap
+// to the neighbour times m is exact (a power of two times m): comparing |r| with
+// it decides the rounding, ties to the even significand.  Outside the range
+// where those products cannot overflow or underflow, divide.
+__device__ __forceinline__ double mul_div_same(double x, double m)
 {
-    int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (j >= count_lvl) return;
-    int64_t nid = base + j;
-    int32_t cnt = nd.count[nid];
-    if (cnt == 0) return;  // empty child: no kernel reads it (parents test the count first)
-    int32_t start = nd.start[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
-    uint8_t mode = nd.mode[nid];
-    Sums tot, own;  // tot: whole routed range; own: the reference's mass set
-    tot.zero();
-    own.zero();
-    uint8_t cmask = 0;
-    if (first >= 0) {
-        for (int o = 0; o < 8; o++) {
-            int64_t c = first + o;
-            if (nd.count[c] == 0) continue;
-            own.add_node(nd, c);
-            if (nd.mass[c] != 0.0) cmask |= (uint8_t)(1u << o);
-        }
-        tot = own;
-        for (int32_t i = start + cnt - ndrop; i < start + cnt; i++) tot.add_particle(P, i);
-        if (mode == MODE_PAR) own = tot;  // the parallel path sums escapers too (Node.cpp:477-499)
-    } else {
-        for (int32_t i = start; i < start + cnt; i++) tot.add_particle(P, i);
-        if (mode == MODE_VEC1) {
-            own = tot;
-        } else {
-            for (int32_t i = start; i < start + cnt - ndrop; i++) own.add_particle(P, i);
-        }
-    }
+    const double q = __dmul_rn(x, m);
+    const double ax = fabs(x);
+    if (!(m > 0x1p-400 && m < 0x1p400 && ax < 0x1p400 && (ax > 0x1p-400 || x == 0.0))) return __ddiv_rn(q, m);
+    const double r = __fma_rn(-x, m, q);
+    if (r == 0.0) return x;
+    const long long bits = __double_as_longlong(x);
+    const bool away = (r > 0.0) == (x > 0.0);  // |q/m| > |x|
+    const double y = __longlong_as_double(away ? bits + 1 : bits - 1);  // neighbour on that side
+    const double lim = __dmul_rn(0.5 * fabs(__dsub_rn(y, x)), m);
+    const double ar = fabs(r);
+    if (ar < lim) return x;
+    if (ar > lim) return y;
+    return (bits & 1) ? y : x;
+}
+
+// node record shared by leaves and internal nodes: moments, FP32 walk records
+__device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particles &P, const Sums &tot, double mass,
+                                           double cx, double cy, double cz, double gas, double mvx, double mvy,
+                                           double mvz, int32_t ng, uint8_t cmask, bool leaf, int32_t lp, double theta)
+{
     nd.tm[nid] = tot.m;
     nd.tmx[nid] = tot.mx;
     nd.tmy[nid] = tot.my;
@@ -601,30 +710,109 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
     nd.tfirst[nid] = tot.first_id;
     nd.tfirstm[nid] = tot.first_m;
     nd.childmask[nid] = cmask;
+    nd.mass[nid] = mass;
+    nd.comx[nid] = cx;
+    nd.comy[nid] = cy;
+    nd.comz[nid] = cz;
+    nd.gas[nid] = gas;
+    nd.mvx[nid] = mvx;
+    nd.mvy[nid] = mvy;
+    nd.mvz[nid] = mvz;
+    nd.ngas[nid] = ng;
+    // FP32 walk record: COM split into hi + lo floats
+    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    const float lx = (float)(cx - (double)hx), ly = (float)(cy - (double)hy), lz = (float)(cz - (double)hz);
+    nd.wA[nid] = make_float4(hx, hy, hz, (float)mass);
+    float mac = -1.0f;
+    if (!leaf) {
+        const double q = nd.radius[nid] / theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
+        mac = (float)(q * q);
+    }
+    nd.wB[nid] = make_float4(lx, ly, lz, mac);
+    if (leaf && lp >= 0)
+        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)gas);
+    else
+        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)gas);
+}
 
-    double mass = own.m, cx = 0.0, cy = 0.0, cz = 0.0, gas = own.g, mvx = 0.0, mvy = 0.0, mvz = 0.0;
-    int32_t lp = nd.leafpos[nid];
-    bool leaf = first < 0;
-    if (leaf && lp >= 0) {
-        double mp = P.m[lp];
-        bool isgas = P.type[lp] == 2;
+// Moments from the node's own mass set: the centre of mass and gas velocity as
+// ratios of sums, the NaN rule of serial nodes whose first particle is
+// massless, and the uniform-gas gasMass table.
+__device__ __forceinline__ void finish_sums(Nodes &nd, int64_t nid, uint8_t mode, const Sums &own,
+                                            const double *gas_prefix, const int32_t *gas_off, const uint8_t *gas_uni,
+                                            double &mass, double &cx, double &cy, double &cz, double &gas,
+                                            double &mvx, double &mvy, double &mvz)
+{
+    mass = own.m;
+    gas = own.g;
+    cx = cy = cz = mvx = mvy = mvz = 0.0;
+    const bool serial = (mode == MODE_SER || mode == MODE_SER_ENTRY);
+    if (serial && own.first_m == 0.0 && own.first_id != INT32_MAX) {
+        // serial insertion's running mean starts with (0*0 + x*0)/0 when the
+        // first particle to arrive is massless (Node.cpp:698): the centre of
+        // mass is NaN from then on, so the node is always opened
+        cx = cy = cz = __longlong_as_double(0x7ff8000000000000LL);
+    } else if (mass > 0.0) {
+        const double im = 1.0 / mass;  // one FP64 division per node
+        cx = own.mx * im;
+        cy = own.my * im;
+        cz = own.mz * im;
+    }
+    const int k = nd.inst[nid];
+    if (gas_uni[k]) gas = gas_prefix[gas_off[k] + own.ng];
+    if (own.g > 0) {
+        const double ig = 1.0 / own.g;
+        mvx = own.gvx * ig;
+        mvy = own.gvy * ig;
+        mvz = own.gvz * ig;
+    }
+}
+
+// Leaves (every level at once: a leaf's moments read only its particles).
+__global__ void __launch_bounds__(kBlock) k_moments_leaf(int nleaf, const int32_t *__restrict__ list, Nodes nd,
+                                                         Particles P, const double *gas_prefix,
+                                                         const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nleaf) return;
+    const int64_t nid = list[t];
+    const int32_t cnt = nd.count[nid], start = nd.start[nid], ndrop = nd.ndrop[nid];
+    const uint8_t mode = nd.mode[nid];
+    Sums tot, own;  // tot: whole routed range; own: the reference's mass set
+    tot.zero();
+    for (int32_t i = start; i < start + cnt; i++) tot.add_particle(P, i);
+    if (mode == MODE_VEC1) {
+        own = tot;
+    } else {
+        own.zero();
+        for (int32_t i = start; i < start + cnt - ndrop; i++) own.add_particle(P, i);
+    }
+    double mass, cx, cy, cz, gas, mvx, mvy, mvz;
+    const int32_t lp = nd.leafpos[nid];
+    if (lp >= 0) {
+        const double mp = P.m[lp];
+        const bool isgas = P.type[lp] == 2;
+        mass = mp;
+        gas = isgas ? mp : 0.0;
+        mvx = mvy = mvz = 0.0;
         if (mode == MODE_VEC1) {
             // Node.cpp:409-418: COM is the position itself, mVel stays zero
-            mass = mp;
             cx = P.px[lp];
             cy = P.py[lp];
             cz = P.pz[lp];
-            gas = isgas ? mp : 0.0;
         } else {
             // one serial insertion into an empty leaf (Node.cpp:678-698): the
             // running mean (0*(m-m) + x*m)/m, rounded as the reference rounds it
-            mass = mp;
-            if (mass != 0.0) {
+            cx = cy = cz = 0.0;
+            if (mass > 0.0) {
+                cx = mul_div_same(P.px[lp], mp);
+                cy = mul_div_same(P.py[lp], mp);
+                cz = mul_div_same(P.pz[lp], mp);
+            } else if (mass != 0.0) {
                 cx = __ddiv_rn(__dmul_rn(P.px[lp], mp), mass);
                 cy = __ddiv_rn(__dmul_rn(P.py[lp], mp), mass);
                 cz = __ddiv_rn(__dmul_rn(P.pz[lp], mp), mass);
             }
-            gas = isgas ? mp : 0.0;
             if (isgas && gas > 0) {
                 // gas velocity of a leaf is only ever read for export (the walk
                 // uses the leaf particle's own velocity, Node.cpp:111-113)
@@ -634,53 +822,37 @@ __global__ void k_moments(int64_t base, int64_t count_lvl, Nodes nd, Particles P
             }
         }
     } else {
-        const bool serial = (mode == MODE_SER || mode == MODE_SER_ENTRY);
-        if (serial && own.first_m == 0.0 && own.first_id != INT32_MAX) {
-            // serial insertion's running mean starts with (0*0 + x*0)/0 when the
-            // first particle to arrive is massless (Node.cpp:698): the centre of
-            // mass is NaN from then on, so the node is always opened
-            cx = cy = cz = __longlong_as_double(0x7ff8000000000000LL);
-        } else if (mass > 0.0) {
-            double im = 1.0 / mass;  // one FP64 division per node
-            cx = own.mx * im;
-            cy = own.my * im;
-            cz = own.mz * im;
-        }
-        const int k = nd.inst[nid];
-        if (gas_uni[k]) gas = gas_prefix[gas_off[k] + own.ng];
-        if (own.g > 0) {
-            double ig = 1.0 / own.g;
-            mvx = own.gvx * ig;
-            mvy = own.gvy * ig;
-            mvz = own.gvz * ig;
-        }
+        finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
     }
-    nd.mass[nid] = mass;
-    nd.comx[nid] = cx;
-    nd.comy[nid] = cy;
-    nd.comz[nid] = cz;
-    nd.gas[nid] = gas;
-    nd.mvx[nid] = mvx;
-    nd.mvy[nid] = mvy;
-    nd.mvz[nid] = mvz;
-    nd.ngas[nid] = own.ng;
+    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, 0, true, lp, theta);
+}
 
-    // FP32 walk record: COM split into hi + lo floats
-    float hx = (float)cx, hy = (float)cy, hz = (float)cz;
-    float lx = (float)(cx - (double)hx), ly = (float)(cy - (double)hy), lz = (float)(cz - (double)hz);
-    nd.wA[nid] = make_float4(hx, hy, hz, (float)mass);
-    float mac;
-    if (leaf) {
-        mac = -1.0f;
-    } else {
-        double q = nd.radius[nid] / theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
-        mac = (float)(q * q);
+// Internal nodes of one level, after the level below: sums over the children
+// in octant order, plus the node's out-of-bounds tail for the routed range.
+__global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list, Nodes nd,
+                                                        Particles P, const double *gas_prefix,
+                                                        const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt_lvl) return;
+    const int64_t nid = list[t];
+    const int32_t cnt = nd.count[nid], start = nd.start[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
+    const uint8_t mode = nd.mode[nid];
+    Sums tot, own;
+    own.zero();
+    uint8_t cmask = 0;
+    for (int o = 0; o < 8; o++) {
+        const int64_t c = first + o;
+        if (nd.count[c] == 0) continue;
+        own.add_node(nd, c);
+        if (nd.mass[c] != 0.0) cmask |= (uint8_t)(1u << o);
     }
-    nd.wB[nid] = make_float4(lx, ly, lz, mac);
-    if (leaf && lp >= 0)
-        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)gas);
-    else
-        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)gas);
+    tot = own;
+    for (int32_t i = start + cnt - ndrop; i < start + cnt; i++) tot.add_particle(P, i);
+    if (mode == MODE_PAR) own = tot;  // the parallel path sums escapers too (Node.cpp:477-499)
+    double mass, cx, cy, cz, gas, mvx, mvy, mvz;
+    finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
+    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, theta);
 }
 
 // count, min and max mass of each instance's gas particles (order-preserving
@@ -762,7 +934,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
     G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
     G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(tfirst) G(tfirstm) G(wA) G(wB) G(wD) G(flag)
-    G(rho)
+    G(rho) G(nlx) G(ilist)
 #undef G
     if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;
     c->node_cap = nc;
@@ -827,6 +999,38 @@ static int prepare_gas_tables(Ctx *c, int n)
     return AG2_OK;
 }
 
+// buffers of a level: w = level & 1 selects the current half of each pair
+static LevelBufs level_bufs(Ctx *c, int w)
+{
+    int32_t *perm[2] = {c->perm, c->perm2};
+    int32_t *pos[2] = {c->posnode, c->posnode2};
+    const size_t cap = c->cap;
+    int64_t *key = c->pkey;  // [buffer][coordinate][cap]
+    LevelBufs b;
+    b.ap = c->ap[w];
+    b.ap_next = c->ap[w ^ 1];
+    b.posnode = pos[w];
+    b.posnode_next = pos[w ^ 1];
+    b.perm = perm[w];
+    b.perm_next = perm[w ^ 1];
+    b.kx = key + (3 * w + 0) * cap;
+    b.ky = key + (3 * w + 1) * cap;
+    b.kz = key + (3 * w + 2) * cap;
+    b.kx_next = key + (3 * (w ^ 1) + 0) * cap;
+    b.ky_next = key + (3 * (w ^ 1) + 1) * cap;
+    b.kz_next = key + (3 * (w ^ 1) + 2) * cap;
+    b.perm_final = c->perm_final;
+    b.pnode = c->pnode;
+    b.digit = c->digit;
+    b.hist = c->hist;
+    b.cursor = c->cursor;
+    b.nl = c->nl[w];
+    b.nl_next = c->nl[w ^ 1];
+    b.leaves = c->leaves;
+    b.drop_list = c->drop_list;
+    return b;
+}
+
 int build_tree(Ctx *c)
 {
     const int n = (int)c->n;
@@ -861,35 +1065,31 @@ int build_tree(Ctx *c)
     const int thresh = c->prm.split_threshold;
     AG2_LAUNCH(c, k_ctl_reset, 1, 1, 0, c->ctl, K);
     AG2_LAUNCH(c, k_root_init, grid_for(K, kBlock), kBlock, 0, K, c->nd, c->ctl, c->inst_first, c->inst_R, thresh,
-               c->pnode);
+               c->nl[0], c->leaves);
+    AG2_LAUNCH(c, k_level0, grid_for(n, kBlock), kBlock, 0, n, c->pinst, c->nd, S.px, S.py, S.pz, level_bufs(c, 0),
+               c->ctl);
     c->inst_R_h.resize(K);
     AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if ((rc = sync_ctl(c)) != AG2_OK) return rc;
     c->root_radius = c->inst_R_h[0];
-    int root_needs = c->ctl_host->next_needs;
-    AG2_LAUNCH(c, k_init_positions, grid_for(n, kBlock), kBlock, 0, n, c->pinst, c->nd.needs, c->perm, c->posnode);
 
     c->level_base.assign({0, (int64_t)K});
+    c->int_off.assign({0});
     int level = 0;
-    int needs = root_needs;
-    while (needs > 0) {
-        int64_t base = c->level_base[level];
-        int64_t cnt_lvl = c->level_base[level + 1] - base;
-        if ((rc = ensure_hist(c, (size_t)cnt_lvl)) != AG2_OK) return rc;
-        if ((rc = ensure_node_capacity(c, (size_t)(c->level_base[level + 1] + 8 * cnt_lvl))) != AG2_OK) return rc;
-        AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, 9 * cnt_lvl * sizeof(int32_t), c->stream));
+    int nnl = c->ctl_host->next_needs;  // split list of the level
+    int nap = c->ctl_host->next_active; // active slots of the level
+    while (nnl > 0) {
+        if ((rc = ensure_hist(c, (size_t)nnl)) != AG2_OK) return rc;
+        if ((rc = ensure_node_capacity(c, (size_t)(c->level_base[level + 1] + 8 * (int64_t)nnl))) != AG2_OK)
+            return rc;
+        AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, 9 * (size_t)nnl * sizeof(int32_t), c->stream));
         AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_needs, 0, sizeof(int32_t), c->stream));
-        Particles &Sp = c->S();
-        AG2_LAUNCH(c, k_digit, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, Sp.px, Sp.py, Sp.pz,
-                   c->nd, c->digit, c->hist);
-        AG2_LAUNCH(c, k_nodes, grid_for((size_t)cnt_lvl * 8, kBlock), kBlock, 0, base, cnt_lvl, level, thresh,
-                   (int64_t)c->node_cap, c->nd, c->ctl, c->hist, c->cursor, (int)AG2_MAX_DEPTH, c->drop_list);
-        AG2_CUDA(c, cudaMemcpyAsync(c->perm2, c->perm, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
-        AG2_CUDA(c, cudaMemsetAsync(c->posnode2, 0xFF, n * sizeof(int32_t), c->stream));
-        AG2_LAUNCH(c, k_scatter, grid_for(n, kBlock), kBlock, 0, n, base, c->posnode, c->perm, c->digit, c->nd,
-                   c->cursor, c->perm2, c->posnode2, c->pnode);
-        std::swap(c->perm, c->perm2);
-        std::swap(c->posnode, c->posnode2);
+        AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_active, 0, sizeof(int32_t), c->stream));
+        const LevelBufs b = level_bufs(c, level & 1);
+        AG2_LAUNCH(c, k_digit, grid_for(nap, kBlock), kBlock, 0, nap, b, c->nd);
+        AG2_LAUNCH(c, k_nodes, grid_for((size_t)nnl * 8, kBlock), kBlock, 0, nnl, level, thresh,
+                   (int64_t)c->node_cap, c->nd, c->ctl, b, (int)AG2_MAX_DEPTH);
+        AG2_LAUNCH(c, k_scatter, grid_for(nap, kBlock), kBlock, 0, nap, b, c->nd, c->ctl);
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
         const Ctx::Ctl &h = *c->ctl_host;
         if (h.err_code) {
@@ -900,32 +1100,36 @@ int build_tree(Ctx *c)
             return set_err(c, h.err_code, "octree build failed");
         }
         c->level_base.push_back(h.node_count);
-        needs = h.next_needs;
+        c->int_off.push_back(h.nint);
+        nnl = h.next_needs;
+        nap = h.next_active;
         level++;
     }
     phase_mark(c, "build: levels");
     c->max_level = (int)c->level_base.size() - 2;
     c->nnodes = c->level_base.back();
     c->ninternal = (c->nnodes - K) / 8;
+    c->nleaves = c->ctl_host->nleaf;
     if (c->ctl_host->ndrop_nodes > kMaxDropNodes)
         return set_err(c, AG2_E_CAPACITY, "more than 65536 nodes with out-of-bounds particles");
     if (c->ctl_host->ndrop_nodes > 0)
         AG2_LAUNCH(c, k_sort_drops, (unsigned)c->ctl_host->ndrop_nodes, kBlock, 0, c->ctl_host->ndrop_nodes,
-                   c->drop_list, c->nd, c->perm, S.id, c->perm2);
+                   c->drop_list, c->nd, c->perm_final, S.id, c->perm2);
 
     // particle state into tree order
     Particles &src = c->st[c->cur];
     Particles &dst = c->st[c->cur ^ 1];
-    AG2_LAUNCH(c, k_reorder, grid_for(n, kBlock), kBlock, 0, n, c->perm, src, dst);
+    AG2_LAUNCH(c, k_reorder, grid_for(n, kBlock), kBlock, 0, n, c->perm_final, src, dst);
     c->cur ^= 1;
     AG2_LAUNCH(c, k_refnode, grid_for(n, kBlock), kBlock, 0, n, c->nd, c->pnode, c->S().id, c->refnode);
     phase_mark(c, "build: reorder");
 
-    // moments, deepest level first
-    for (int L = c->max_level; L >= 0; L--) {
-        int64_t base = c->level_base[L];
-        int64_t cnt = c->level_base[L + 1] - base;
-        AG2_LAUNCH(c, k_moments, grid_for((size_t)cnt, kBlock), kBlock, 0, base, cnt, c->nd, c->S(),
+    // moments: every leaf at once, then the internal nodes level by level, deepest first
+    AG2_LAUNCH(c, k_moments_leaf, grid_for(c->nleaves, kBlock), kBlock, 0, c->nleaves, c->leaves, c->nd, c->S(),
+               c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+    for (int L = (int)c->int_off.size() - 2; L >= 0; L--) {
+        const int32_t b0 = c->int_off[L], cnt = c->int_off[L + 1] - b0;
+        AG2_LAUNCH(c, k_moments_int, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.ilist + b0, c->nd, c->S(),
                    c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
     }
     phase_mark(c, "build: moments");

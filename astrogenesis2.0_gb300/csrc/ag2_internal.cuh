@@ -66,6 +66,9 @@ struct Nodes {
     // SPH / visual density scratch
     uint8_t *flag;
     double *rho;
+    // build scratch sized by the node pool
+    int32_t *nlx;    // index of a node in its level's split list
+    int32_t *ilist;  // internal nodes, one segment per level
 };
 
 struct Ctx {
@@ -90,8 +93,18 @@ struct Ctx {
     Particles st[2] = {};
     int cur = 0;
 
-    // build scratch
+    // build scratch.  During the level loop a slot (position in the partition)
+    // is active while its node is still split; perm/posnode/pkey hold the
+    // active slots' particle, split-list index and coordinate keys (two
+    // buffers, level after level), perm_final the particle a slot ends with.
     int32_t *perm = nullptr, *perm2 = nullptr, *posnode = nullptr, *posnode2 = nullptr;
+    int32_t *perm_final = nullptr;
+    int32_t *ap[2] = {};          // active slots of a level (compact list)
+    int32_t *nl[2] = {};          // split list of a level (node ids)
+    int32_t *leaves = nullptr;    // every non-empty leaf
+    int64_t *pkey = nullptr;      // 2 buffers x 3 coordinates x cap ordered keys
+    std::vector<int32_t> int_off; // internal-node list: first entry of each level
+    int32_t nleaves = 0;
     int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
     int32_t *refnode = nullptr;   // the reference's Particle::node per slot (-1 = null)
     int32_t *slot_of = nullptr;   // tree-order slot of each upload index
@@ -158,6 +171,10 @@ struct Ctx {
         unsigned long long inter_grav, inter_sph;
         int32_t list_count;
         int32_t ndrop_nodes;
+        int32_t next_active;    // active slots at the next level
+        int32_t nleaf;          // entries of the leaf list
+        int32_t nint;           // entries of the internal-node list
+        int32_t pad_;
     };
     Ctl *ctl = nullptr;      // device
     Ctl *ctl_host = nullptr; // pinned mirror
