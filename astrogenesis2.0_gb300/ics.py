@@ -150,6 +150,16 @@ def ensemble_sizes(count: int = 512, lo: int = 1024, hi: int = 65536, seed: int 
     return np.exp(g.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
 
 
+def ensemble(count: int = 512, lo: int = 1024, hi: int = 65536, seed: int = 4) -> dict:
+    """Independent Plummer spheres (M = 1, a = 1) with N_k log-uniform in
+    [lo, hi], concatenated; instance k owns indices [first[k], first[k+1])."""
+    sizes = ensemble_sizes(count, lo, hi, seed)
+    parts = [plummer(int(nk), seed=seed * 100003 + k) for k, nk in enumerate(sizes)]
+    out = {key: np.concatenate([q[key] for q in parts]) for key in ("pos", "vel", "mass", "type", "U")}
+    out["first"] = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return out
+
+
 def small_gas_cloud(n: int = 2000, seed: int = 5, gas_fraction: float = 0.5, u: float = 0.01):
     """Plummer sphere with a share of gas particles (SPH parity cases)."""
     d = plummer(n, seed=seed)

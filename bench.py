@@ -44,6 +44,9 @@ WORKLOADS = {
                      make=lambda: ics.merger(2097152, seed=3), e0=0.02, theta=0.5, dt=1e-3),
     "disk1m": dict(desc="isolated disk galaxy, 786,432 DM + 196,608 stars + 65,536 gas",
                    make=lambda: ics.disk_galaxy(seed=2), e0=0.02, theta=0.5, dt=1e-3),
+    "ensemble512": dict(desc="512 independent Plummer spheres (M=1, a=1), N log-uniform in [1024, 65536], "
+                             "gravity only, one tree build and one walk launch per step over all instances",
+                        make=lambda: ics.ensemble(512), e0=0.01, theta=0.5, dt=1e-3),
     "plummer16k": dict(desc="Plummer sphere N=16,384, M=1, a=1", make=lambda: ics.plummer(16384, seed=1), e0=0.01,
                        theta=0.5, dt=1e-3),
 }
@@ -151,6 +154,34 @@ def cpu_step_time(d: dict, wl: dict, walk_fraction: int, threads: int, world=Non
     return scaled, world, sample
 
 
+def cpu_step_time_instances(d: dict, wl: dict, every: int, threads: int, worlds=None):
+    """One step of every `every`-th independent simulation on the host (each its
+    own tree and walk over all its particles), scaled to all particles."""
+    import oracle
+
+    first = d["first"]
+    ks = list(range(0, len(first) - 1, every))
+    if worlds is None:
+        worlds = [oracle.World(d["pos"][first[k]:first[k + 1]], d["mass"][first[k]:first[k + 1]],
+                               d["type"][first[k]:first[k + 1]], d["vel"][first[k]:first[k + 1]],
+                               d["U"][first[k]:first[k + 1]], kind="port") for k in ks]
+    dt = wl["dt"]
+    m = 0
+    t0 = time.perf_counter()
+    for w in worlds:
+        w.kick(dt)
+        w.drift(dt)
+        w.build(threads)
+        w.forces(wl["e0"], wl["theta"], threads)
+        w.kick(dt)
+        m += w.n
+    t = time.perf_counter() - t0
+    n = int(first[-1])
+    sample = (f"{len(ks)} of {len(first) - 1} simulations (every {every}th, {m} particles), a full step each, "
+              f"scaled by {n / m:.1f}")
+    return t * n / m, worlds, sample
+
+
 def reference_arm(args, wl, d):
     from dist import finalize, init
 
@@ -163,7 +194,10 @@ def reference_arm(args, wl, d):
     world = None
     times = []
     for k in range(args.warmup + args.steps):
-        t, world, sample = cpu_step_time(d, wl, args.ref_walk_fraction, threads, world)
+        if "first" in d:
+            t, world, sample = cpu_step_time_instances(d, wl, args.ref_walk_fraction, threads, world)
+        else:
+            t, world, sample = cpu_step_time(d, wl, args.ref_walk_fraction, threads, world)
         if k >= args.warmup:
             times.append(t)
     per = sum(times) / len(times)
@@ -194,7 +228,8 @@ def config_block(args, wl, d, walk=None, split_threshold=100):
     n = int(len(d["mass"]))
     l2 = (f"per-step working set ~{n * BYTES_PER_PARTICLE / 2**30:.1f} GiB, far above the 129 MB L2 (no flush)"
           if not needs_flush(n) else "L2 flushed (512 MiB write) between timed steps")
-    return {"workload": f"{args.workload}: {wl['desc']}", "particles": n,
+    extra = {"instances": int(len(d["first"]) - 1)} if "first" in d else {}
+    return {"workload": f"{args.workload}: {wl['desc']}", "particles": n, **extra,
             "gas_particles": int(np.sum(d["type"] == 2)), "theta": wl["theta"], "eps": wl["e0"], "dt": wl["dt"],
             "G": 1.0, "walk": walk or args.precision, "split_threshold": split_threshold, "parallelism": "replicas",
             "l2": l2}
@@ -221,6 +256,8 @@ def our_arm(args, wl, d):
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     ctx.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    if "first" in d:
+        ctx.set_instances(d["first"])
     dt = wl["dt"]
     # initial forces as Simulation::init does (Simulation.cpp:120-139)
     ctx.build_tree()
@@ -337,6 +374,8 @@ def our_arm(args, wl, d):
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             ctx.upload(hpos, hmass, htype, vel=hvel, U=hU)
+            if "first" in d:
+                ctx.set_instances(d["first"])
             ctx.set_field("acc", hacc)
             ctx.step(dt)
             ctx.download("pos", out=hpos)
@@ -349,10 +388,20 @@ def our_arm(args, wl, d):
                "h2d_bytes_per_step": int(n * (24 + 24 + 8 + 8 + 1 + 24)),
                "d2h_bytes_per_step": int(n * (24 + 24 + 24 + 8))}
 
+    # independent simulations: each one stepped on its own (its own context and
+    # launches), with the plain FP64 walk and with the FP32 walk
+    per_launch = None
+    if "first" in d and args.plain_steps > 0:
+        ctx.close()
+        per_launch = one_sim_per_launch(d, wl, args.plain_steps, stream)
+
     cpu = None
     if D.rank == 0 and D.world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        tcpu, _, sample = cpu_step_time(d, wl, args.cpu_walk_fraction, threads)
+        if "first" in d:
+            tcpu, _, sample = cpu_step_time_instances(d, wl, args.cpu_walk_fraction, threads)
+        else:
+            tcpu, _, sample = cpu_step_time(d, wl, args.cpu_walk_fraction, threads)
         cpu = {"value": n / tcpu, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
 
     traffic = None
@@ -384,9 +433,50 @@ def our_arm(args, wl, d):
             "speedup_vs_plain": value / plain if plain else None,
             "force_error": force_error,
         }
+        if per_launch:
+            out["one_sim_per_launch"] = per_launch
+            out["speedup_vs_plain_per_launch"] = value / per_launch["fp64"]["value"]
         print(json.dumps(out), flush=True)
     ctx.close()
     finalize(D)
+
+
+def one_sim_per_launch(d, wl, steps, stream):
+    """Throughput of the same instances stepped one simulation at a time."""
+    import torch
+
+    import ag2
+
+    first = d["first"]
+    ctxs = []
+    for k in range(len(first) - 1):
+        a, b = int(first[k]), int(first[k + 1])
+        c = ag2.Context(b - a, e0=wl["e0"], theta=wl["theta"])
+        c.set_stream(stream.cuda_stream)
+        c.upload(d["pos"][a:b], d["mass"][a:b], d["type"][a:b], vel=d["vel"][a:b], U=d["U"][a:b])
+        c.build_tree()
+        c.forces()
+        ctxs.append(c)
+    n = int(first[-1])
+    res = {}
+    for prec in ("fp64", "fp32"):
+        for c in ctxs:
+            c.set(precision=prec)
+            c.step(wl["dt"])  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            for c in ctxs:
+                c.step(wl["dt"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        res[prec] = {"value": n * steps / t, "unit": UNIT, "steps": steps,
+                     "ms_per_step": t / steps * 1e3}
+    for c in ctxs:
+        c.close()
+    return res
 
 
 def main():
