@@ -192,6 +192,10 @@ class Context:
         a = np.ascontiguousarray(values, dtype=np.float64)
         self._check(self.L.ag2_set_field(self.h, FIELDS[field], _ptr(a), 0))
 
+    def set_field_device(self, field: str, src_ptr: int):
+        """Overwrite one field from a device buffer in the original particle order."""
+        self._check(self.L.ag2_set_field(self.h, FIELDS[field], ctypes.c_void_p(src_ptr), 1))
+
     # -- hot path -----------------------------------------------------------
     def build_tree(self):
         self._check(self.L.ag2_build_tree(self.h))

@@ -205,6 +205,7 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
     c->gas_stats_dirty = true;
     c->n_inst = 1;
     c->inst_dirty = true;
+    c->inst_explicit = false;
     int rc = sync_ctl(c);
     if (rc) return rc;
     if (c->ctl_host->err_code == AG2_E_NAN) return set_err(c, AG2_E_NAN, "non-finite particle position");
@@ -226,7 +227,7 @@ int ensure_instance_tables(Ctx *c)
         if (!ok) return set_err(c, AG2_E_NOMEM, "instance table allocation failed");
         c->inst_cap = K;
     }
-    if (K == 1) {
+    if (K == 1 && !c->inst_explicit) {
         c->inst_first_h = {0, (int64_t)c->n};
         c->inst_massInH_h = {c->prm.massInH};
     }
@@ -398,7 +399,7 @@ int ag2_set_params(ag2_ctx *c, const ag2_params *p)
     bool retree = p->split_threshold != c->prm.split_threshold;
     c->prm = *p;
     if (retree) c->have_tree = false;
-    if (c->n_inst == 1) c->inst_massInH_h = {p->massInH};
+    if (c->n_inst == 1 && !c->inst_explicit) c->inst_massInH_h = {p->massInH};
     return AG2_OK;
 }
 
@@ -594,6 +595,7 @@ int ag2_set_instances(ag2_ctx *c, int32_t n_inst, const int64_t *first, const do
     c->inst_massInH_h.assign(n_inst, c->prm.massInH);
     if (massInH) c->inst_massInH_h.assign(massInH, massInH + n_inst);
     c->inst_dirty = true;
+    c->inst_explicit = true;
     c->have_tree = false;
     return AG2_OK;
 }

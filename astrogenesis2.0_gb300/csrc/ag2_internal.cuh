@@ -150,6 +150,7 @@ struct Ctx {
     int32_t ngroups = 0;
     size_t groups_cap = 0;
     bool inst_dirty = true;         // instance tables need uploading
+    bool inst_explicit = false;     // layout from ag2_set_instances (keeps its massInH)
     // gasMass tables: instance k's sequential partial sums start at gas_off[k]
     int32_t *gas_off = nullptr;     // device
     uint8_t *gas_uni = nullptr;     // device: instance's gas particles share one mass

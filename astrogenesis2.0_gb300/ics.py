@@ -160,6 +160,35 @@ def ensemble(count: int = 512, lo: int = 1024, hi: int = 65536, seed: int = 4) -
     return out
 
 
+def serving_requests(count: int, seed: int = 7, lo: int = 4096, hi: int = 262144, gas_share: float = 0.3,
+                     gas_fraction: float = 0.1, steps_lo: int = 50, steps_hi: int = 500) -> list:
+    """Request mix of the serving workload: disk galaxies with N log-uniform in
+    [lo, hi] (3/4 dark halo), a share of them with gas at `gas_fraction` of the
+    particles (the rest of the disk in stars, otherwise all of it), and step
+    counts uniform in [steps_lo, steps_hi].  Returns dicts with the particle
+    arrays, massInH and steps."""
+    g = rng(seed)
+    sizes = np.exp(g.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
+    with_gas = g.uniform(0.0, 1.0, count) < gas_share
+    steps = g.integers(steps_lo, steps_hi + 1, count)
+    out = []
+    for k in range(count):
+        n = int(sizes[k])
+        n_dm = (3 * n) // 4
+        n_gas = int(round(gas_fraction * n)) if with_gas[k] else 0
+        d = disk_galaxy(n_dm, n - n_dm - n_gas, n_gas, seed=seed * 1009 + k)
+        if not n_gas:
+            d["massInH"] = 0.0
+        d["steps"] = int(steps[k])
+        out.append(d)
+    return out
+
+
+def poisson_arrivals(count: int, rate: float, seed: int = 8) -> np.ndarray:
+    """Arrival times (s) of a Poisson stream of `count` requests at `rate`/s."""
+    return np.cumsum(rng(seed).exponential(1.0 / rate, count))
+
+
 def small_gas_cloud(n: int = 2000, seed: int = 5, gas_fraction: float = 0.5, u: float = 0.01):
     """Plummer sphere with a share of gas particles (SPH parity cases)."""
     d = plummer(n, seed=seed)

@@ -47,6 +47,9 @@ WORKLOADS = {
     "ensemble512": dict(desc="512 independent Plummer spheres (M=1, a=1), N log-uniform in [1024, 65536], "
                              "gravity only, one tree build and one walk launch per step over all instances",
                         make=lambda: ics.ensemble(512), e0=0.01, theta=0.5, dt=1e-3),
+    "serving": dict(desc="request stream, Poisson arrivals at 10, 50 and 200 requests/s; disk galaxies with N "
+                         "log-uniform in [4096, 262144], 30% with gas at gas fraction 0.1, steps uniform in [50, 500]; "
+                         "continuous batching under a 150 GB budget", make=None, e0=0.02, theta=0.5, dt=1e-3),
     "plummer16k": dict(desc="Plummer sphere N=16,384, M=1, a=1", make=lambda: ics.plummer(16384, seed=1), e0=0.01,
                        theta=0.5, dt=1e-3),
 }
@@ -441,6 +444,179 @@ def our_arm(args, wl, d):
     finalize(D)
 
 
+SERVE_BUDGET_BYTES = 150e9
+SERVE_BYTES_PER_PARTICLE = 2 * BYTES_PER_PARTICLE  # the step context and the initial-force context
+
+
+def _serve_trace(specs, arrivals):
+    import serving
+
+    return [serving.Request(rid=k, pos=q["pos"], vel=q["vel"], mass=q["mass"], type=q["type"], U=q["U"],
+                            steps=q["steps"], massInH=q["massInH"], arrival=float(arrivals[k]))
+            for k, q in enumerate(specs)]
+
+
+def _fcfs(arrivals, service):
+    """Completion latencies of one server taking requests in arrival order."""
+    t_free, lat, end = 0.0, [], 0.0
+    for a, s_ in sorted(zip(arrivals, service)):
+        start = max(a, t_free)
+        t_free = start + s_
+        lat.append(t_free - a)
+        end = t_free
+    return lat, end
+
+
+def serving_arm(args, wl):
+    """Continuous batching of a Poisson request stream (one line; value = the
+    aggregate particle-steps/s at the highest arrival rate)."""
+    import numpy as np
+    import torch
+
+    import ag2
+    import serving
+    from dist import finalize, init
+
+    D = init()
+    torch.cuda.set_device(D.local_rank)
+    specs = ics.serving_requests(args.serve_requests)
+    sizes = np.array([len(q["mass"]) for q in specs])
+    steps = np.array([q["steps"] for q in specs])
+    budget_particles = int(SERVE_BUDGET_BYTES // SERVE_BYTES_PER_PARTICLE)
+    cap = int(min(budget_particles, sizes.sum()))
+    stream = torch.cuda.Stream()
+    eng = serving.Engine(cap, e0=wl["e0"], theta=wl["theta"], dt=wl["dt"], stream=stream)
+    # warm-up: two short simulations through the whole loop
+    warm = _serve_trace(specs[:2], [0.0, 0.0])
+    for q in warm:
+        q.steps = 3
+    serving.serve(eng, warm, realtime=False)
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+    clk = ClockSampler(int(vis) if vis.isdigit() else D.local_rank)
+    time.sleep(0.5)
+    l0 = eng.ctx.launches() + eng.init_ctx.launches()
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    per_rate = []
+    clk.mark_start()
+    for rate in rates:
+        arr = ics.poisson_arrivals(len(specs), rate, seed=8 + int(rate))
+        trace = _serve_trace(specs, arr)
+        ps0, st0 = eng.particle_steps, eng.steps_done
+        t0 = time.perf_counter()
+        res = serving.serve(eng, trace, realtime=True)
+        span = time.perf_counter() - t0
+        lat = np.array([r.completed - r.arrival for r in res])
+        per_rate.append({"rate_per_s": rate, "requests": len(res), "p50_latency_s": float(np.quantile(lat, 0.5)),
+                         "p99_latency_s": float(np.quantile(lat, 0.99)), "makespan_s": span,
+                         "particle_steps_per_s": (eng.particle_steps - ps0) / span,
+                         "engine_steps": eng.steps_done - st0})
+    clk.mark_stop()
+    clocks = clk.stop()
+    launches = eng.ctx.launches() + eng.init_ctx.launches() - l0
+    eng.close()
+
+    # each request alone on the plain FP64 path: per-step time measured on every
+    # 4th request (3 timed steps after its initial forces), fitted as a + b*N,
+    # then a first-come-first-served single server over the same arrivals
+    sample = list(range(0, len(specs), 4))
+    ms = []
+    for k in sample:
+        q = specs[k]
+        c = ag2.Context(len(q["mass"]), e0=wl["e0"], theta=wl["theta"], massInH=q["massInH"], precision="fp64")
+        c.set_stream(stream.cuda_stream)
+        c.upload(q["pos"], q["mass"], q["type"], vel=q["vel"], U=q["U"])
+        c.build_tree()
+        c.sph_density()
+        c.forces()
+        c.step(wl["dt"])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            c.step(wl["dt"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1) / 3)
+        c.close()
+    A = np.stack([np.ones(len(sample)), sizes[sample]], axis=1)
+    coef, *_ = np.linalg.lstsq(A, np.array(ms) / 1e3, rcond=None)
+    service = steps * (coef[0] + coef[1] * sizes)
+    plain = []
+    for rate in rates:
+        arr = ics.poisson_arrivals(len(specs), rate, seed=8 + int(rate))
+        lat, end = _fcfs(arr, service)
+        plain.append({"rate_per_s": rate, "p50_latency_s": float(np.quantile(lat, 0.5)),
+                      "p99_latency_s": float(np.quantile(lat, 0.99)),
+                      "particle_steps_per_s": float((sizes * steps).sum() / end)})
+    top = per_rate[-1]
+    n_h2d = int(sum(len(q["mass"]) * (24 + 24 + 8 + 8 + 1) for q in specs))
+    n_d2h = int(sum(len(q["mass"]) * (24 + 24 + 24 + 8 + 8) for q in specs))
+    if D.rank == 0:
+        out = {
+            "metric": METRIC, "value": top["particle_steps_per_s"], "unit": UNIT, "n_gpus": D.world,
+            "steps": int(top["engine_steps"]), "warmup": 1, "ms_per_step": top["makespan_s"] / top["engine_steps"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"serving: {wl['desc']}", "requests": len(specs), "particles": int(sizes.sum()),
+                       "gas_requests": int(sum((q["type"] == 2).any() for q in specs)), "theta": wl["theta"],
+                       "eps": wl["e0"], "dt": wl["dt"], "capacity_particles": cap,
+                       "budget_particles": budget_particles, "parallelism": "replicas",
+                       "l2": "resident state far above the 129 MB L2 at the higher rates; no flush"},
+            "e2e": {"value": top["particle_steps_per_s"], "unit": UNIT,
+                    "h2d_bytes_per_step": n_h2d / max(1, sum(r["engine_steps"] for r in per_rate)) * len(rates),
+                    "d2h_bytes_per_step": n_d2h / max(1, sum(r["engine_steps"] for r in per_rate)) * len(rates),
+                    "note": "requests arrive as host arrays and results return to the host; latencies are wall clock"},
+            "gpu_launches": launches, "clocks": clocks, "roofline": None,
+            "serving": per_rate,
+            "plain_alone": {"model": f"FP64 path, one request at a time in arrival order; per-step time "
+                                     f"{coef[0] * 1e3:.3f} ms + {coef[1] * 1e9:.3f} ns x N fitted on {len(sample)} "
+                                     f"requests", "rates": plain},
+            "speedup_vs_plain_alone": top["particle_steps_per_s"] / plain[-1]["particle_steps_per_s"],
+        }
+        print(json.dumps(out), flush=True)
+    finalize(D)
+
+
+def serving_reference_arm(args, wl):
+    """The reference's CPU algorithm serving the same requests one at a time."""
+    import numpy as np
+
+    import oracle
+    from dist import finalize, init
+
+    D = init(backend="gloo")
+    if D.rank != 0:
+        finalize(D)
+        return
+    specs = ics.serving_requests(args.serve_requests)
+    threads = os.cpu_count() or 1
+    ks = list(range(0, len(specs), 8))
+    per_step = []
+    for k in ks:
+        q = specs[k]
+        w = oracle.World(q["pos"], q["mass"], q["type"], q["vel"], q["U"], kind="port")
+        t0 = time.perf_counter()
+        w.kick(wl["dt"])
+        w.drift(wl["dt"])
+        w.build(threads)
+        if (q["type"] == 2).any():
+            w.gas_density(q["massInH"])
+        w.forces(wl["e0"], wl["theta"], threads)
+        w.kick(wl["dt"])
+        per_step.append(time.perf_counter() - t0)
+    sizes = np.array([len(q["mass"]) for q in specs])
+    steps = np.array([q["steps"] for q in specs])
+    rate_ps = float(sizes[ks].sum() / np.sum(per_step))
+    out = {"metric": METRIC, "value": rate_ps, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": 1, "warmup": 0, "ms_per_step": float(np.mean(per_step) * 1e3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"serving: {wl['desc']}", "requests": len(specs), "particles": int(sizes.sum()),
+                      "total_particle_steps": int((sizes * steps).sum())},
+           "cpu_baseline": {"value": rate_ps, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"one step of every 8th request ({len(ks)} requests), each alone"},
+           "e2e": {"value": rate_ps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    finalize(D)
+
+
 def one_sim_per_launch(d, wl, steps, stream):
     """Throughput of the same instances stepped one simulation at a time."""
     import torch
@@ -493,10 +669,18 @@ def main():
     ap.add_argument("--cpu-walk-fraction", type=int, default=8)
     ap.add_argument("--ref-walk-fraction", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rates", default="10,50,200")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     wl = WORKLOADS[args.workload]
+    if args.workload == "serving":
+        if args.impl == "reference":
+            serving_reference_arm(args, wl)
+        else:
+            serving_arm(args, wl)
+        return
     d = wl["make"]()
     if args.impl == "reference":
         reference_arm(args, wl, d)

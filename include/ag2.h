@@ -119,7 +119,8 @@ size_t ag2_count(const ag2_ctx *ctx);
  * neighbour mass (massInH[k]; NULL = params.massInH) and its own walk groups, so
  * its results do not depend on what else shares the context; every hot-path
  * call below then processes all instances at once.  ag2_upload resets the
- * layout to one instance. */
+ * layout to one instance that follows params.massInH; a layout set here (even
+ * of one instance) keeps its own massInH until the next upload. */
 int ag2_set_instances(ag2_ctx *ctx, int32_t n_inst, const int64_t *first, const double *massInH);
 int ag2_instance_radius(ag2_ctx *ctx, int32_t instance, double *radius);
 
