@@ -72,13 +72,22 @@ DeviceState &device_state(const Sim *sim)
     return *st;
 }
 
+// What the integrator reads of the root node (Simulation.cpp:123-126:
+// tree->root->radius for the initial size and visualDensityRadius).
+struct RootInfo {
+    double radius = 0.0;
+};
+
 template <class Sim>
 class Tree {
 public:
     explicit Tree(Sim *sim) : simulation(sim) {}
     ~Tree() = default;
+    Tree(const Tree &) = delete;
+    Tree &operator=(const Tree &) = delete;
 
     Sim *simulation;
+    RootInfo *root = &root_info_;  // valid after buildTree
 
     // Tree::buildTree (Tree.cpp:24-55)
     void buildTree()
@@ -110,7 +119,8 @@ public:
         dudt_.resize(n);
         for (size_t i = 0; i < n; i++) dudt_[i] = ps[i]->dUdt;
         if (!check(ag2_set_field(ctx(), AG2_DUDT, dudt_.data(), 0), "buildTree")) return;
-        check(ag2_build_tree(ctx()), "buildTree");
+        if (!check(ag2_build_tree(ctx()), "buildTree")) return;
+        check(ag2_root_radius(ctx(), &root_info_.radius), "buildTree");
     }
 
     // Tree::calculateForces (Tree.cpp:57-83): acc and dUdt of every particle
@@ -160,6 +170,7 @@ public:
     }
 
 private:
+    RootInfo root_info_;
     std::vector<double> pos_, vel_, mass_, U_, acc_, dudt_, tmp_;
     std::vector<uint8_t> type_;
 

@@ -218,6 +218,16 @@ def reference_arm(args, wl, d):
 
 
 L2_BYTES = 129 * 2 ** 20
+
+
+def _hbm_peak() -> float:
+    try:
+        return float(json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0  # fallback: one earlier copy-bandwidth measurement on a GB300
+
+
+HBM_PEAK_GBS = _hbm_peak()
 BYTES_PER_PARTICLE = 1400  # particle state (~200 B) + ~3.9 nodes of ~300 B
 
 
@@ -274,7 +284,11 @@ def our_arm(args, wl, d):
 
     def step(ev=None):
         ctx.kick_drift(dt)
+        if ev is not None:
+            ev[2].record(stream)
         ctx.build_tree()
+        if ev is not None:
+            ev[3].record(stream)
         ctx.sph_density()
         if ev is not None:
             ev[0].record(stream)
@@ -300,7 +314,7 @@ def our_arm(args, wl, d):
             with torch.cuda.stream(stream):
                 flush.fill_(1.0)
         se = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev = tuple(torch.cuda.Event(enable_timing=True) for _ in range(4))  # walk start/end, build start/end
         se[0].record(stream)
         step(ev)
         se[1].record(stream)
@@ -318,7 +332,14 @@ def our_arm(args, wl, d):
     t = sum(a.elapsed_time(b) for a, b in step_ev) / 1e3
     tmax = max_over_ranks(t, D)
     value = n * args.steps * D.world / tmax
-    walk_ms = [a.elapsed_time(b) for a, b in walk_ev]
+    walk_ms = [e[0].elapsed_time(e[1]) for e in walk_ev]
+    build_ms = [e[2].elapsed_time(e[3]) for e in walk_ev]
+    _, n_internal, _ = ctx.node_count()
+    # algorithmic build bytes per step: N (32 read pos+mass + 12 write key+index) + N 24 (sort pass) +
+    # N (33 + 32) (gather/scatter into tree order) + occupied nodes x 2 x 64 (write, then read for moments);
+    # occupied nodes = internal nodes + at most N non-empty leaves
+    build_bytes = n * (32 + 12 + 24 + 33 + 32) + (n_internal + n) * 128
+    build_avg_s = sum(build_ms) / len(build_ms) / 1e3
     walk_avg_s = sum(walk_ms) / len(walk_ms) / 1e3
     flop_per_walk = (FLOP_GRAV * inter_g + FLOP_SPH * inter_s) / args.steps
     achieved = flop_per_walk / walk_avg_s / 1e12
@@ -429,6 +450,11 @@ def our_arm(args, wl, d):
                          "traffic": traffic, "peak_source": "measured FP32 FMA throughput (ag2_fp32_peak_probe, "
                                                             "this run)", "walk_ms": walk_avg_s * 1e3,
                          "flop_per_launch": flop_per_walk},
+            "roofline_build": {"bound": "hbm", "kernel": "octree build (every build kernel, one step)",
+                               "achieved": build_bytes / build_avg_s / 1e9, "peak": HBM_PEAK_GBS, "unit": "GB/s",
+                               "frac": build_bytes / build_avg_s / 1e9 / HBM_PEAK_GBS, "traffic": None,
+                               "bytes_per_build": build_bytes, "build_ms": build_avg_s * 1e3,
+                               "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "cpu_baseline": cpu,
             "interactions_per_s": (inter_g + inter_s) / args.steps / walk_avg_s,
             "interactions_per_step": {"gravity": inter_g / args.steps, "sph": inter_s / args.steps},

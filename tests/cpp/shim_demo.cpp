@@ -65,6 +65,8 @@ int main(int argc, char **argv)
         // initial forces (Simulation.cpp:120-139)
         ag2host::Tree<Simulation> tree(&sim);
         tree.buildTree();
+        sim.visualDensityRadius = tree.root->radius / 100000;  // Simulation.cpp:126
+        tree.calcVisualDensity();
         tree.calcGasDensity();
         tree.calculateForces();
     }
