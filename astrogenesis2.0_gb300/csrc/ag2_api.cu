@@ -169,7 +169,7 @@ void free_nodes(Nodes &d)
                   d.cx,    d.cy,    d.cz,    d.bkey,  d.mass,   d.comx,    d.comy, d.comz, d.gas,   d.mvx,
                   d.mvy,   d.mvz,   d.ngas,  d.tm,    d.tmx,    d.tmy,     d.tmz,  d.tg,   d.tgvx,  d.tgvy,
                   d.tgvz,  d.tng,   d.tfirst, d.tfirstm, d.wA,   d.wB,      d.wD,   d.flag, d.rho,
-                  d.radius, d.inst, d.nlx, d.ilist};
+                  d.radius, d.inst, d.nlx, d.lint, d.lil};
     for (void *q : ps) cudaFree(q);
     d = Nodes{};
 }
@@ -346,6 +346,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
         return rc;
     }
     c->stream = c->own_stream;
+    c->leaves_cap = cap + kLeafListSpare;
     bool ok = alloc_particles(c, c->st[0], cap) == AG2_OK && alloc_particles(c, c->st[1], cap) == AG2_OK;
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
@@ -356,7 +357,9 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
          cudaMalloc(&c->pinst, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->perm_final, cap * 4) == cudaSuccess && cudaMalloc(&c->ap[0], cap * 4) == cudaSuccess &&
          cudaMalloc(&c->ap[1], cap * 4) == cudaSuccess && cudaMalloc(&c->nl[0], cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->nl[1], cap * 4) == cudaSuccess && cudaMalloc(&c->leaves, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->nl[1], cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->leaves, (cap + kLeafListSpare) * 4) == cudaSuccess &&
+         cudaMalloc(&c->lroots, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->pkey, 6 * cap * sizeof(int64_t)) == cudaSuccess &&
          cudaMalloc(&c->ctl, sizeof(Ctx::Ctl)) == cudaSuccess &&
          cudaMallocHost(&c->ctl_host, sizeof(Ctx::Ctl)) == cudaSuccess;
@@ -383,7 +386,7 @@ int ag2_destroy(ag2_ctx *c)
                   c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
                   c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->inst_first, c->inst_R,
                   c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax,
-                  c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey};
+                  c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     for (auto &e : c->ev)
@@ -621,7 +624,7 @@ int ag2_node_count(ag2_ctx *c, int64_t *nodes, int64_t *internal, int32_t *max_d
 {
     if (!c) return AG2_E_INVALID;
     if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
-    if (nodes) *nodes = c->nnodes;
+    if (nodes) *nodes = c->nnodes_true;
     if (internal) *internal = c->ninternal;
     if (max_depth) *max_depth = c->max_level;
     return AG2_OK;

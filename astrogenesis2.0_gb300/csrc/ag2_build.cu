@@ -185,7 +185,7 @@ __device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
 // root of instance k is node k (Tree.cpp:28-33: centre at the origin, half-width
 // from calcTreeWidth, depth 0)
 __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *first, const double *R, int thresh,
-                            int32_t *nl0, int32_t *leaves)
+                            int32_t *nl0, int32_t *leaves, bool local_ok, int32_t *lroots)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_inst) return;
@@ -204,15 +204,19 @@ __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *
     nd.inst[k] = k;
     const uint8_t mode = n == 0 ? MODE_EMPTY : n == 1 ? MODE_VEC1 : n < thresh ? MODE_SER_ENTRY : MODE_PAR;
     nd.mode[k] = mode;
-    const uint8_t needs = (mode == MODE_PAR || mode == MODE_SER_ENTRY) ? 1 : 0;
+    // 1: split by the level loop; 2: a serial subtree built by one warp (k_local)
+    const uint8_t needs = mode == MODE_PAR ? 1 : mode == MODE_SER_ENTRY ? (local_ok ? 2 : 1) : 0;
     nd.needs[k] = needs;
     nd.leafpos[k] = (mode == MODE_VEC1) ? start : -1;
     if (mode == MODE_VEC1) leaves[atomicAdd(&ctl->nleaf, 1)] = k;
-    if (needs) {
-        set_bounds(nd, k, R[k]);
+    if (needs == 2) atomicAdd(&ctl->nlocal_part, n);
+    if (needs) set_bounds(nd, k, R[k]);
+    if (needs == 1) {
         const int q = atomicAdd(&ctl->next_needs, 1);
         nl0[q] = k;
         nd.nlx[k] = q;
+    } else if (needs == 2) {
+        lroots[atomicAdd(&ctl->nlocal, 1)] = k;
     }
 }
 
@@ -226,7 +230,6 @@ __global__ void k_ctl_reset(Ctx::Ctl *ctl, int n_inst)
     ctl->ndrop_nodes = 0;
     ctl->next_active = 0;
     ctl->nleaf = 0;
-    ctl->nint = 0;
 }
 
 // Block-wide reservation in a compact list: every thread of the block calls
@@ -273,6 +276,8 @@ struct LevelBufs {
     int32_t *nl_next;
     int32_t *leaves;         // every non-empty leaf
     int32_t *drop_list;      // nodes with out-of-bounds tails of two or more
+    int32_t *lroots;         // roots of serial subtrees for k_local
+    bool local_ok;           // serial subtrees go to k_local (else they stay in the level loop)
 };
 
 // Level 0: the slots of an instance whose root is split are active (the
@@ -290,7 +295,8 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
     int32_t *posnode = const_cast<int32_t *>(b.posnode);
     if (i < n) {
         const int k = pinst[i];
-        if (nd.needs[k]) {
+        const uint8_t nk = nd.needs[k];
+        if (nk == 1) {
             act = true;
             perm[i] = i;
             posnode[i] = nd.nlx[k];
@@ -299,7 +305,12 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
             const_cast<int64_t *>(b.kz)[i] = okey(pz[i]);
         } else {
             b.perm_final[i] = i;
-            b.pnode[i] = k;  // one-particle root
+            b.pnode[i] = k;  // one-particle root, or a serial root for k_local
+            if (nk == 2) {
+                const_cast<int64_t *>(b.kx)[i] = okey(px[i]);
+                const_cast<int64_t *>(b.ky)[i] = okey(py[i]);
+                const_cast<int64_t *>(b.kz)[i] = okey(pz[i]);
+            }
         }
     }
     const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
@@ -426,8 +437,9 @@ __global__ void __launch_bounds__(kBlock) k_nodes(int nnl, int level, int thresh
         else
             cm = MODE_PAR;
         nd.mode[c] = cm;
-        const bool cneeds = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER);
-        nd.needs[c] = cneeds ? 1 : 0;
+        const bool clocal = b.local_ok && cm == MODE_SER_ENTRY;
+        const bool cneeds = (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER) && !clocal;
+        nd.needs[c] = cneeds ? 1 : clocal ? 2 : 0;
         nd.leafpos[c] = (cm == MODE_VEC1) ? s : -1;
         if (cc > 0) {  // empty children's centres are never read on the device
             const double x = __dadd_rn(nd.cx[nid], (o & 1) ? rc : -rc);
@@ -436,24 +448,31 @@ __global__ void __launch_bounds__(kBlock) k_nodes(int nnl, int level, int thresh
             nd.cx[c] = x;
             nd.cy[c] = y;
             nd.cz[c] = z;
-            if (cneeds) set_bounds_v(nd, c, x, y, z, rc);
+            if (cm != MODE_VEC1) set_bounds_v(nd, c, x, y, z, rc);
         }
     }
-    const bool cneeds = split && (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER);
+    const bool clocal = split && b.local_ok && cm == MODE_SER_ENTRY;
+    const int32_t qr = block_reserve<int32_t>(clocal, &ctl->nlocal, 1, sh, &sbase);
+    if (clocal) b.lroots[qr] = (int32_t)c;
+    {
+        const unsigned lp = __reduce_add_sync(0xffffffffu, clocal ? (unsigned)h[o] : 0u);
+        if (lane == 0 && lp) atomicAdd(&ctl->nlocal_part, (int)lp);
+    }
+    const bool cneeds = split && !clocal && (cm == MODE_PAR || cm == MODE_SER_ENTRY || cm == MODE_SER);
     const int32_t q = block_reserve<int32_t>(cneeds, &ctl->next_needs, 1, sh, &sbase);
     if (cneeds) {
         b.nl_next[q] = (int32_t)c;
         nd.nlx[c] = q;
     }
     // leaves: one-particle children of a parallel node, and nodes of this list
-    // that stay leaves; internal nodes of this level
+    // that stay leaves; internal nodes with their level
     const bool leaf_self = exists && o == 0 && !internal;
     const bool lflag = (split && cm == MODE_VEC1) || leaf_self;
     const int32_t ql = block_reserve<int32_t>(lflag, &ctl->nleaf, 1, sh, &sbase);
     if (lflag) b.leaves[ql] = (int32_t)(leaf_self ? nid : c);
     const bool iflag = split && o == 0;
-    const int32_t qi = block_reserve<int32_t>(iflag, &ctl->nint, 1, sh, &sbase);
-    if (iflag) nd.ilist[qi] = (int32_t)nid;
+    const int32_t qi = block_reserve<int32_t>(iflag, &ctl->nlint, 1, sh, &sbase);
+    if (iflag) nd.lint[qi] = make_int2((int)nid, level);
 }
 
 // Partition of every active slot's particle by digit; settled particles go to
@@ -477,14 +496,17 @@ __global__ void __launch_bounds__(kBlock) k_scatter(int nap, LevelBufs b, Nodes 
         const int32_t first = nd.first[nid];
         if (first >= 0 && d < 8) {
             const int32_t child = first + d;
-            if (nd.needs[child]) {
-                b.perm_next[np] = p;
+            const uint8_t cn = nd.needs[child];
+            if (cn) {  // split again: by the next level (1) or by k_local (2), which reads the keys there
                 b.kx_next[np] = b.kx[i];
                 b.ky_next[np] = b.ky[i];
                 b.kz_next[np] = b.kz[i];
+            }
+            if (cn == 1) {
+                b.perm_next[np] = p;
             } else {
                 b.perm_final[np] = p;
-                b.pnode[np] = child;  // single-particle leaf
+                b.pnode[np] = child;  // single-particle leaf, or a serial root for k_local
             }
         } else {
             b.perm_final[np] = p;
@@ -499,7 +521,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(int nap, LevelBufs b, Nodes 
             if (nd.start[first + o + 2] <= i) o += 2;
             if (nd.start[first + o + 1] <= i) o += 1;
             const int32_t cnode = first + o;
-            if (nd.needs[cnode]) {
+            if (nd.needs[cnode] == 1) {
                 act = true;
                 nj = nd.nlx[cnode];
             }
@@ -669,28 +691,36 @@ struct Sums {
     }
 };
 
-// RN(RN(x*m)/m) for m > 0 without a division.  With q = RN(x*m) = x*m*(1+e),
+// RN(q/m) for q = RN(x*m) and m > 0, without a division.  With q = x*m*(1+e),
 // |e| <= 2^-53, the quotient q/m lies strictly within one unit in the last
 // place of x, so it rounds to x or to x's neighbour on the quotient's side.
-// The residual r = q - x*m is exact (one fma), q/m - x = r/m, and the half gap
-// to the neighbour times m is exact (a power of two times m): comparing |r| with
-// it decides the rounding, ties to the even significand.  Outside the range
-// where those products cannot overflow or underflow, divide.
-__device__ __forceinline__ double mul_div_same(double x, double m)
+// The residual r = q - x*m is exact (one fma) and q/m - x = r/m.  Half the gap
+// to that neighbour is a power of two, so comparing |r| with it times m is a
+// comparison of bit patterns after an exponent shift; ties go to the even
+// significand.  Outside magnitudes 2^-400 .. 2^400 (where none of this can
+// underflow or overflow), divide.
+__device__ __forceinline__ double div_back(double x, double m, double q)
 {
-    const double q = __dmul_rn(x, m);
-    const double ax = fabs(x);
-    if (!(m > 0x1p-400 && m < 0x1p400 && ax < 0x1p400 && (ax > 0x1p-400 || x == 0.0))) return __ddiv_rn(q, m);
-    const double r = __fma_rn(-x, m, q);
-    if (r == 0.0) return x;
-    const long long bits = __double_as_longlong(x);
-    const bool away = (r > 0.0) == (x > 0.0);  // |q/m| > |x|
-    const double y = __longlong_as_double(away ? bits + 1 : bits - 1);  // neighbour on that side
-    const double lim = __dmul_rn(0.5 * fabs(__dsub_rn(y, x)), m);
-    const double ar = fabs(r);
-    if (ar < lim) return x;
-    if (ar > lim) return y;
-    return (bits & 1) ? y : x;
+    const long long bx = __double_as_longlong(x), bm = __double_as_longlong(m);
+    const int ex = (int)((bx >> 52) & 0x7ff), em = (int)((bm >> 52) & 0x7ff);
+    const bool xzero = (bx << 1) == 0;
+    if (bm < 0 || em < 1023 - 400 || em >= 1023 + 400 || (!xzero && (ex < 1023 - 400 || ex >= 1023 + 400)))
+        return __ddiv_rn(q, m);
+    if (xzero) return x;
+    const double r = __fma_rn(-x, m, q);  // exact: q - x*m
+    const long long br = __double_as_longlong(r);
+    if ((br << 1) == 0) return x;
+    const bool away = (br < 0) == (bx < 0);  // |q/m| > |x|
+    // half the gap on that side: 2^(e-53) for the ulp 2^(e-52) of x's binade,
+    // 2^(e-54) toward zero from a power of two (the binade below is twice as fine)
+    const bool pow2 = (bx & 0x000fffffffffffffLL) == 0;
+    const int k = (ex - 1023) - 53 - ((!away && pow2) ? 1 : 0);
+    const long long blim = bm + ((long long)k << 52);  // m * 2^k, still normal in the guarded range
+    const long long bar = br & 0x7fffffffffffffffLL;   // |r|
+    const long long by = away ? bx + 1 : bx - 1;       // the neighbour
+    if (bar < blim) return x;
+    if (bar > blim) return __longlong_as_double(by);
+    return (bx & 1) ? __longlong_as_double(by) : x;
 }
 
 // node record shared by leaves and internal nodes: moments, FP32 walk records
@@ -768,28 +798,76 @@ __device__ __forceinline__ void finish_sums(Nodes &nd, int64_t nid, uint8_t mode
     }
 }
 
-// Leaves (every level at once: a leaf's moments read only its particles).
-__global__ void __launch_bounds__(kBlock) k_moments_leaf(int nleaf, const int32_t *__restrict__ list, Nodes nd,
-                                                         Particles P, const double *gas_prefix,
-                                                         const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+// Leaf moments.  idx(k) is the state index of the k-th particle of the node's
+// range (the leaf particle, when there is one, is the first).
+template <class Idx>
+__device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Particles &P, Idx idx,
+                                             const double *gas_prefix, const int32_t *gas_off,
+                                             const uint8_t *gas_uni, double theta)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nleaf) return;
-    const int64_t nid = list[t];
-    const int32_t cnt = nd.count[nid], start = nd.start[nid], ndrop = nd.ndrop[nid];
+    const int32_t cnt = nd.count[nid], ndrop = nd.ndrop[nid];
     const uint8_t mode = nd.mode[nid];
+    if (cnt == 1 && ndrop == 0) {
+        // the common leaf: one particle inside its bounds.  Its sums are the
+        // particle's own values (0 + a = a and 0 + x*m = RN(x*m) exactly).
+        const int32_t i = idx(0);
+        const double mp = P.m[i], px = P.px[i], py = P.py[i], pz = P.pz[i];
+        const bool isgas = P.type[i] == 2;
+        Sums t;
+        t.m = mp;
+        t.mx = __dmul_rn(px, mp);
+        t.my = __dmul_rn(py, mp);
+        t.mz = __dmul_rn(pz, mp);
+        t.g = isgas ? mp : 0.0;
+        t.gvx = t.gvy = t.gvz = 0.0;
+        double mvx = 0.0, mvy = 0.0, mvz = 0.0;
+        if (isgas) {
+            const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
+            t.gvx = __dmul_rn(vx, mp);
+            t.gvy = __dmul_rn(vy, mp);
+            t.gvz = __dmul_rn(vz, mp);
+            if (mode != MODE_VEC1 && __double_as_longlong(mp) > 0) {  // Node.cpp:679-696
+                mvx = vx;
+                mvy = vy;
+                mvz = vz;
+            }
+        }
+        t.ng = isgas ? 1 : 0;
+        t.first_id = P.id[i];
+        t.first_m = mp;
+        double cx = px, cy = py, cz = pz;  // VEC1: the position itself (Node.cpp:409-418)
+        if (mode != MODE_VEC1) {
+            // one serial insertion into an empty leaf (Node.cpp:678-698): the
+            // running mean (0*(m-m) + x*m)/m, rounded as the reference rounds it
+            const long long bm = __double_as_longlong(mp);
+            if (bm > 0) {
+                cx = div_back(px, mp, t.mx);
+                cy = div_back(py, mp, t.my);
+                cz = div_back(pz, mp, t.mz);
+            } else if ((bm << 1) != 0) {
+                cx = __ddiv_rn(t.mx, mp);
+                cy = __ddiv_rn(t.my, mp);
+                cz = __ddiv_rn(t.mz, mp);
+            } else {
+                cx = cy = cz = 0.0;
+            }
+        }
+        store_node(nd, nid, P, t, mp, cx, cy, cz, t.g, mvx, mvy, mvz, t.ng, 0, true, i, theta);
+        return;
+    }
     Sums tot, own;  // tot: whole routed range; own: the reference's mass set
     tot.zero();
-    for (int32_t i = start; i < start + cnt; i++) tot.add_particle(P, i);
+    for (int32_t k = 0; k < cnt; k++) tot.add_particle(P, idx(k));
     if (mode == MODE_VEC1) {
         own = tot;
     } else {
         own.zero();
-        for (int32_t i = start; i < start + cnt - ndrop; i++) own.add_particle(P, i);
+        for (int32_t k = 0; k < cnt - ndrop; k++) own.add_particle(P, idx(k));
     }
     double mass, cx, cy, cz, gas, mvx, mvy, mvz;
-    const int32_t lp = nd.leafpos[nid];
-    if (lp >= 0) {
+    const bool has = nd.leafpos[nid] >= 0;
+    const int32_t lp = has ? idx(0) : -1;
+    if (has) {
         const double mp = P.m[lp];
         const bool isgas = P.type[lp] == 2;
         mass = mp;
@@ -805,9 +883,9 @@ __global__ void __launch_bounds__(kBlock) k_moments_leaf(int nleaf, const int32_
             // running mean (0*(m-m) + x*m)/m, rounded as the reference rounds it
             cx = cy = cz = 0.0;
             if (mass > 0.0) {
-                cx = mul_div_same(P.px[lp], mp);
-                cy = mul_div_same(P.py[lp], mp);
-                cz = mul_div_same(P.pz[lp], mp);
+                cx = div_back(P.px[lp], mp, __dmul_rn(P.px[lp], mp));
+                cy = div_back(P.py[lp], mp, __dmul_rn(P.py[lp], mp));
+                cz = div_back(P.pz[lp], mp, __dmul_rn(P.pz[lp], mp));
             } else if (mass != 0.0) {
                 cx = __ddiv_rn(__dmul_rn(P.px[lp], mp), mass);
                 cy = __ddiv_rn(__dmul_rn(P.py[lp], mp), mass);
@@ -827,16 +905,15 @@ __global__ void __launch_bounds__(kBlock) k_moments_leaf(int nleaf, const int32_
     store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, 0, true, lp, theta);
 }
 
-// Internal nodes of one level, after the level below: sums over the children
-// in octant order, plus the node's out-of-bounds tail for the routed range.
-__global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list, Nodes nd,
-                                                        Particles P, const double *gas_prefix,
-                                                        const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+// Internal-node moments after its children's: sums over the children in octant
+// order, plus the node's out-of-bounds tail (idx(k), k in [count - ndrop, count))
+// for the routed range.
+template <class Idx>
+__device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const Particles &P, Idx idx,
+                                                 const double *gas_prefix, const int32_t *gas_off,
+                                                 const uint8_t *gas_uni, double theta)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt_lvl) return;
-    const int64_t nid = list[t];
-    const int32_t cnt = nd.count[nid], start = nd.start[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
+    const int32_t cnt = nd.count[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
     const uint8_t mode = nd.mode[nid];
     Sums tot, own;
     own.zero();
@@ -848,11 +925,398 @@ __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32
         if (nd.mass[c] != 0.0) cmask |= (uint8_t)(1u << o);
     }
     tot = own;
-    for (int32_t i = start + cnt - ndrop; i < start + cnt; i++) tot.add_particle(P, i);
+    for (int32_t k = cnt - ndrop; k < cnt; k++) tot.add_particle(P, idx(k));
     if (mode == MODE_PAR) own = tot;  // the parallel path sums escapers too (Node.cpp:477-499)
     double mass, cx, cy, cz, gas, mvx, mvy, mvz;
     finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
     store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, theta);
+}
+
+// Leaves (every level at once), on the state in tree order.  -1 entries pad
+// the list's per-warp stretches.
+__global__ void __launch_bounds__(kBlock) k_moments_leaf(int nleaf, const int32_t *__restrict__ list, Nodes nd,
+                                                         Particles P, const double *gas_prefix,
+                                                         const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nleaf) return;
+    const int64_t nid = list[t];
+    if (nid < 0) return;
+    const int32_t start = nd.start[nid];
+    moments_leaf(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+}
+
+// Internal nodes of one level, after the level below.
+__global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list, Nodes nd,
+                                                        Particles P, const double *gas_prefix,
+                                                        const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt_lvl) return;
+    const int64_t nid = list[t];
+    const int32_t start = nd.start[nid];
+    moments_internal(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+}
+
+// internal nodes per level (one shared-memory histogram per block)
+__global__ void __launch_bounds__(kBlock) k_lvl_hist(int n, const int2 *__restrict__ lint, int32_t *cnt)
+{
+    __shared__ int32_t hs[AG2_MAX_DEPTH];
+    for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x) hs[k] = 0;
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        const int2 e = lint[t];
+        if (e.x >= 0) atomicAdd(&hs[e.y], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x)
+        if (hs[k]) atomicAdd(&cnt[k], hs[k]);
+}
+
+// internal nodes into one list segment per level (cursors start at the segments)
+__global__ void k_bucket(int n, const int2 *__restrict__ lint, int32_t *lvl_off, int32_t *lil)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int2 e = lint[t];
+    if (e.x < 0) return;
+    lil[agg_inc(lvl_off, e.y)] = e.x;
+}
+
+// ---- serial subtrees, one warp each ---------------------------------------
+//
+// A node with fewer than split_threshold particles under a parallel node is the
+// root of a serial subtree (Node.cpp:420-428, 597-699): every node below it
+// splits when two of its particles land inside its bounds.  Such a subtree
+// never holds more than split_threshold - 1 particles, so one warp builds it in
+// shared memory, level by level, with the level loop's rules: the same rounded
+// bounds, digits, modes, drop tails in upload order, child centres and
+// half-widths.  Its leaves and internal nodes join the lists the moments
+// passes read.
+//
+// Nodes come from a warp-private pool of kPoolChunk nodes (one global atomic
+// per chunk); a chunk's unused tail stays a hole in the pool, which no kernel
+// reaches (every traversal starts at a root, and the per-node passes only
+// touch a node's own fields).
+
+constexpr int kLocalCapMax = 1024;  // largest serial subtree (particles) built by one warp
+constexpr int kLocalWarps = 8;      // warps per thread block of k_local (fewer for large subtrees)
+constexpr int kPoolChunk = 512;     // nodes per warp-private pool chunk
+constexpr int kLeafChunk = 256;     // leaf-list entries per warp-private stretch
+constexpr int kIntChunk = 128;      // internal-node-list entries per warp-private stretch
+
+// Shared memory of one warp for subtrees of up to `cap` particles (cap a
+// multiple of 8).  Per particle: keys 3 x 8 B and particle index 4 B (fixed
+// slots), position -> slot 2 x 2 B, digit 1 B.  Per frontier node (at most one
+// per particle): node 2 x 4 B, start and count 2 x 2 x 2 B, first child 4 B,
+// digit starts 9 x 2 B.
+__host__ __device__ constexpr size_t local_smem_bytes(int cap) { return (size_t)cap * 72; }
+
+__global__ void __launch_bounds__(kLocalWarps * 32) k_local(int nroots, const int32_t *__restrict__ roots, int cap,
+                                                            Nodes nd, Ctx::Ctl *ctl, const int64_t *__restrict__ pkey,
+                                                            int64_t keycap, int32_t *perm_final, int32_t *pnode,
+                                                            const int32_t *__restrict__ sid, int32_t *leaves,
+                                                            int64_t leaf_cap, int max_depth, int64_t node_cap)
+{
+    extern __shared__ __align__(16) unsigned char lsm[];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned char *base = lsm + (size_t)wib * local_smem_bytes(cap);
+    int64_t *KX = reinterpret_cast<int64_t *>(base);
+    int64_t *KY = KX + cap, *KZ = KY + cap;
+    int32_t *PID = reinterpret_cast<int32_t *>(KZ + cap);
+    int32_t *const FN0 = PID + cap, *const FN1 = PID + 2 * cap;
+    int32_t *FF = PID + 3 * cap;  // per frontier node: first child, -1 leaf, -2 cannot split
+    int16_t *const L0 = reinterpret_cast<int16_t *>(FF + cap);
+    int16_t *const L1 = L0 + cap;
+    int16_t *const FS0 = L1 + cap, *const FS1 = L1 + 2 * cap;
+    int16_t *const FC0 = L1 + 3 * cap, *const FC1 = L1 + 4 * cap;
+    int16_t *const FH = L1 + 5 * cap;  // 9 per frontier node
+    uint8_t *DIG = reinterpret_cast<uint8_t *>(FH + 9 * cap);
+
+    unsigned long long pool = 0, pool_end = 0;  // warp-private node pool [pool, pool_end)
+    int lpool = 0, lpool_end = 0;                // warp-private stretch of the leaf list
+    int ipool = 0, ipool_end = 0;                // ... and of the internal-node list
+    long long splits = 0;
+    int deepest = 0;
+    for (int r = blockIdx.x * (blockDim.x >> 5) + wib; r < nroots; r += nwarps) {
+        const int32_t v0 = roots[r];
+        const int32_t s0 = nd.start[v0], n = nd.count[v0];
+        int level = nd.level[v0];
+        {
+            const int bsel = level & 1;  // the level loop left the keys in the buffer of this node's level
+            const int64_t *gx = pkey + (3 * bsel + 0) * keycap, *gy = pkey + (3 * bsel + 1) * keycap,
+                          *gz = pkey + (3 * bsel + 2) * keycap;
+            for (int j = lane; j < n; j += 32) {
+                PID[j] = perm_final[s0 + j];
+                KX[j] = gx[s0 + j];
+                KY[j] = gy[s0 + j];
+                KZ[j] = gz[s0 + j];
+                L0[j] = (int16_t)j;
+            }
+        }
+        if (lane == 0) {
+            FN0[0] = v0;
+            FS0[0] = 0;
+            FC0[0] = (int16_t)n;
+        }
+        int nf = 1, cur = 0;
+        __syncwarp();
+        while (nf > 0) {
+            const int nxt = cur ^ 1;
+            // this level's (c) and the next level's (n) halves of the double buffers
+            int32_t *const fnc = cur ? FN1 : FN0, *const fnn = cur ? FN0 : FN1;
+            int16_t *const fsc = cur ? FS1 : FS0, *const fsn = cur ? FS0 : FS1;
+            int16_t *const fcc = cur ? FC1 : FC0, *const fcn = cur ? FC0 : FC1;
+            int16_t *const lc = cur ? L1 : L0, *const ln = cur ? L0 : L1;
+            // (a) digits and split decision, one lane per frontier node
+            for (int f = lane; f < nf; f += 32) {
+                const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
+                const int64_t *bk = nd.bkey + 9 * (int64_t)v;
+                const int64_t b0 = bk[0], b1 = bk[1], b2 = bk[2], b3 = bk[3], b4 = bk[4], b5 = bk[5], b6 = bk[6],
+                              b7 = bk[7], b8 = bk[8];
+                int16_t *hh = FH + 9 * f;
+#pragma unroll
+                for (int d = 0; d < 9; d++) hh[d] = 0;
+                for (int j = ls; j < ls + cnt; j++) {
+                    const int q = lc[j];
+                    const int64_t x = KX[q], y = KY[q], z = KZ[q];
+                    int d;
+                    // inclusive bounds and octant of Node.cpp:606-608, 706-716, as in k_digit
+                    if (x < b0 || x > b3 || y < b1 || y > b4 || z < b2 || z > b5)
+                        d = 8;
+                    else
+                        d = (x > b6 ? 1 : 0) | (y > b7 ? 2 : 0) | (z > b8 ? 4 : 0);
+                    DIG[j] = (uint8_t)d;
+                    hh[d]++;
+                }
+                const int32_t ndrop = hh[8], reached = cnt - ndrop;
+                int32_t acc = ls;
+#pragma unroll
+                for (int d = 0; d < 9; d++) {  // counts -> starts
+                    const int32_t cd = hh[d];
+                    hh[d] = (int16_t)acc;
+                    acc += cd;
+                }
+                nd.ndrop[v] = ndrop;
+                if (ndrop) ctl->any_drop = 1;
+                int32_t flag = 1;
+                if (reached < 2) {  // a leaf: serial insertion splits only for a second in-bounds particle
+                    nd.first[v] = -1;
+                    nd.leafpos[v] = reached == 1 ? s0 + ls : -1;
+                    flag = -1;
+                } else if (level + 1 >= max_depth) {
+                    atomicExch(&ctl->err_code, (int)AG2_E_COINCIDENT);
+                    atomicExch(&ctl->err_info, (int)v);
+                    nd.first[v] = -1;
+                    nd.leafpos[v] = -1;
+                    flag = -2;
+                }
+                FF[f] = flag;
+            }
+            __syncwarp();
+            // (b) 8-child blocks of this level's splits, from the warp's pool
+            int ns = 0;
+            for (int f = lane; f < nf; f += 32) ns += FF[f] == 1 ? 1 : 0;
+            ns = (int)__reduce_add_sync(full, (unsigned)ns);
+            unsigned long long cbase = 0;
+            if (ns) {
+                const unsigned long long need = 8ull * (unsigned long long)ns;
+                if (pool + need > pool_end) {
+                    const unsigned long long grab = need > (unsigned long long)kPoolChunk ? need : kPoolChunk;
+                    unsigned long long b = 0;
+                    if (lane == 0) b = atomicAdd((unsigned long long *)&ctl->node_count, grab);
+                    b = __shfl_sync(full, b, 0);
+                    if ((int64_t)(b + grab) > node_cap) {
+                        if (lane == 0) atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+                        return;
+                    }
+                    pool = b;
+                    pool_end = b + grab;
+                }
+                cbase = pool;
+                pool += need;
+                splits += ns;
+            }
+            {
+                int run = 0;
+                for (int f0 = 0; f0 < nf; f0 += 32) {
+                    const int f = f0 + lane;
+                    const bool s = f < nf && FF[f] == 1;
+                    const unsigned bb = __ballot_sync(full, s);
+                    if (s) {
+                        const int32_t fc = (int32_t)(cbase + 8ull * (unsigned long long)(run + __popc(bb & lt)));
+                        FF[f] = fc;
+                        nd.first[fnc[f]] = fc;
+                        nd.leafpos[fnc[f]] = -1;
+                    }
+                    run += __popc(bb);
+                }
+            }
+            // the leaves of this level join the leaf list
+            {
+                int nl = 0;
+                for (int f = lane; f < nf; f += 32) nl += FF[f] == -1 ? 1 : 0;
+                nl = (int)__reduce_add_sync(full, (unsigned)nl);
+                if (nl) {
+                    const int rem = lpool_end - lpool;
+                    int nb = 0;
+                    if (nl > rem) {  // the rest goes to a fresh stretch
+                        const int grab = max(nl - rem, kLeafChunk);
+                        if (lane == 0) nb = atomicAdd(&ctl->nleaf, grab);
+                        nb = __shfl_sync(full, nb, 0);
+                        if ((int64_t)nb + grab > leaf_cap) {
+                            if (lane == 0) atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+                            return;
+                        }
+                    }
+                    int run = 0;
+                    for (int f0 = 0; f0 < nf; f0 += 32) {
+                        const int f = f0 + lane;
+                        const bool isl = f < nf && FF[f] == -1;
+                        const unsigned bl = __ballot_sync(full, isl);
+                        if (isl) {
+                            const int k = run + __popc(bl & lt);
+                            leaves[k < rem ? lpool + k : nb + (k - rem)] = fnc[f];
+                        }
+                        run += __popc(bl);
+                    }
+                    if (nl > rem) {
+                        const int grab = max(nl - rem, kLeafChunk);
+                        lpool = nb + (nl - rem);
+                        lpool_end = nb + grab;
+                    } else {
+                        lpool += nl;
+                    }
+                }
+            }
+            // this level's internal nodes join the internal-node list with their level
+            {
+                int ni = 0;
+                for (int f = lane; f < nf; f += 32) ni += FF[f] >= 0 ? 1 : 0;
+                ni = (int)__reduce_add_sync(full, (unsigned)ni);
+                if (ni) {
+                    const int rem = ipool_end - ipool;
+                    int nb = 0, grab = 0;
+                    if (ni > rem) {
+                        grab = max(ni - rem, kIntChunk);
+                        if (lane == 0) nb = atomicAdd(&ctl->nlint, grab);
+                        nb = __shfl_sync(full, nb, 0);
+                        if ((int64_t)nb + grab > node_cap) {
+                            if (lane == 0) atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+                            return;
+                        }
+                    }
+                    int run = 0;
+                    for (int f0 = 0; f0 < nf; f0 += 32) {
+                        const int f = f0 + lane;
+                        const bool isi = f < nf && FF[f] >= 0;
+                        const unsigned bi = __ballot_sync(full, isi);
+                        if (isi) {
+                            const int k = run + __popc(bi & lt);
+                            nd.lint[k < rem ? ipool + k : nb + (k - rem)] = make_int2(fnc[f], level);
+                        }
+                        run += __popc(bi);
+                    }
+                    if (ni > rem) {
+                        ipool = nb + (ni - rem);
+                        ipool_end = nb + grab;
+                    } else {
+                        ipool += ni;
+                    }
+                }
+            }
+            __syncwarp();
+            // (c) partition by digit into the other order; leaves and drop tails settle
+            // (the digit starts serve as cursors: afterwards hh[d] is the end of digit d)
+            for (int f = lane; f < nf; f += 32) {
+                const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
+                int16_t *hh = FH + 9 * f;
+                for (int j = ls; j < ls + cnt; j++) {
+                    const int d = DIG[j];
+                    ln[hh[d]] = lc[j];
+                    hh[d]++;
+                }
+                // the out-of-bounds tail in upload order (the level loop's k_sort_drops rule)
+                const int32_t tb = hh[7], te = ls + cnt;
+                for (int a = tb + 1; a < te; a++) {
+                    const int16_t la = ln[a];
+                    const int32_t ka = sid[PID[la]];
+                    int bpos = a - 1;
+                    while (bpos >= tb && sid[PID[ln[bpos]]] > ka) {
+                        ln[bpos + 1] = ln[bpos];
+                        bpos--;
+                    }
+                    ln[bpos + 1] = la;
+                }
+                const int32_t sb = FF[f] >= 0 ? tb : ls;  // a split node settles its tail; a leaf everything
+                for (int p = sb; p < te; p++) {
+                    perm_final[s0 + p] = PID[ln[p]];
+                    pnode[s0 + p] = v;
+                }
+            }
+            __syncwarp();
+            // (d) children: 8 lanes per split node, coalesced; non-empty ones form the next frontier
+            int nn = 0;
+            for (int f0 = 0; f0 < nf; f0 += 4) {
+                const int f = f0 + (lane >> 3), o = lane & 7;
+                const int32_t ff = f < nf ? FF[f] : -1;
+                bool join = false;
+                int32_t c = 0, cs = 0, cc = 0;
+                if (ff >= 0) {
+                    const int32_t v = fnc[f];
+                    const int16_t *hh = FH + 9 * f;
+                    c = ff + o;
+                    cs = o ? hh[o - 1] : fsc[f];
+                    cc = hh[o] - cs;
+                    const double rc = nd.radius[v] / 2;  // Node.cpp:640
+                    nd.start[c] = s0 + cs;
+                    nd.count[c] = cc;
+                    nd.ndrop[c] = 0;
+                    nd.first[c] = -1;
+                    nd.parent[c] = v;
+                    nd.level[c] = (int8_t)(level + 1);
+                    nd.radius[c] = rc;
+                    nd.inst[c] = nd.inst[v];
+                    nd.mode[c] = cc ? MODE_SER : MODE_EMPTY;
+                    nd.needs[c] = 0;
+                    nd.leafpos[c] = -1;
+                    if (cc > 0) {  // child o: centre c + r*(+-0.5) (Node.cpp:630-642)
+                        const double x = __dadd_rn(nd.cx[v], (o & 1) ? rc : -rc);
+                        const double y = __dadd_rn(nd.cy[v], (o & 2) ? rc : -rc);
+                        const double z = __dadd_rn(nd.cz[v], (o & 4) ? rc : -rc);
+                        nd.cx[c] = x;
+                        nd.cy[c] = y;
+                        nd.cz[c] = z;
+                        set_bounds_v(nd, c, x, y, z, rc);
+                        join = true;
+                    }
+                }
+                const unsigned bj = __ballot_sync(full, join);
+                if (join) {
+                    const int q = nn + __popc(bj & lt);
+                    fnn[q] = c;
+                    fsn[q] = (int16_t)cs;
+                    fcn[q] = (int16_t)cc;
+                }
+                nn += __popc(bj);
+            }
+            __syncwarp();
+            if (nn) deepest = max(deepest, level + 1);
+            cur = nxt;
+            nf = nn;
+            level++;
+        }
+    }
+    for (int k = lpool + lane; k < lpool_end; k += 32) leaves[k] = -1;  // the stretches' unused tails
+    for (int k = ipool + lane; k < ipool_end; k += 32) nd.lint[k] = make_int2(-1, 0);
+    if (lane == 0) {
+        if (splits) atomicAdd((unsigned long long *)&ctl->local_splits, (unsigned long long)splits);
+        if (deepest) atomicMax(&ctl->maxlev, deepest);
+    }
 }
 
 // count, min and max mass of each instance's gas particles (order-preserving
@@ -934,7 +1398,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
     G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
     G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(tfirst) G(tfirstm) G(wA) G(wB) G(wD) G(flag)
-    G(rho) G(nlx) G(ilist)
+    G(rho) G(nlx) G(lint) G(lil)
 #undef G
     if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;
     c->node_cap = nc;
@@ -1028,10 +1492,32 @@ static LevelBufs level_bufs(Ctx *c, int w)
     b.nl_next = c->nl[w ^ 1];
     b.leaves = c->leaves;
     b.drop_list = c->drop_list;
+    b.lroots = c->lroots;
+    b.local_ok = false;
     return b;
 }
 
+static int build_tree_once(Ctx *c, bool &local_nomem);
+
+// The pool is sized before each level of the loop; serial subtrees may still
+// need more nodes than estimated, in which case the build is redone with a
+// larger pool (the particle state is untouched until the reorder).
 int build_tree(Ctx *c)
+{
+    for (int attempt = 0;; attempt++) {
+        bool local_nomem = false;
+        const int rc = build_tree_once(c, local_nomem);
+        if (rc == AG2_E_NOMEM && local_nomem && attempt < 4) {
+            c->err.clear();
+            const int g = ensure_node_capacity(c, 2 * c->node_cap);
+            if (g != AG2_OK) return g;
+            continue;
+        }
+        return rc;
+    }
+}
+
+static int build_tree_once(Ctx *c, bool &local_nomem)
 {
     const int n = (int)c->n;
     c->have_tree = false;
@@ -1064,8 +1550,10 @@ int build_tree(Ctx *c)
     if ((rc = ensure_node_capacity(c, (size_t)K + 1024)) != AG2_OK) return rc;
     const int thresh = c->prm.split_threshold;
     AG2_LAUNCH(c, k_ctl_reset, 1, 1, 0, c->ctl, K);
+    // serial subtrees (fewer than split_threshold particles) are built one warp each when they fit
+    const bool local_ok = thresh - 1 <= kLocalCapMax;
     AG2_LAUNCH(c, k_root_init, grid_for(K, kBlock), kBlock, 0, K, c->nd, c->ctl, c->inst_first, c->inst_R, thresh,
-               c->nl[0], c->leaves);
+               c->nl[0], c->leaves, local_ok, c->lroots);
     AG2_LAUNCH(c, k_level0, grid_for(n, kBlock), kBlock, 0, n, c->pinst, c->nd, S.px, S.py, S.pz, level_bufs(c, 0),
                c->ctl);
     c->inst_R_h.resize(K);
@@ -1074,7 +1562,6 @@ int build_tree(Ctx *c)
     c->root_radius = c->inst_R_h[0];
 
     c->level_base.assign({0, (int64_t)K});
-    c->int_off.assign({0});
     int level = 0;
     int nnl = c->ctl_host->next_needs;  // split list of the level
     int nap = c->ctl_host->next_active; // active slots of the level
@@ -1085,7 +1572,8 @@ int build_tree(Ctx *c)
         AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, 9 * (size_t)nnl * sizeof(int32_t), c->stream));
         AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_needs, 0, sizeof(int32_t), c->stream));
         AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_active, 0, sizeof(int32_t), c->stream));
-        const LevelBufs b = level_bufs(c, level & 1);
+        LevelBufs b = level_bufs(c, level & 1);
+        b.local_ok = local_ok;
         AG2_LAUNCH(c, k_digit, grid_for(nap, kBlock), kBlock, 0, nap, b, c->nd);
         AG2_LAUNCH(c, k_nodes, grid_for((size_t)nnl * 8, kBlock), kBlock, 0, nnl, level, thresh,
                    (int64_t)c->node_cap, c->nd, c->ctl, b, (int)AG2_MAX_DEPTH);
@@ -1100,15 +1588,46 @@ int build_tree(Ctx *c)
             return set_err(c, h.err_code, "octree build failed");
         }
         c->level_base.push_back(h.node_count);
-        c->int_off.push_back(h.nint);
         nnl = h.next_needs;
         nap = h.next_active;
         level++;
     }
     phase_mark(c, "build: levels");
-    c->max_level = (int)c->level_base.size() - 2;
-    c->nnodes = c->level_base.back();
-    c->ninternal = (c->nnodes - K) / 8;
+
+    // serial subtrees: one warp each
+    const int nloc = c->ctl_host->nlocal;
+    const int64_t loop_nodes = c->ctl_host->node_count;
+    if (nloc > 0) {
+        const int lcap = std::max(8, ((thresh - 1) + 7) & ~7);
+        const int wpb = (int)std::max<size_t>(1, std::min<size_t>(kLocalWarps, (150u << 10) / local_smem_bytes(lcap)));
+        const size_t smem = (size_t)wpb * local_smem_bytes(lcap);
+        AG2_CUDA(c, cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0, sms = 0;
+        AG2_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local, wpb * 32, smem));
+        AG2_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+        const int blocks = std::max(1, std::min((nloc + wpb - 1) / wpb, std::max(per_sm, 1) * sms));
+        const size_t need = (size_t)loop_nodes + 12 * (size_t)c->ctl_host->nlocal_part +
+                            (size_t)blocks * wpb * kPoolChunk + 1024;
+        if ((rc = ensure_node_capacity(c, need)) != AG2_OK) return rc;
+        AG2_LAUNCH(c, k_local, blocks, wpb * 32, smem, nloc, c->lroots, lcap, c->nd, c->ctl, c->pkey,
+                   (int64_t)c->cap, c->perm_final, c->pnode, S.id, c->leaves, (int64_t)c->leaves_cap,
+                   (int)AG2_MAX_DEPTH, (int64_t)c->node_cap);
+        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        const Ctx::Ctl &h = *c->ctl_host;
+        if (h.err_code) {
+            if (h.err_code == AG2_E_COINCIDENT)
+                return set_err(c, AG2_E_COINCIDENT,
+                               "particles too close to separate within AG2_MAX_DEPTH levels "
+                               "(the reference recurses without end on coincident particles)");
+            if (h.err_code == AG2_E_NOMEM) local_nomem = true;
+            return set_err(c, h.err_code, "octree build failed");
+        }
+        phase_mark(c, "build: serial subtrees");
+    }
+    c->max_level = std::max((int)c->level_base.size() - 2, (int)c->ctl_host->maxlev);
+    c->nnodes = c->ctl_host->node_count;
+    c->nnodes_true = loop_nodes + 8 * (int64_t)c->ctl_host->local_splits;
+    c->ninternal = (c->nnodes_true - K) / 8;
     c->nleaves = c->ctl_host->nleaf;
     if (c->ctl_host->ndrop_nodes > kMaxDropNodes)
         return set_err(c, AG2_E_CAPACITY, "more than 65536 nodes with out-of-bounds particles");
@@ -1124,13 +1643,30 @@ int build_tree(Ctx *c)
     AG2_LAUNCH(c, k_refnode, grid_for(n, kBlock), kBlock, 0, n, c->nd, c->pnode, c->S().id, c->refnode);
     phase_mark(c, "build: reorder");
 
-    // moments: every leaf at once, then the internal nodes level by level, deepest first
+    // moments: every leaf at once, then the internal nodes level by level,
+    // deepest first (the internal-node list bucketed by level)
     AG2_LAUNCH(c, k_moments_leaf, grid_for(c->nleaves, kBlock), kBlock, 0, c->nleaves, c->leaves, c->nd, c->S(),
                c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
-    for (int L = (int)c->int_off.size() - 2; L >= 0; L--) {
-        const int32_t b0 = c->int_off[L], cnt = c->int_off[L + 1] - b0;
-        AG2_LAUNCH(c, k_moments_int, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.ilist + b0, c->nd, c->S(),
-                   c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+    {
+        const int nlint = c->ctl_host->nlint;
+        AG2_LAUNCH(c, k_lvl_hist, grid_for(nlint, kBlock), kBlock, 0, nlint, c->nd.lint, c->ctl->lvl_cnt);
+        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        c->lvl_cnt_h.assign(c->ctl_host->lvl_cnt, c->ctl_host->lvl_cnt + AG2_MAX_DEPTH);
+        c->lvl_start_h.assign(AG2_MAX_DEPTH, 0);
+        int32_t acc = 0;
+        for (int L = 0; L < AG2_MAX_DEPTH; L++) {
+            c->lvl_start_h[L] = acc;
+            acc += c->lvl_cnt_h[L];
+        }
+        AG2_CUDA(c, cudaMemcpyAsync(c->ctl->lvl_off, c->lvl_start_h.data(), AG2_MAX_DEPTH * sizeof(int32_t),
+                                    cudaMemcpyHostToDevice, c->stream));
+        AG2_LAUNCH(c, k_bucket, grid_for(nlint, kBlock), kBlock, 0, nlint, c->nd.lint, c->ctl->lvl_off, c->nd.lil);
+        for (int L = AG2_MAX_DEPTH - 1; L >= 0; L--) {
+            const int32_t cnt = c->lvl_cnt_h[L];
+            if (!cnt) continue;
+            AG2_LAUNCH(c, k_moments_int, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.lil + c->lvl_start_h[L], c->nd,
+                       c->S(), c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+        }
     }
     phase_mark(c, "build: moments");
     c->have_tree = true;

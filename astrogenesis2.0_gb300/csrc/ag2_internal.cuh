@@ -68,7 +68,8 @@ struct Nodes {
     double *rho;
     // build scratch sized by the node pool
     int32_t *nlx;    // index of a node in its level's split list
-    int32_t *ilist;  // internal nodes, one segment per level
+    int2 *lint;      // internal nodes with their level (padding: node -1)
+    int32_t *lil;    // the same, one segment per level, deepest last
 };
 
 struct Ctx {
@@ -101,9 +102,12 @@ struct Ctx {
     int32_t *perm_final = nullptr;
     int32_t *ap[2] = {};          // active slots of a level (compact list)
     int32_t *nl[2] = {};          // split list of a level (node ids)
-    int32_t *leaves = nullptr;    // every non-empty leaf
+    int32_t *leaves = nullptr;    // every non-empty leaf (-1 entries are padding)
+    size_t leaves_cap = 0;
+    int32_t *lroots = nullptr;    // roots of serial subtrees built by one warp each
     int64_t *pkey = nullptr;      // 2 buffers x 3 coordinates x cap ordered keys
-    std::vector<int32_t> int_off; // internal-node list: first entry of each level
+    int64_t nnodes_true = 0;      // nodes of the tree (nnodes also counts unused pool tails)
+    std::vector<int32_t> lvl_cnt_h, lvl_start_h;  // internal nodes per level and their list segments
     int32_t nleaves = 0;
     int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
     int32_t *refnode = nullptr;   // the reference's Particle::node per slot (-1 = null)
@@ -174,8 +178,14 @@ struct Ctx {
         int32_t ndrop_nodes;
         int32_t next_active;    // active slots at the next level
         int32_t nleaf;          // entries of the leaf list
-        int32_t nint;           // entries of the internal-node list
+        int32_t nlocal;         // serial subtree roots for k_local
+        int32_t nlint;          // entries of the internal-node list
+        int32_t lvl_cnt[AG2_MAX_DEPTH];  // internal nodes per level
+        int32_t lvl_off[AG2_MAX_DEPTH];  // bucketing cursors
+        int32_t maxlev;         // deepest level of the serial subtrees
+        int32_t nlocal_part;    // particles in serial subtrees
         int32_t pad_;
+        unsigned long long local_splits;  // split nodes of the serial subtrees
     };
     Ctl *ctl = nullptr;      // device
     Ctl *ctl_host = nullptr; // pinned mirror
@@ -213,6 +223,10 @@ __host__ __device__ inline int64_t okey(double x)
 #endif
     return b >= 0 ? (int64_t)b : (int64_t)(b ^ 0x7FFFFFFFFFFFFFFFLL);
 }
+
+// entries of the leaf list beyond one per particle: the unused tails of the
+// build's per-warp stretches
+constexpr size_t kLeafListSpare = size_t(1) << 22;
 
 // status helpers
 int set_err(Ctx *c, int code, const std::string &msg);

@@ -55,6 +55,10 @@ def check_topology(t, ref, uniform_gas, exact_fp=False):
         assert np.array_equal(t[k], ref[k]), k
     if uniform_gas:
         assert np.array_equal(t["gas_mass"], ref["gas_mass"])
+    # a leaf's centre of mass is the reference's one-insertion running mean,
+    # (0*(m-m) + x*m)/m, or the position itself: bit-exact
+    leaf = (t["is_leaf"] == 1) & (t["particle"] >= 0) & (ref["mass"] > 0)
+    assert np.array_equal(t["com"][leaf], ref["com"][leaf])
     scale = np.max(np.abs(ref["center"])) + ref["radius"][0]
     for k in ("mass", "gas_mass", "mvel", "com"):
         s = scale if k == "com" else max(np.max(np.abs(ref[k])), 1e-300)
