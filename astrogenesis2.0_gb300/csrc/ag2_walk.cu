@@ -473,15 +473,19 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         }
         asm volatile("" : "+f"(hi_), "+f"(pr), "+f"(cs), "+f"(vxi), "+f"(vyi), "+f"(vzi));
         const float h2x4 = 4.0f * hi_ * hi_;
-        // group bounding sphere (radius about the group centre, with slack for
+        // group bounding box (half-extents about the group centre, with slack for
         // rounding) and the largest SPH reach of its gas lanes
-        float Rg = valid ? sqrtf(ox * ox + oy * oy + oz * oz) : 0.f;
+        float hbx = valid ? fabsf(ox) : 0.f, hby = valid ? fabsf(oy) : 0.f, hbz = valid ? fabsf(oz) : 0.f;
         float gas_reach2 = (kGas && gas_i && valid) ? h2x4 : 0.f;
         for (int o = 16; o > 0; o >>= 1) {
-            Rg = fmaxf(Rg, __shfl_xor_sync(0xffffffffu, Rg, o));
+            hbx = fmaxf(hbx, __shfl_xor_sync(0xffffffffu, hbx, o));
+            hby = fmaxf(hby, __shfl_xor_sync(0xffffffffu, hby, o));
+            hbz = fmaxf(hbz, __shfl_xor_sync(0xffffffffu, hbz, o));
             gas_reach2 = fmaxf(gas_reach2, __shfl_xor_sync(0xffffffffu, gas_reach2, o));
         }
-        Rg = Rg * (1.0f + 1e-6f) + 1e-30f;
+        hbx = hbx * (1.0f + 1e-6f) + 1e-30f;
+        hby = hby * (1.0f + 1e-6f) + 1e-30f;
+        hbz = hbz * (1.0f + 1e-6f) + 1e-30f;
         float sx = 0, sy = 0, sz = 0, kx = 0, ky = 0, kz = 0;  // Kahan sums
         Vec3<float> side = {0, 0, 0};  // SPH and FP64-path contributions
         float du = 0;
@@ -548,27 +552,30 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 W.cfirst[lane] = f;
                 W.ccm[lane] = ccm;
                 if (kGas) W.cgas[lane] = D;
-                // Every lane's distance lies in [dc - Rg, dc + Rg].  When the whole
-                // interval is clear of the opening threshold (outside the guard
-                // band) and of the near-zero and SPH cases, all lanes decide alike
-                // and no per-lane test is needed.  NaN centres fall through.
+                // Every lane's squared distance lies in [lo2, hi2], the nearest and
+                // farthest points of the group's box.  When the whole interval is
+                // clear of the opening threshold (outside the guard band) and of
+                // the near-zero and SPH cases, all lanes decide alike and no
+                // per-lane test is needed.  NaN centres fall through.
                 unsigned selfm = 0u;
                 if (B.w < 0.0f) {
                     const int lp = a.leafpos[c] - gd.x;
                     if (lp >= 0 && lp < 32) selfm = 1u << lp;
                 }
                 W.cself[lane] = selfm;
-                const float dc = sqrtf(cx * cx + cy * cy + cz * cz);
-                const float lo = dc - Rg, hi = dc + Rg;
+                const float ax_ = fabsf(cx), ay_ = fabsf(cy), az_ = fabsf(cz);
+                const float nx = fmaxf(ax_ - hbx, 0.f), ny = fmaxf(ay_ - hby, 0.f), nz = fmaxf(az_ - hbz, 0.f);
+                const float fx = ax_ + hbx, fy = ay_ + hby, fz = az_ + hbz;
+                const float lo2 = fmaf(nx, nx, fmaf(ny, ny, nz * nz)), hi2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
                 const float mac = B.w;
                 unsigned char cls = 0;
-                const bool no_sph = !kGas || !(D.w > 0.0f) || lo * lo > gas_reach2;
+                const bool no_sph = !kGas || !(D.w > 0.0f) || lo2 > gas_reach2;
                 if (mac >= 0.0f) {
-                    if (lo > 0.0f && hi * hi < mac * (1.0f - 4.0f * kGuard))
+                    if (lo2 > 0.0f && hi2 < mac * (1.0f - 4.0f * kGuard))
                         cls = 1;
-                    else if (lo > 0.0f && lo * lo > mac * (1.0f + 4.0f * kGuard) && no_sph)
+                    else if (lo2 > mac * (1.0f + 4.0f * kGuard) && no_sph)
                         cls = 2;
-                } else if (lo > 0.0f && lo * lo > 4e-12f * eps02 && no_sph) {
+                } else if (lo2 > 4e-12f * eps02 && no_sph) {
                     cls = 2;
                 }
                 W.ccls[lane] = cls;
