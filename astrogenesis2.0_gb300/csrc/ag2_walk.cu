@@ -322,12 +322,28 @@ struct alignas(16) WarpSmem {
     unsigned char ccm[kBatch];  // child mask of the child
     unsigned char ccls[kBatch]; // group-level class: 0 per-lane, 1 every lane opens, 2 every lane accepts
     unsigned cself[kBatch];     // lane whose own leaf this child is (bit), else 0
+    unsigned char mq[kBatch];   // batch slot of the q-th child the lanes decide one by one
     float4 lpos[kList];      // accepted nodes: relative com, mass
     unsigned lmask[kList];   // lanes that accepted them
     double xd[3][32];        // FP64 positions of the group (read only by the exact re-check)
     int2 stk[kStack];        // (first child of a node to open, lane mask)
     unsigned char stkcm[kStack];
 };
+
+// 32 x 32 bit transpose across the warp: lane i holds row i (bit j = column
+// j); afterwards lane j holds column j (bit i = row i).  Five butterfly stages
+// swap the off-diagonal blocks of halving size.
+__device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
+{
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const unsigned m = s == 16 ? 0x0000ffffu : s == 8 ? 0x00ff00ffu : s == 4 ? 0x0f0f0f0fu : s == 2 ? 0x33333333u
+                                                                                                  : 0x55555555u;
+        const unsigned y = __shfl_xor_sync(0xffffffffu, x, s);
+        x = (lane & s) ? ((x & ~m) | ((y & ~m) >> s)) : ((x & m) | ((y & m) << s));
+    }
+    return x;
+}
 
 // Force loop over the interaction list: every lane evaluates every entry and
 // keeps it when its bit is set (predicated, no branches), summing into a batch
@@ -612,50 +628,68 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 nl += __popc(am);
             }
             __syncwarp();
+            // children the lanes decide one by one: every lane decides all of them
+            // (bit q of its masks for the q-th), then a transpose gives lane q the
+            // lanes that accept / open that child, and the entries are placed at once
+            if (mixed) {
+                unsigned accb = 0u, opnb = 0u;
+                int q = 0;
 #pragma unroll 1
-            while (mixed) {
-                const int j = __ffs(mixed) - 1;
-                mixed &= mixed - 1u;
-                const int c = W.bchild[j];
-                const unsigned bm = W.bmask[j];
-                const bool in = (bm >> lane) & 1u;
-                int decision = 0;  // 0 skip, 1 accept (FP32 list), 2 open, 3 done in FP64
-                const float4 Pc = W.cpos[j];
-                if (in && c != myleaf) {
-                    const float mac = W.cmac[j];
-                    const bool leaf = mac < 0.0f;
-                    const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
-                    if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
-                        decision = recheck_fp64<kGeneral>(a, c, leaf, W.xd, lane, r2 <= tiny, side, cnt_g);
-                    else
-                        decision = (leaf || r2 > mac) ? 1 : 2;
-                    if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) {
-                        const float4 D = W.cgas[j];
-                        if (D.w > 0.0f) {
-                            const float r = sqrtf(r2);
-                            sph_pair<float>(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs, side,
-                                            du);
-                            cnt_s++;
+                for (unsigned mm = mixed; mm; mm &= mm - 1u, q++) {
+                    const int j = __ffs(mm) - 1;
+                    const int c = W.bchild[j];
+                    const bool in = (W.bmask[j] >> lane) & 1u;
+                    int decision = 0;  // 0 skip, 1 accept (FP32 list), 2 open, 3 done in FP64
+                    if (in && c != myleaf) {
+                        const float4 Pc = W.cpos[j];
+                        const float mac = W.cmac[j];
+                        const bool leaf = mac < 0.0f;
+                        const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
+                        if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
+                            decision = recheck_fp64<kGeneral>(a, c, leaf, W.xd, lane, r2 <= tiny, side, cnt_g);
+                        else
+                            decision = (leaf || r2 > mac) ? 1 : 2;
+                        if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) {
+                            const float4 D = W.cgas[j];
+                            if (D.w > 0.0f) {
+                                const float r = sqrtf(r2);
+                                sph_pair<float>(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs,
+                                                side, du);
+                                cnt_s++;
+                            }
                         }
                     }
+                    accb |= (decision == 1 ? 1u : 0u) << q;
+                    opnb |= (decision == 2 ? 1u : 0u) << q;
                 }
-                const unsigned am = __ballot_sync(0xffffffffu, decision == 1);
-                const unsigned om = __ballot_sync(0xffffffffu, decision == 2);
-                if (om && sp >= kStack) overflow = true;
-                if (lane == 0) {
-                    if (am) {
-                        W.lpos[nl] = Pc;
-                        W.lmask[nl] = am;
-                    }
-                    if (om && sp < kStack) {
-                        W.stk[sp] = make_int2(W.cfirst[j], (int)om);
-                        W.stkcm[sp] = W.ccm[j];
-                    }
+                const unsigned below = (1u << lane) - 1u;
+                if ((mixed >> lane) & 1u) W.mq[__popc(mixed & below)] = (unsigned char)lane;
+                accb = transpose32(accb, lane);
+                opnb = transpose32(opnb, lane);
+                __syncwarp();
+                const int nm = __popc(mixed);
+                const int jq = lane < nm ? (int)W.mq[lane] : 0;
+                const bool ha = lane < nm && accb != 0u, ho = lane < nm && opnb != 0u;
+                const unsigned hab = __ballot_sync(0xffffffffu, ha), hob = __ballot_sync(0xffffffffu, ho);
+                if (ha) {
+                    const int p = nl + __popc(hab & below);
+                    W.lpos[p] = W.cpos[jq];
+                    W.lmask[p] = accb;
                 }
-                nl += am ? 1 : 0;
-                sp += (om && sp < kStack) ? 1 : 0;
+                nl += __popc(hab);
+                const int nop = __popc(hob);
+                if (sp + nop > kStack) {
+                    overflow = true;
+                } else {
+                    if (ho) {
+                        const int p = sp + __popc(hob & below);
+                        W.stk[p] = make_int2(W.cfirst[jq], (int)opnb);
+                        W.stkcm[p] = W.ccm[jq];
+                    }
+                    sp += nop;
+                }
             }
             __syncwarp();
             if (overflow) break;
