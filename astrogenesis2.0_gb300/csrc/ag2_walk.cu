@@ -316,6 +316,7 @@ struct alignas(16) WarpSmem {
     float4 cpos[kBatch];     // com - group centre (lane-invariant part), mass
     float4 cgas[kBatch];     // gas velocity, gasMass
     float cmac[kBatch];      // (radius/theta)^2, or -1 for a leaf
+    float4 cthr[kBatch];     // per-lane test thresholds on r^2: open above .y and below .z, accept above .w
     int cfirst[kBatch];      // first child of the child (-1 leaf)
     int bchild[kBatch];      // node index of batch slot j
     unsigned bmask[kBatch];  // lanes that evaluate batch slot j
@@ -565,6 +566,14 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                             cz = (A.z - ghz) + (B.z - glz);
                 W.cpos[lane] = make_float4(cx, cy, cz, A.w);
                 W.cmac[lane] = B.w;
+                {
+                    // r^2 at or below `tiny`, or within the guard band around the
+                    // opening threshold, is decided exactly in FP64 (recheck_fp64)
+                    const float m = B.w;
+                    const float tiny = m < 0.0f ? 1e-12f * eps02 : 1e-10f * m;
+                    W.cthr[lane] = m < 0.0f ? make_float4(m, tiny, -1.0f, tiny)
+                                            : make_float4(m, tiny, m - kGuard * m, m + kGuard * m);
+                }
                 W.cfirst[lane] = f;
                 W.ccm[lane] = ccm;
                 if (kGas) W.cgas[lane] = D;
@@ -632,44 +641,64 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             // (bit q of its masks for the q-th), then a transpose gives lane q the
             // lanes that accept / open that child, and the entries are placed at once
             if (mixed) {
-                unsigned accb = 0u, opnb = 0u;
-                int q = 0;
+                const unsigned below = (1u << lane) - 1u;
+                if ((mixed >> lane) & 1u) W.mq[__popc(mixed & below)] = (unsigned char)lane;
+                __syncwarp();
+                const int nm = __popc(mixed);
+                unsigned accb = 0u, opnb = 0u, sphb = 0u, rqb = 0u;
+#pragma unroll 2
+                for (int q = 0; q < nm; q++) {
+                    const int j = W.mq[q];
+                    // the lanes that evaluate this child, except the one whose own leaf it is
+                    const bool in = ((W.bmask[j] & ~W.cself[j]) >> lane) & 1u;
+                    if (in) {
+                        const float4 Pc = W.cpos[j];
+                        const float4 T = W.cthr[j];
+                        const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const bool acc = r2 > T.w, opn = r2 > T.y && r2 < T.z;
+                        accb |= (acc ? 1u : 0u) << q;
+                        opnb |= (opn ? 1u : 0u) << q;
+                        rqb |= (acc || opn ? 0u : 1u) << q;
+                        if (kGas && gas_i && acc && r2 < h2x4) sphb |= 1u << q;
+                    }
+                }
+                // the rare tests decided in FP64 (near zero distance, or the guard band)
+                if (__any_sync(0xffffffffu, rqb != 0u)) {
 #pragma unroll 1
-                for (unsigned mm = mixed; mm; mm &= mm - 1u, q++) {
-                    const int j = __ffs(mm) - 1;
-                    const int c = W.bchild[j];
-                    const bool in = (W.bmask[j] >> lane) & 1u;
-                    int decision = 0;  // 0 skip, 1 accept (FP32 list), 2 open, 3 done in FP64
-                    if (in && c != myleaf) {
+                    for (unsigned bq = rqb; bq; bq &= bq - 1u) {
+                        const int q = __ffs(bq) - 1, j = W.mq[q];
                         const float4 Pc = W.cpos[j];
                         const float mac = W.cmac[j];
                         const bool leaf = mac < 0.0f;
                         const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
                         const float r2 = dx * dx + dy * dy + dz * dz;
                         const float tiny = leaf ? 1e-12f * eps02 : 1e-10f * mac;
-                        if (r2 <= tiny || (!leaf && fabsf(r2 - mac) <= kGuard * mac))
-                            decision = recheck_fp64<kGeneral>(a, c, leaf, W.xd, lane, r2 <= tiny, side, cnt_g);
-                        else
-                            decision = (leaf || r2 > mac) ? 1 : 2;
-                        if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) {
-                            const float4 D = W.cgas[j];
-                            if (D.w > 0.0f) {
-                                const float r = sqrtf(r2);
-                                sph_pair<float>(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs,
-                                                side, du);
-                                cnt_s++;
-                            }
+                        const int decision = recheck_fp64<kGeneral>(a, W.bchild[j], leaf, W.xd, lane, r2 <= tiny, side,
+                                                                    cnt_g);  // 0 skip, 1 accept, 2 open, 3 done
+                        accb |= (decision == 1 ? 1u : 0u) << q;
+                        opnb |= (decision == 2 ? 1u : 0u) << q;
+                        if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) sphb |= 1u << q;
+                    }
+                }
+                // SPH pairs of the gas lanes (rare): a separate pass keeps the loop above small
+                if (kGas && __any_sync(0xffffffffu, sphb != 0u)) {
+#pragma unroll 1
+                    for (unsigned bq = sphb; bq; bq &= bq - 1u) {
+                        const int j = W.mq[__ffs(bq) - 1];
+                        const float4 D = W.cgas[j];
+                        if (D.w > 0.0f) {
+                            const float4 Pc = W.cpos[j];
+                            const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
+                            const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+                            sph_pair<float>(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs, side,
+                                            du);
+                            cnt_s++;
                         }
                     }
-                    accb |= (decision == 1 ? 1u : 0u) << q;
-                    opnb |= (decision == 2 ? 1u : 0u) << q;
                 }
-                const unsigned below = (1u << lane) - 1u;
-                if ((mixed >> lane) & 1u) W.mq[__popc(mixed & below)] = (unsigned char)lane;
                 accb = transpose32(accb, lane);
                 opnb = transpose32(opnb, lane);
-                __syncwarp();
-                const int nm = __popc(mixed);
                 const int jq = lane < nm ? (int)W.mq[lane] : 0;
                 const bool ha = lane < nm && accb != 0u, ho = lane < nm && opnb != 0u;
                 const unsigned hab = __ballot_sync(0xffffffffu, ha), hob = __ballot_sync(0xffffffffu, ho);
