@@ -33,7 +33,7 @@ EXPORTS = [
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
     "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
-    "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius",
+    "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy",
 ]
 
 
@@ -93,6 +93,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_interactions.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.ag2_direct_sum.argtypes = [P, ctypes.c_size_t, P, P]
     L.ag2_diagnostics.argtypes = [P, P]
+    L.ag2_energy.argtypes = [P, P]
     L.ag2_fp32_peak_probe.argtypes = [P, dp]
     L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.ag2_root_radius_noalloc.argtypes = [P, ctypes.c_int64, P, P]
@@ -258,6 +259,13 @@ class Context:
         out = np.empty(8)
         self._check(self.L.ag2_diagnostics(self.h, _ptr(out)))
         return {"mass": out[0], "ekin": out[1], "momentum": out[2:5], "angmom": out[5:8]}
+
+    def energy(self) -> dict:
+        """Kinetic, potential, thermal and total energy of the current state
+        (needs a tree built from the current positions)."""
+        out = np.empty(4)
+        self._check(self.L.ag2_energy(self.h, _ptr(out)))
+        return {"kinetic": out[0], "potential": out[1], "thermal": out[2], "total": out[3]}
 
     def fp32_peak_gflops(self) -> float:
         g = ctypes.c_double()

@@ -661,6 +661,12 @@ int ag2_diagnostics(ag2_ctx *c, double *out8)
     return run_diagnostics(c, out8);
 }
 
+int ag2_energy(ag2_ctx *c, double *out4)
+{
+    if (!c || !out4) return AG2_E_INVALID;
+    return run_energy(c, out4);
+}
+
 int ag2_fp32_peak_probe(ag2_ctx *c, double *gflops)
 {
     if (!c || !gflops) return AG2_E_INVALID;

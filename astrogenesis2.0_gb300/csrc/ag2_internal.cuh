@@ -269,6 +269,7 @@ int run_scale(Ctx *c, double f);
 int sync_ctl(Ctx *c);  // copy ctl to host (synchronises the stream)
 int run_direct_sum(Ctx *c, size_t ns, const int64_t *ids_host, double *out_host);
 int run_diagnostics(Ctx *c, double *out8);
+int run_energy(Ctx *c, double *out4);
 int run_fma_probe(Ctx *c, double *gflops);
 int run_autotune(Ctx *c, int *chosen);
 

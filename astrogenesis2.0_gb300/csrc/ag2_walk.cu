@@ -754,6 +754,114 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
     }
 }
 
+// Potential of every particle for the energy check, FP64, with the FP64
+// walk's traversal and opening rule: phi_i = sum over accepted nodes and
+// particles of -(G m / e0) atan(e0 / r), the potential of the pair force
+// G m / (r^2 + e0^2) along d/r (Node.cpp:285-305 for e0 < 0.6).
+__global__ void __launch_bounds__(kWalkBlock) k_potential(WalkArgs a, double *phi)
+{
+    __shared__ int2 stk_all[(kWalkBlock / 32) * kStack];
+    const int lane = threadIdx.x & 31;
+    int2 *stk = stk_all + (threadIdx.x >> 5) * kStack;
+    const double e0 = a.e0;
+    for (;;) {
+        int grp = 0;
+        if (lane == 0) grp = atomicAdd(&a.ctl->list_count, 1);
+        grp = __shfl_sync(0xffffffffu, grp, 0);
+        if (grp >= a.ngroups) break;
+        const int4 gd = a.groups[grp];
+        const int i = gd.x + lane;
+        const bool live = lane < gd.y;
+        const bool valid = live && a.m[i] != 0.0;
+        double xi = 0, yi = 0, zi = 0;
+        int myleaf = -1;
+        if (live) {
+            xi = a.px[i];
+            yi = a.py[i];
+            zi = a.pz[i];
+            const int pn = a.pnode[i];
+            myleaf = (pn >= 0 && a.leafpos[pn] == i) ? pn : -1;
+        }
+        double p = 0.0;
+        const unsigned all = __ballot_sync(0xffffffffu, valid);
+        int sp = 0;
+        bool overflow = false;
+        if (all && a.mass[gd.z] != 0.0) {
+            stk[0] = make_int2(gd.z, (int)all);
+            sp = 1;
+        }
+        __syncwarp();
+        while (sp > 0) {
+            sp--;
+            const int2 e = stk[sp];
+            __syncwarp();
+            const int c = e.x;
+            const bool in = ((unsigned)e.y >> lane) & 1u;
+            bool open = false;
+            const int32_t fc = a.first[c];
+            const bool leaf = fc < 0;
+            if (in && !(leaf && c == myleaf)) {
+                const double dx = a.comx[c] - xi, dy = a.comy[c] - yi, dz = a.comz[c] - zi;
+                const double r = sqrt(dx * dx + dy * dy + dz * dz);
+                if (r != 0.0) {
+                    if (leaf || a.radius[c] / r < a.theta) {
+                        const double t = -(a.G * a.mass[c] / e0) * atan(e0 / r);
+                        if (!isnan(t)) p += t;
+                    } else {
+                        open = true;
+                    }
+                }
+            }
+            const unsigned om = __ballot_sync(0xffffffffu, open);
+            if (om) {
+                const unsigned cm = a.childmask[c];
+                if (sp + __popc(cm) > kStack) {
+                    overflow = true;
+                    break;
+                }
+                for (int o = 7; o >= 0; o--)
+                    if ((cm >> o) & 1u) {
+                        if (lane == 0) stk[sp] = make_int2(fc + o, (int)om);
+                        sp++;
+                    }
+            }
+            __syncwarp();
+        }
+        if (overflow && lane == 0) {
+            atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
+            atomicExch(&a.ctl->err_info, grp);
+        }
+        if (live) phi[i] = valid ? p : 0.0;
+        __syncwarp();
+    }
+}
+
+// per-block sums of m v^2 / 2, m phi / 2 and (gas) m U, in a fixed order
+__global__ void __launch_bounds__(256) k_energy_sums(int n, const double *m, const double *vx, const double *vy,
+                                                    const double *vz, const double *phi, const double *U,
+                                                    const uint8_t *type, double *part)
+{
+    __shared__ double sh[3][256];
+    double k = 0, w = 0, u = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double mi = m[i];
+        k += 0.5 * mi * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        w += 0.5 * mi * phi[i];
+        if (type[i] == 2) u += mi * U[i];
+    }
+    sh[0][threadIdx.x] = k;
+    sh[1][threadIdx.x] = w;
+    sh[2][threadIdx.x] = u;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 3; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; q++) part[3 * blockIdx.x + q] = sh[q][0];
+}
+
 __global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double *radius, float4 *wB, double theta)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -765,15 +873,8 @@ __global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double 
 
 }  // namespace
 
-int run_forces(Ctx *c)
+static WalkArgs walk_args(Ctx *c)
 {
-    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_forces needs a tree (call ag2_build_tree)");
-    if (c->n == 0) return AG2_OK;
-    if (c->prm.theta != c->tree_theta) {
-        AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.radius,
-                   c->nd.wB, c->prm.theta);
-        c->tree_theta = c->prm.theta;
-    }
     Particles &S = c->S();
     WalkArgs a;
     a.n = (int)c->n;
@@ -794,6 +895,50 @@ int run_forces(Ctx *c)
     a.e0 = c->prm.e0;
     a.G = c->prm.G;
     a.ctl = c->ctl;
+    return a;
+}
+
+int run_energy(Ctx *c, double *out4)
+{
+    for (int k = 0; k < 4; k++) out4[k] = 0.0;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_energy needs a tree of the current positions");
+    if (!(c->prm.e0 > 0.0 && c->prm.e0 < 0.6))
+        return set_err(c, AG2_E_INVALID, "ag2_energy needs 0 < e0 < 0.6 (the softening law's Plummer form)");
+    const int n = (int)c->n;
+    if (n == 0) return AG2_OK;
+    Particles &S = c->S();
+    WalkArgs a = walk_args(c);
+    double *phi = c->staging;        // n doubles
+    double *part = c->staging + n;   // 3 per block (the staging area holds 6 doubles per particle)
+    const int eb = (int)std::max<int64_t>(1, std::min<int64_t>(256, (6 * (int64_t)c->cap - n) / 3));
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int blocks = std::min((c->ngroups + 3) / 4, sms * 16);
+    AG2_LAUNCH(c, k_potential, std::max(blocks, 1), kWalkBlock, 0, a, phi);
+    AG2_LAUNCH(c, k_energy_sums, eb, 256, 0, n, S.m, S.vx, S.vy, S.vz, phi, S.U, S.type, part);
+    std::vector<double> h(3 * eb);
+    AG2_CUDA(c, cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    int rc = sync_ctl(c);
+    if (rc) return rc;
+    if (c->ctl_host->err_code) return set_err(c, c->ctl_host->err_code, "potential walk failed");
+    for (int b = 0; b < eb; b++)
+        for (int q = 0; q < 3; q++) out4[q] += h[3 * b + q];
+    out4[3] = out4[0] + out4[1] + out4[2];
+    return AG2_OK;
+}
+
+int run_forces(Ctx *c)
+{
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_forces needs a tree (call ag2_build_tree)");
+    if (c->n == 0) return AG2_OK;
+    if (c->prm.theta != c->tree_theta) {
+        AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.radius,
+                   c->nd.wB, c->prm.theta);
+        c->tree_theta = c->prm.theta;
+    }
+    WalkArgs a = walk_args(c);
     // The softening law reduces to Plummer softening with e0 whenever the
     // truncated |e| of Node.cpp:302 is 0 for every distance, i.e. e0 < 0.66.
     const bool general = !(c->prm.e0 > 0.0 && c->prm.e0 < 0.6);

@@ -345,6 +345,17 @@ def our_arm(args, wl, d):
     achieved = flop_per_walk / walk_avg_s / 1e12
     peak = ctx.fp32_peak_gflops() / 1e3
 
+    # energy drift of the FP32 form over --drift-steps further steps (untimed)
+    drift = None
+    if args.drift_steps > 0 and 0.0 < wl["e0"] < 0.6:
+        e_a = ctx.energy()
+        for _ in range(args.drift_steps):
+            step()
+        e_b = ctx.energy()
+        drift = {"steps": args.drift_steps, "dt": dt, "start": e_a, "end": e_b,
+                 "relative": (e_b["total"] - e_a["total"]) / abs(e_a["total"]),
+                 "potential_from": "FP64 tree walk of the pair force's potential -(G m/e0) atan(e0/r)"}
+
     # plain FP64 walk on the same workload (the reference's arithmetic on the GPU)
     plain = None
     if args.plain_steps > 0:
@@ -461,6 +472,7 @@ def our_arm(args, wl, d):
             "plain_fp64": {"value": plain, "unit": UNIT, "steps": args.plain_steps} if plain else None,
             "speedup_vs_plain": value / plain if plain else None,
             "force_error": force_error,
+            "energy_drift": drift,
         }
         if per_launch:
             out["one_sim_per_launch"] = per_launch
@@ -695,6 +707,7 @@ def main():
     ap.add_argument("--cpu-walk-fraction", type=int, default=8)
     ap.add_argument("--ref-walk-fraction", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rates", default="10,50,200")
     args = ap.parse_args()

@@ -178,6 +178,15 @@ int ag2_interactions(ag2_ctx *ctx, int64_t *gravity, int64_t *sph);
 int ag2_direct_sum(ag2_ctx *ctx, size_t ns, const int64_t *ids, double *out);
 /* out[0..7] = total mass, kinetic energy, momentum xyz, angular momentum xyz. */
 int ag2_diagnostics(ag2_ctx *ctx, double *out8);
+/* Energy of the current state: out[0] kinetic sum m v^2 / 2, out[1] potential
+ * sum m phi / 2, out[2] thermal sum over gas of m U, out[3] their total.  phi
+ * is the potential of the walk's own pair force G m / (r^2 + e0^2) along d/r
+ * (Node.cpp:285-305 with e0 < 0.6), -(G m / e0) atan(e0 / r), summed over the
+ * nodes and particles the FP64 walk accepts (the same opening rule, FP64).
+ * Needs a tree built from the current positions (after ag2_build_tree or
+ * ag2_step); AG2_E_INVALID for e0 outside (0, 0.6).  No counterpart in the
+ * reference, which computes no potential; this is the energy-drift check. */
+int ag2_energy(ag2_ctx *ctx, double *out4);
 /* FP32 FMA throughput of this GPU in GFLOP/s (roofline denominator of the walk). */
 int ag2_fp32_peak_probe(ag2_ctx *ctx, double *gflops);
 /* Allocation-free root half-width.  No counterpart in the reference: it computes
