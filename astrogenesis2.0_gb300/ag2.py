@@ -33,7 +33,7 @@ EXPORTS = [
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
     "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
-    "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy",
+    "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy", "ag2_step_graphs",
 ]
 
 
@@ -94,6 +94,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_direct_sum.argtypes = [P, ctypes.c_size_t, P, P]
     L.ag2_diagnostics.argtypes = [P, P]
     L.ag2_energy.argtypes = [P, P]
+    L.ag2_step_graphs.argtypes = [P, I]
     L.ag2_fp32_peak_probe.argtypes = [P, dp]
     L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.ag2_root_radius_noalloc.argtypes = [P, ctypes.c_int64, P, P]
@@ -259,6 +260,10 @@ class Context:
         out = np.empty(8)
         self._check(self.L.ag2_diagnostics(self.h, _ptr(out)))
         return {"mass": out[0], "ekin": out[1], "momentum": out[2:5], "angmom": out[5:8]}
+
+    def step_graphs(self, enable: bool = True):
+        """Run later steps as replays of a captured CUDA graph."""
+        self._check(self.L.ag2_step_graphs(self.h, 1 if enable else 0))
 
     def energy(self) -> dict:
         """Kinetic, potential, thermal and total energy of the current state

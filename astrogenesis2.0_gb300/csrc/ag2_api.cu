@@ -206,6 +206,7 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
     c->n_inst = 1;
     c->inst_dirty = true;
     c->inst_explicit = false;
+    c->graph_epoch++;
     int rc = sync_ctl(c);
     if (rc) return rc;
     if (c->ctl_host->err_code == AG2_E_NAN) return set_err(c, AG2_E_NAN, "non-finite particle position");
@@ -335,6 +336,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     if (!c) return AG2_E_NOMEM;
     c->prm = *params;
     cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     if (const char *dbg = std::getenv("AG2_DEBUG_SYNC")) c->debug_sync = dbg[0] == '1';
     size_t cap = std::max(capacity, (size_t)1);
     c->cap = cap;
@@ -389,6 +391,10 @@ int ag2_destroy(ag2_ctx *c)
                   c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    if (c->inst_R_pin) cudaFreeHost(c->inst_R_pin);
+    for (auto &x : c->step_exec)
+        if (x) cudaGraphExecDestroy(x);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -403,6 +409,7 @@ int ag2_set_params(ag2_ctx *c, const ag2_params *p)
     c->prm = *p;
     if (retree) c->have_tree = false;
     if (c->n_inst == 1 && !c->inst_explicit) c->inst_massInH_h = {p->massInH};
+    c->graph_epoch++;
     return AG2_OK;
 }
 
@@ -417,6 +424,7 @@ int ag2_set_stream(ag2_ctx *c, void *stream)
 {
     if (!c) return AG2_E_INVALID;
     c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    c->graph_epoch++;
     return AG2_OK;
 }
 
@@ -472,6 +480,7 @@ int ag2_set_field(ag2_ctx *c, int f, const double *src, int src_is_device)
     AG2_LAUNCH(c, k_scatter_in, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), f, in);
     if (f == AG2_POS || f == AG2_MASS) c->have_tree = false;
     if (f == AG2_MASS) c->gas_stats_dirty = true;
+    c->graph_epoch++;
     return AG2_OK;
 }
 
@@ -538,9 +547,155 @@ int ag2_kick_drift(ag2_ctx *c, double dt) { return c ? run_kick_drift(c, dt) : A
 int ag2_ueuler(ag2_ctx *c, double dt) { return c ? run_ueuler(c, dt) : AG2_E_INVALID; }
 int ag2_scale_positions(ag2_ctx *c, double f) { return c ? run_scale(c, f) : AG2_E_INVALID; }
 
+// ---- step graphs -------------------------------------------------------------
+
+static unsigned long long fnv(unsigned long long h, const void *p, size_t n)
+{
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
+// everything a captured step bakes in: sizes, pointers of every pool, parameters
+static unsigned long long step_key(Ctx *c, double dt, double hubble, int with_visual, double Rv)
+{
+    unsigned long long h = 1469598103934665603ull;
+    const void *ptrs[] = {c->nd.start, c->nd.bkey, c->nd.wA, c->nd.lint, c->hist, c->stream, c->gas_prefix,
+                          c->groups, c->inst_first, c->leaves, c->pkey};
+    h = fnv(h, ptrs, sizeof(ptrs));
+    const int64_t sizes[] = {(int64_t)c->n, c->n_inst, (int64_t)c->node_cap, (int64_t)c->hist_cap, c->ngas,
+                             c->walk_variant, c->ngroups, with_visual, c->graph_epoch};
+    h = fnv(h, sizes, sizeof(sizes));
+    h = fnv(h, &c->prm, sizeof(c->prm));
+    const double d[] = {dt, hubble, Rv};
+    return fnv(h, d, sizeof(d));
+}
+
+static int capture_step(Ctx *c, double dt, double hubble, int with_visual, double Rv, cudaGraphExec_t *exec,
+                        int64_t *nlaunch)
+{
+    const int64_t l0 = c->launches;
+    const bool had_tree = c->have_tree;
+    c->capturing = true;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    int rc = e == cudaSuccess ? AG2_OK : cuda_check(c, e, "cudaStreamBeginCapture");
+    if (!rc) rc = run_kick_drift(c, dt);
+    if (!rc) rc = build_tree_captured(c);
+    if (!rc && with_visual) rc = run_visual_density(c, Rv);
+    if (!rc) rc = run_sph_density(c);
+    if (!rc) {
+        e = cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream);
+        if (e != cudaSuccess) rc = cuda_check(c, e, "cudaMemsetAsync");
+    }
+    if (!rc) rc = run_forces(c);
+    if (!rc) rc = run_close_step(c, dt, hubble);
+    if (!rc) {
+        e = cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(Ctx::Ctl), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->inst_R_pin, c->inst_R, c->n_inst * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream);
+        if (e != cudaSuccess) rc = cuda_check(c, e, "cudaMemcpyAsync");
+    }
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(c->stream, &g);
+    c->capturing = false;
+    c->have_tree = had_tree;
+    // launches per replay: those outside the two loops; the loop bodies
+    // (4 level kernels, 2 moments kernels) are added per iteration
+    *nlaunch = c->launches - l0 - 6;
+    c->launches = l0;
+    if (!rc && e != cudaSuccess) rc = cuda_check(c, e, "cudaStreamEndCapture");
+    if (!rc) {
+        e = cudaGraphInstantiate(exec, g, 0);
+        if (e != cudaSuccess) rc = cuda_check(c, e, "cudaGraphInstantiate");
+    }
+    if (g) cudaGraphDestroy(g);
+    return rc;
+}
+
+static void drop_step_graphs(Ctx *c)
+{
+    for (auto &x : c->step_exec)
+        if (x) {
+            cudaGraphExecDestroy(x);
+            x = nullptr;
+        }
+    c->step_key = 0;
+}
+
+// One step as a replay of a captured graph: the same launches as ag2_step, with
+// the build's counts kept on the device (the level loop and the moments levels
+// are conditional WHILE nodes).  Two graphs, one per state buffer the step
+// starts from (the build's reorder swaps them).
+static int run_step_graph(Ctx *c, double dt, double hubble, int with_visual, double Rv)
+{
+    int rc;
+    if (c->n == 0) return AG2_OK;
+    if ((rc = prepare_captured_build(c)) != AG2_OK) return rc;
+    if (c->n_inst == 1 && !c->inst_explicit) {
+        AG2_CUDA(c, cudaMemcpy(c->inst_massInH, &c->prm.massInH, sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (!c->side_stream) AG2_CUDA(c, cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+    if (c->inst_R_pin_cap < (size_t)c->n_inst) {
+        if (c->inst_R_pin) cudaFreeHost(c->inst_R_pin);
+        c->inst_R_pin = nullptr;
+        AG2_CUDA(c, cudaMallocHost(&c->inst_R_pin, c->n_inst * sizeof(double)));
+        c->inst_R_pin_cap = c->n_inst;
+        drop_step_graphs(c);
+    }
+    const unsigned long long key = step_key(c, dt, hubble, with_visual, Rv);
+    if (key != c->step_key || !c->step_exec[c->cur]) {
+        drop_step_graphs(c);
+        const int cur0 = c->cur;
+        for (int p = 0; p < 2 && !rc; p++) {
+            c->cur = cur0 ^ p;
+            rc = capture_step(c, dt, hubble, with_visual, Rv, &c->step_exec[c->cur], &c->graph_launches[c->cur]);
+        }
+        c->cur = cur0;
+        if (rc) {
+            drop_step_graphs(c);
+            return rc;
+        }
+        c->step_key = key;
+    }
+    const int from = c->cur;
+    AG2_CUDA(c, cudaGraphLaunch(c->step_exec[from], c->stream));
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->cur ^= 1;
+    const Ctx::Ctl &h = *c->ctl_host;
+    int mlevels = 0;
+    for (int L = 0; L < AG2_MAX_DEPTH; L++) mlevels += h.lvl_cnt[L] ? 1 : 0;
+    c->launches += c->graph_launches[from] + 4 * (int64_t)(h.level + 1) + 2 * (int64_t)mlevels;
+    c->inter_grav = (int64_t)h.inter_grav;
+    c->inter_sph = (int64_t)h.inter_sph;
+    if (h.err_code) {
+        c->have_tree = false;
+        c->hist_dirty = true;
+        switch (h.err_code) {
+        case AG2_E_STACK: return set_err(c, AG2_E_STACK, "walk stack overflow (tree deeper than the walk stack supports)");
+        case AG2_E_COINCIDENT:
+            return set_err(c, AG2_E_COINCIDENT, "particles too close to separate within AG2_MAX_DEPTH levels");
+        case AG2_E_NOMEM: return set_err(c, AG2_E_NOMEM, "node pool of the step graph exhausted (redo the step)");
+        default: return set_err(c, h.err_code, "captured step failed");
+        }
+    }
+    build_tree_finish_captured(c);
+    if (hubble != 1.0) c->have_tree = false;
+    return AG2_OK;
+}
+
+int ag2_step_graphs(ag2_ctx *c, int enable)
+{
+    if (!c) return AG2_E_INVALID;
+    c->use_graphs = enable != 0;
+    if (!c->use_graphs) drop_step_graphs(c);
+    return AG2_OK;
+}
+
 int ag2_step(ag2_ctx *c, double dt, double hubble_factor, int with_visual, double Rv)
 {
     if (!c) return AG2_E_INVALID;
+    if (c->use_graphs && !c->timing) return run_step_graph(c, dt, hubble_factor, with_visual, Rv);
     int rc;
     // phase names follow the reference's Log::startProcess calls (Simulation.cpp:256-351)
     phase_reset(c);
@@ -600,6 +755,7 @@ int ag2_set_instances(ag2_ctx *c, int32_t n_inst, const int64_t *first, const do
     c->inst_dirty = true;
     c->inst_explicit = true;
     c->have_tree = false;
+    c->graph_epoch++;
     return AG2_OK;
 }
 

@@ -280,6 +280,12 @@ struct LevelBufs {
     bool local_ok;           // serial subtrees go to k_local (else they stay in the level loop)
 };
 
+// The buffers of both level parities: a level reads b[level & 1], the level it
+// runs at coming from the control block, so the same launches serve every level.
+struct LevelPair {
+    LevelBufs b[2];
+};
+
 // Level 0: the slots of an instance whose root is split are active (the
 // coordinates become ordered keys, in slot order); the slot of a one-particle
 // root is final at once.
@@ -318,10 +324,11 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
 }
 
 // digit of every active slot against its node's bounds
-__global__ void __launch_bounds__(kBlock) k_digit(int nap, LevelBufs b, Nodes nd)
+__global__ void __launch_bounds__(kBlock) k_digit(LevelPair lp, Nodes nd, const Ctx::Ctl *ctl)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nap) return;
+    const int nap = ctl->cur_nap;
+    const LevelBufs &b = lp.b[ctl->level & 1];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nap; t += gridDim.x * blockDim.x) {
     const int i = b.ap[t];
     const int j = b.posnode[i];
     const int64_t *k = nd.bkey + 9 * (int64_t)b.nl[j];
@@ -335,6 +342,7 @@ __global__ void __launch_bounds__(kBlock) k_digit(int nap, LevelBufs b, Nodes nd
     }
     b.digit[t] = (uint8_t)d;
     agg_inc(b.hist, 9 * j + d);
+    }
 }
 
 // Split decisions and children of the nodes of this level's split list.  Eight
@@ -342,13 +350,17 @@ __global__ void __launch_bounds__(kBlock) k_digit(int nap, LevelBufs b, Nodes nd
 // written with coalesced stores; the first thread of each group of eight
 // decides the split and writes the parent.  Child blocks, the next split list,
 // the leaf list and the internal-node list are reserved once per thread block.
-__global__ void __launch_bounds__(kBlock) k_nodes(int nnl, int level, int thresh, int64_t node_cap, Nodes nd,
-                                                  Ctx::Ctl *ctl, LevelBufs b, int max_depth)
+__global__ void __launch_bounds__(kBlock) k_nodes(LevelPair lpair, int thresh, int64_t node_cap, Nodes nd,
+                                                  Ctx::Ctl *ctl, int max_depth)
 {
     __shared__ int32_t sh[kBlock / 32 + 1];
     __shared__ unsigned long long sbase64;
     __shared__ int32_t sbase;
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int nnl = ctl->cur_nnl, level = ctl->level;
+    const LevelBufs &b = lpair.b[level & 1];
+    // block-uniform trip count: the block-wide reservations need every thread
+    for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < 8 * (int64_t)nnl; t0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = t0 + threadIdx.x;
     const int lane = lane_id();
     const int o = lane & 7;
     const int64_t j = t >> 3;
@@ -473,17 +485,28 @@ __global__ void __launch_bounds__(kBlock) k_nodes(int nnl, int level, int thresh
     const bool iflag = split && o == 0;
     const int32_t qi = block_reserve<int32_t>(iflag, &ctl->nlint, 1, sh, &sbase);
     if (iflag) nd.lint[qi] = make_int2((int)nid, level);
+    // the histogram entries of this node are consumed: leave them zero for the next level
+    __syncwarp();
+    if (exists) {
+        int32_t *hw = b.hist + 9 * j;
+        hw[o] = 0;
+        if (o == 0) hw[8] = 0;
+    }
+    }
 }
 
 // Partition of every active slot's particle by digit; settled particles go to
 // their final slot, the others (and their keys) to the next level's buffers.
 // The next level's active slots are the slots that land in a child that is
 // split again; they are listed in slot order within each thread block.
-__global__ void __launch_bounds__(kBlock) k_scatter(int nap, LevelBufs b, Nodes nd, Ctx::Ctl *ctl)
+__global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, Ctx::Ctl *ctl)
 {
     __shared__ int32_t sh[kBlock / 32 + 1];
     __shared__ int32_t sbase;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nap = ctl->cur_nap;
+    const LevelBufs &b = lpair.b[ctl->level & 1];
+    for (int t0 = blockIdx.x * blockDim.x; t0 < nap; t0 += gridDim.x * blockDim.x) {  // block-uniform trip count
+    const int t = t0 + threadIdx.x;
     bool act = false;
     int i = 0, nj = 0;
     if (t < nap) {
@@ -532,6 +555,21 @@ __global__ void __launch_bounds__(kBlock) k_scatter(int nap, LevelBufs b, Nodes 
         b.ap_next[q] = i;
         b.posnode_next[i] = nj;
     }
+    }
+}
+
+// Between levels: the counts the last level produced become the next level's,
+// the accumulators restart.  `inc` advances the level (0 before the first).
+// In a captured step the loop is a conditional node whose condition this sets.
+__global__ void k_level_next(Ctx::Ctl *ctl, int inc, int max_depth, cudaGraphConditionalHandle h, int use_h)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    ctl->level += inc;
+    ctl->cur_nnl = ctl->next_needs;
+    ctl->cur_nap = ctl->next_active;
+    ctl->next_needs = 0;
+    ctl->next_active = 0;
+    if (use_h) cudaGraphSetConditional(h, (ctl->cur_nnl > 0 && ctl->err_code == 0 && ctl->level < max_depth) ? 1u : 0u);
 }
 
 // Out-of-bounds tails are the only ranges whose order the partition leaves
@@ -541,10 +579,13 @@ __global__ void __launch_bounds__(kBlock) k_scatter(int nap, LevelBufs b, Nodes 
 // tails.
 constexpr int kDropSort = 4096;
 
-__global__ void k_sort_drops(int ndn, const int32_t *drop_list, Nodes nd, int32_t *perm, const int32_t *id,
+__global__ void k_sort_drops(Ctx::Ctl *ctl, const int32_t *drop_list, Nodes nd, int32_t *perm, const int32_t *id,
                              int32_t *scratch)
 {
     __shared__ long long key[kDropSort];
+    const int ndn = min(ctl->ndrop_nodes, kMaxDropNodes);
+    if (ctl->ndrop_nodes > kMaxDropNodes && blockIdx.x == 0 && threadIdx.x == 0)
+        atomicExch(&ctl->err_code, (int)AG2_E_CAPACITY);
     for (int q = blockIdx.x; q < ndn; q += gridDim.x) {
         const int64_t nid = drop_list[q];
         const int32_t nd8 = nd.ndrop[nid];
@@ -934,54 +975,96 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
 
 // Leaves (every level at once), on the state in tree order.  -1 entries pad
 // the list's per-warp stretches.
-__global__ void __launch_bounds__(kBlock) k_moments_leaf(int nleaf, const int32_t *__restrict__ list, Nodes nd,
-                                                         Particles P, const double *gas_prefix,
+__global__ void __launch_bounds__(kBlock) k_moments_leaf(const Ctx::Ctl *ctl, const int32_t *__restrict__ list,
+                                                         Nodes nd, Particles P, const double *gas_prefix,
                                                          const int32_t *gas_off, const uint8_t *gas_uni, double theta)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nleaf) return;
-    const int64_t nid = list[t];
-    if (nid < 0) return;
-    const int32_t start = nd.start[nid];
-    moments_leaf(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+    const int nleaf = ctl->nleaf;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nleaf; t += gridDim.x * blockDim.x) {
+        const int64_t nid = list[t];
+        if (nid < 0) continue;
+        const int32_t start = nd.start[nid];
+        moments_leaf(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+    }
 }
 
-// Internal nodes of one level, after the level below.
-__global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list, Nodes nd,
-                                                        Particles P, const double *gas_prefix,
-                                                        const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+// Internal nodes of one level, after the level below: the level's list
+// segment given explicitly, or (kDev) the level ctl->mlev of the control block.
+template <bool kDev>
+__global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list,
+                                                        const Ctx::Ctl *ctl, Nodes nd, Particles P,
+                                                        const double *gas_prefix, const int32_t *gas_off,
+                                                        const uint8_t *gas_uni, double theta)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cnt_lvl) return;
-    const int64_t nid = list[t];
-    const int32_t start = nd.start[nid];
-    moments_internal(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+    if (kDev) {
+        const int L = ctl->mlev;
+        if (L < 0) return;
+        cnt_lvl = ctl->lvl_cnt[L];
+        list += ctl->lvl_start[L];
+    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt_lvl; t += gridDim.x * blockDim.x) {
+        const int64_t nid = list[t];
+        const int32_t start = nd.start[nid];
+        moments_internal(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+    }
 }
 
 // internal nodes per level (one shared-memory histogram per block)
-__global__ void __launch_bounds__(kBlock) k_lvl_hist(int n, const int2 *__restrict__ lint, int32_t *cnt)
+__global__ void __launch_bounds__(kBlock) k_lvl_hist(Ctx::Ctl *ctl, const int2 *__restrict__ lint)
 {
     __shared__ int32_t hs[AG2_MAX_DEPTH];
     for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x) hs[k] = 0;
     __syncthreads();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) {
+    const int n = ctl->nlint;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int2 e = lint[t];
         if (e.x >= 0) atomicAdd(&hs[e.y], 1);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x)
-        if (hs[k]) atomicAdd(&cnt[k], hs[k]);
+        if (hs[k]) atomicAdd(&ctl->lvl_cnt[k], hs[k]);
+}
+
+// node count at the end of the level loop (the serial subtrees allocate from a pool after it)
+__global__ void k_mark_loop_nodes(Ctx::Ctl *ctl)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) ctl->loop_nodes = ctl->node_count;
+}
+
+// list segments per level (and the bucketing cursors); the deepest level with
+// internal nodes starts the moments pass
+__global__ void k_lvl_prefix(Ctx::Ctl *ctl, cudaGraphConditionalHandle h, int use_h)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int32_t acc = 0, deepest = -1;
+    for (int L = 0; L < AG2_MAX_DEPTH; L++) {
+        ctl->lvl_start[L] = acc;
+        ctl->lvl_off[L] = acc;
+        acc += ctl->lvl_cnt[L];
+        if (ctl->lvl_cnt[L]) deepest = L;
+    }
+    ctl->mlev = deepest;
+    if (use_h) cudaGraphSetConditional(h, deepest >= 0 ? 1u : 0u);
+}
+
+// the next shallower level with internal nodes (-1 when done)
+__global__ void k_mlev_next(Ctx::Ctl *ctl, cudaGraphConditionalHandle h, int use_h)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int L = ctl->mlev - 1;
+    while (L >= 0 && ctl->lvl_cnt[L] == 0) L--;
+    ctl->mlev = L;
+    if (use_h) cudaGraphSetConditional(h, L >= 0 ? 1u : 0u);
 }
 
 // internal nodes into one list segment per level (cursors start at the segments)
-__global__ void k_bucket(int n, const int2 *__restrict__ lint, int32_t *lvl_off, int32_t *lil)
+__global__ void k_bucket(Ctx::Ctl *ctl, const int2 *__restrict__ lint, int32_t *lil)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int2 e = lint[t];
-    if (e.x < 0) return;
-    lil[agg_inc(lvl_off, e.y)] = e.x;
+    const int n = ctl->nlint;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int2 e = lint[t];
+        if (e.x >= 0) lil[agg_inc(ctl->lvl_off, e.y)] = e.x;
+    }
 }
 
 // ---- serial subtrees, one warp each ---------------------------------------
@@ -1013,7 +1096,7 @@ constexpr int kIntChunk = 128;      // internal-node-list entries per warp-priva
 // digit starts 9 x 2 B.
 __host__ __device__ constexpr size_t local_smem_bytes(int cap) { return (size_t)cap * 72; }
 
-__global__ void __launch_bounds__(kLocalWarps * 32) k_local(int nroots, const int32_t *__restrict__ roots, int cap,
+__global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__restrict__ roots, int cap,
                                                             Nodes nd, Ctx::Ctl *ctl, const int64_t *__restrict__ pkey,
                                                             int64_t keycap, int32_t *perm_final, int32_t *pnode,
                                                             const int32_t *__restrict__ sid, int32_t *leaves,
@@ -1037,6 +1120,7 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(int nroots, const in
     int16_t *const FH = L1 + 5 * cap;  // 9 per frontier node
     uint8_t *DIG = reinterpret_cast<uint8_t *>(FH + 9 * cap);
 
+    const int nroots = ctl->nlocal;
     unsigned long long pool = 0, pool_end = 0;  // warp-private node pool [pool, pool_end)
     int lpool = 0, lpool_end = 0;                // warp-private stretch of the leaf list
     int ipool = 0, ipool_end = 0;                // ... and of the internal-node list
@@ -1417,6 +1501,8 @@ static int ensure_hist(Ctx *c, size_t nodes_in_level)
         cudaMalloc(&c->cursor, nc * sizeof(int32_t)) != cudaSuccess)
         return set_err(c, AG2_E_NOMEM, "histogram allocation failed");
     c->hist_cap = nc;
+    // k_nodes leaves every entry it used zero again, so the histogram is zeroed only here
+    AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, nc * sizeof(int32_t), c->stream));
     return AG2_OK;
 }
 
@@ -1497,7 +1583,67 @@ static LevelBufs level_bufs(Ctx *c, int w)
     return b;
 }
 
-static int build_tree_once(Ctx *c, bool &local_nomem);
+// Launch configuration of k_local for split threshold `thresh` (persistent
+// grid: every resident block, each warp looping over subtree roots).
+struct LocalConfig {
+    int lcap = 0, wpb = 0, blocks = 0;
+    size_t smem = 0;
+};
+static int local_config(Ctx *c, int thresh, LocalConfig &lc)
+{
+    lc.lcap = std::max(8, ((thresh - 1) + 7) & ~7);
+    lc.wpb = (int)std::max<size_t>(1, std::min<size_t>(kLocalWarps, (150u << 10) / local_smem_bytes(lc.lcap)));
+    lc.smem = (size_t)lc.wpb * local_smem_bytes(lc.lcap);
+    AG2_CUDA(c, cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem));
+    int per_sm = 0;
+    AG2_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local, lc.wpb * 32, lc.smem));
+    lc.blocks = std::max(per_sm, 1) * c->sms;
+    return AG2_OK;
+}
+
+static int build_error(Ctx *c, int code)
+{
+    c->hist_dirty = true;
+    if (code == AG2_E_COINCIDENT)
+        return set_err(c, AG2_E_COINCIDENT,
+                       "particles too close to separate within AG2_MAX_DEPTH levels "
+                       "(the reference recurses without end on coincident particles)");
+    if (code == AG2_E_CAPACITY) return set_err(c, AG2_E_CAPACITY, "more than 65536 nodes with out-of-bounds particles");
+    return set_err(c, code, "octree build failed");
+}
+
+// Run `body` (launches on c->stream) as the body of a WHILE node of the graph
+// being captured on c->stream; `h` is the node's condition.
+template <class F>
+static int capture_while(Ctx *c, cudaGraphConditionalHandle h, F body)
+{
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edata = nullptr;
+    size_t nd = 0;
+    AG2_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edata, &nd));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    AG2_CUDA(c, cudaGraphAddNode(&node, g, deps, edata, nd, &p));
+    AG2_CUDA(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+    cudaStream_t outer = c->stream;
+    c->stream = c->side_stream;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    int rc = e == cudaSuccess ? body() : cuda_check(c, e, "cudaStreamBeginCaptureToGraph");
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(c->stream, &out);
+    c->stream = outer;
+    if (rc) return rc;
+    return e == cudaSuccess ? AG2_OK : cuda_check(c, e, "cudaStreamEndCapture");
+}
+
+static int build_tree_once(Ctx *c, bool &local_nomem, bool capture);
 
 // The pool is sized before each level of the loop; serial subtrees may still
 // need more nodes than estimated, in which case the build is redone with a
@@ -1506,7 +1652,7 @@ int build_tree(Ctx *c)
 {
     for (int attempt = 0;; attempt++) {
         bool local_nomem = false;
-        const int rc = build_tree_once(c, local_nomem);
+        const int rc = build_tree_once(c, local_nomem, false);
         if (rc == AG2_E_NOMEM && local_nomem && attempt < 4) {
             c->err.clear();
             const int g = ensure_node_capacity(c, 2 * c->node_cap);
@@ -1517,15 +1663,72 @@ int build_tree(Ctx *c)
     }
 }
 
-static int build_tree_once(Ctx *c, bool &local_nomem)
+// The build inside a captured step: every count stays on the device (fixed
+// grids, the level loop and the moments levels as WHILE nodes).  The caller
+// has prepared the tables and sized the pools.
+int build_tree_captured(Ctx *c)
+{
+    bool unused = false;
+    return build_tree_once(c, unused, true);
+}
+
+// Host-side view of the tree after a captured step (from the control block).
+void build_tree_finish_captured(Ctx *c)
+{
+    const Ctx::Ctl &h = *c->ctl_host;
+    c->max_level = std::max((int)h.level, (int)h.maxlev);
+    c->nnodes = h.node_count;
+    c->nnodes_true = h.loop_nodes + 8 * (int64_t)h.local_splits;
+    c->ninternal = (c->nnodes_true - c->n_inst) / 8;
+    c->nleaves = h.nleaf;
+    c->root_radius = c->inst_R_pin ? c->inst_R_pin[0] : 0.0;
+    c->inst_R_h.assign(c->inst_R_pin, c->inst_R_pin + c->n_inst);
+    c->have_tree = true;
+    c->tree_theta = c->prm.theta;
+}
+
+// Sizes a captured build needs fixed in advance: histogram of a split list as
+// long as the particle count, and a node pool with room to grow.
+int prepare_captured_build(Ctx *c)
+{
+    int rc;
+    if ((rc = ensure_instance_tables(c)) != AG2_OK) return rc;
+    if ((rc = prepare_gas_tables(c, (int)c->n)) != AG2_OK) return rc;
+    if ((rc = ensure_hist(c, std::max<size_t>(c->n, 1))) != AG2_OK) return rc;
+    LocalConfig lc;
+    if ((rc = local_config(c, c->prm.split_threshold, lc)) != AG2_OK) return rc;
+    c->loc_lcap = lc.lcap;
+    c->loc_wpb = lc.wpb;
+    c->loc_blocks = lc.blocks;
+    c->loc_smem = lc.smem;
+    const size_t want = (size_t)(2 * std::max<int64_t>(c->nnodes, 4 * (int64_t)c->n)) +
+                        (size_t)lc.blocks * lc.wpb * kPoolChunk + 1024;
+    if ((rc = ensure_node_capacity(c, want)) != AG2_OK) return rc;
+    if (c->hist_dirty) {
+        AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, c->hist_cap * sizeof(int32_t), c->stream));
+        c->hist_dirty = false;
+    }
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    return AG2_OK;
+}
+
+static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
 {
     const int n = (int)c->n;
     c->have_tree = false;
     int rc;
-    if ((rc = ensure_instance_tables(c)) != AG2_OK) return rc;
+    if (!capture) {
+        if ((rc = ensure_instance_tables(c)) != AG2_OK) return rc;
+        if ((rc = prepare_gas_tables(c, n)) != AG2_OK) return rc;
+        if ((rc = ensure_hist(c, 1)) != AG2_OK) return rc;
+        if (c->hist_dirty) {
+            AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, c->hist_cap * sizeof(int32_t), c->stream));
+            c->hist_dirty = false;
+        }
+    }
     const int K = c->n_inst;
     Particles &S = c->S();
-    if ((rc = prepare_gas_tables(c, n)) != AG2_OK) return rc;
+    const unsigned fixed_grid = (unsigned)c->sms * 8;  // grid-stride launches of a captured build
 
     // root half-width of every instance
     AG2_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream));
@@ -1547,7 +1750,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem)
         AG2_LAUNCH(c, k_width_max, grid_for(n, kBlock), kBlock, 0, n, S.px, S.py, S.pz, c->pinst, c->width_thr,
                    c->inst_R);
     phase_mark(c, "build: root width");
-    if ((rc = ensure_node_capacity(c, (size_t)K + 1024)) != AG2_OK) return rc;
+    if (!capture && (rc = ensure_node_capacity(c, (size_t)K + 1024)) != AG2_OK) return rc;
     const int thresh = c->prm.split_threshold;
     AG2_LAUNCH(c, k_ctl_reset, 1, 1, 0, c->ctl, K);
     // serial subtrees (fewer than split_threshold particles) are built one warp each when they fit
@@ -1556,84 +1759,102 @@ static int build_tree_once(Ctx *c, bool &local_nomem)
                c->nl[0], c->leaves, local_ok, c->lroots);
     AG2_LAUNCH(c, k_level0, grid_for(n, kBlock), kBlock, 0, n, c->pinst, c->nd, S.px, S.py, S.pz, level_bufs(c, 0),
                c->ctl);
-    c->inst_R_h.resize(K);
-    AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-    c->root_radius = c->inst_R_h[0];
+    LevelPair lpair;
+    lpair.b[0] = level_bufs(c, 0);
+    lpair.b[1] = level_bufs(c, 1);
+    lpair.b[0].local_ok = lpair.b[1].local_ok = local_ok;
 
+    // the level loop
     c->level_base.assign({0, (int64_t)K});
-    int level = 0;
-    int nnl = c->ctl_host->next_needs;  // split list of the level
-    int nap = c->ctl_host->next_active; // active slots of the level
-    while (nnl > 0) {
-        if ((rc = ensure_hist(c, (size_t)nnl)) != AG2_OK) return rc;
-        if ((rc = ensure_node_capacity(c, (size_t)(c->level_base[level + 1] + 8 * (int64_t)nnl))) != AG2_OK)
-            return rc;
-        AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, 9 * (size_t)nnl * sizeof(int32_t), c->stream));
-        AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_needs, 0, sizeof(int32_t), c->stream));
-        AG2_CUDA(c, cudaMemsetAsync(&c->ctl->next_active, 0, sizeof(int32_t), c->stream));
-        LevelBufs b = level_bufs(c, level & 1);
-        b.local_ok = local_ok;
-        AG2_LAUNCH(c, k_digit, grid_for(nap, kBlock), kBlock, 0, nap, b, c->nd);
-        AG2_LAUNCH(c, k_nodes, grid_for((size_t)nnl * 8, kBlock), kBlock, 0, nnl, level, thresh,
-                   (int64_t)c->node_cap, c->nd, c->ctl, b, (int)AG2_MAX_DEPTH);
-        AG2_LAUNCH(c, k_scatter, grid_for(nap, kBlock), kBlock, 0, nap, b, c->nd, c->ctl);
+    if (capture) {
+        cudaStreamCaptureStatus st;
+        cudaGraph_t g = nullptr;
+        AG2_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g));
+        cudaGraphConditionalHandle h;
+        AG2_CUDA(c, cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+        AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 0, (int)AG2_MAX_DEPTH, h, 1);
+        rc = capture_while(c, h, [&]() -> int {
+            AG2_LAUNCH(c, k_digit, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
+            AG2_LAUNCH(c, k_nodes, fixed_grid, kBlock, 0, lpair, thresh, (int64_t)c->node_cap, c->nd, c->ctl,
+                       (int)AG2_MAX_DEPTH);
+            AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
+            AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 1, (int)AG2_MAX_DEPTH, h, 1);
+            return AG2_OK;
+        });
+        if (rc) return rc;
+        AG2_LAUNCH(c, k_mark_loop_nodes, 1, 32, 0, c->ctl);
+    } else {
+        cudaGraphConditionalHandle none = 0;
+        AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 0, (int)AG2_MAX_DEPTH, none, 0);
+        c->inst_R_h.resize(K);
+        AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream));
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-        const Ctx::Ctl &h = *c->ctl_host;
-        if (h.err_code) {
-            if (h.err_code == AG2_E_COINCIDENT)
-                return set_err(c, AG2_E_COINCIDENT,
-                               "particles too close to separate within AG2_MAX_DEPTH levels "
-                               "(the reference recurses without end on coincident particles)");
-            return set_err(c, h.err_code, "octree build failed");
+        c->root_radius = c->inst_R_h[0];
+        int nnl = c->ctl_host->cur_nnl, nap = c->ctl_host->cur_nap;
+        while (nnl > 0) {
+            if ((rc = ensure_hist(c, (size_t)nnl)) != AG2_OK) return rc;
+            if ((rc = ensure_node_capacity(c, (size_t)(c->level_base.back() + 8 * (int64_t)nnl))) != AG2_OK) return rc;
+            lpair.b[0] = level_bufs(c, 0);
+            lpair.b[1] = level_bufs(c, 1);
+            lpair.b[0].local_ok = lpair.b[1].local_ok = local_ok;
+            AG2_LAUNCH(c, k_digit, grid_for(nap, kBlock), kBlock, 0, lpair, c->nd, c->ctl);
+            AG2_LAUNCH(c, k_nodes, grid_for((size_t)nnl * 8, kBlock), kBlock, 0, lpair, thresh, (int64_t)c->node_cap,
+                       c->nd, c->ctl, (int)AG2_MAX_DEPTH);
+            AG2_LAUNCH(c, k_scatter, grid_for(nap, kBlock), kBlock, 0, lpair, c->nd, c->ctl);
+            AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 1, (int)AG2_MAX_DEPTH, none, 0);
+            if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+            const Ctx::Ctl &h = *c->ctl_host;
+            if (h.err_code) return build_error(c, h.err_code);
+            c->level_base.push_back(h.node_count);
+            nnl = h.cur_nnl;
+            nap = h.cur_nap;
         }
-        c->level_base.push_back(h.node_count);
-        nnl = h.next_needs;
-        nap = h.next_active;
-        level++;
+        AG2_LAUNCH(c, k_mark_loop_nodes, 1, 32, 0, c->ctl);
     }
     phase_mark(c, "build: levels");
 
     // serial subtrees: one warp each
-    const int nloc = c->ctl_host->nlocal;
-    const int64_t loop_nodes = c->ctl_host->node_count;
-    if (nloc > 0) {
-        const int lcap = std::max(8, ((thresh - 1) + 7) & ~7);
-        const int wpb = (int)std::max<size_t>(1, std::min<size_t>(kLocalWarps, (150u << 10) / local_smem_bytes(lcap)));
-        const size_t smem = (size_t)wpb * local_smem_bytes(lcap);
-        AG2_CUDA(c, cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 0, sms = 0;
-        AG2_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local, wpb * 32, smem));
-        AG2_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-        const int blocks = std::max(1, std::min((nloc + wpb - 1) / wpb, std::max(per_sm, 1) * sms));
-        const size_t need = (size_t)loop_nodes + 12 * (size_t)c->ctl_host->nlocal_part +
-                            (size_t)blocks * wpb * kPoolChunk + 1024;
-        if ((rc = ensure_node_capacity(c, need)) != AG2_OK) return rc;
-        AG2_LAUNCH(c, k_local, blocks, wpb * 32, smem, nloc, c->lroots, lcap, c->nd, c->ctl, c->pkey,
+    LocalConfig lc;
+    if (capture) {
+        lc.lcap = c->loc_lcap;  // set up before the capture (no runtime calls inside it)
+        lc.wpb = c->loc_wpb;
+        lc.blocks = c->loc_blocks;
+        lc.smem = c->loc_smem;
+        AG2_LAUNCH(c, k_local, lc.blocks, lc.wpb * 32, lc.smem, c->lroots, lc.lcap, c->nd, c->ctl, c->pkey,
                    (int64_t)c->cap, c->perm_final, c->pnode, S.id, c->leaves, (int64_t)c->leaves_cap,
                    (int)AG2_MAX_DEPTH, (int64_t)c->node_cap);
-        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-        const Ctx::Ctl &h = *c->ctl_host;
-        if (h.err_code) {
-            if (h.err_code == AG2_E_COINCIDENT)
-                return set_err(c, AG2_E_COINCIDENT,
-                               "particles too close to separate within AG2_MAX_DEPTH levels "
-                               "(the reference recurses without end on coincident particles)");
-            if (h.err_code == AG2_E_NOMEM) local_nomem = true;
-            return set_err(c, h.err_code, "octree build failed");
+        AG2_LAUNCH(c, k_sort_drops, fixed_grid, kBlock, 0, c->ctl, c->drop_list, c->nd, c->perm_final, S.id, c->perm2);
+    } else {
+        const int nloc = c->ctl_host->nlocal;
+        const int64_t loop_nodes = c->ctl_host->node_count;
+        if (nloc > 0) {
+            if ((rc = local_config(c, thresh, lc)) != AG2_OK) return rc;
+            const int blocks = std::max(1, std::min((nloc + lc.wpb - 1) / lc.wpb, lc.blocks));
+            const size_t need = (size_t)loop_nodes + 12 * (size_t)c->ctl_host->nlocal_part +
+                                (size_t)blocks * lc.wpb * kPoolChunk + 1024;
+            if ((rc = ensure_node_capacity(c, need)) != AG2_OK) return rc;
+            AG2_LAUNCH(c, k_local, blocks, lc.wpb * 32, lc.smem, c->lroots, lc.lcap, c->nd, c->ctl, c->pkey,
+                       (int64_t)c->cap, c->perm_final, c->pnode, S.id, c->leaves, (int64_t)c->leaves_cap,
+                       (int)AG2_MAX_DEPTH, (int64_t)c->node_cap);
+            if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+            const Ctx::Ctl &h = *c->ctl_host;
+            if (h.err_code) {
+                if (h.err_code == AG2_E_NOMEM) local_nomem = true;
+                return build_error(c, h.err_code);
+            }
+            phase_mark(c, "build: serial subtrees");
         }
-        phase_mark(c, "build: serial subtrees");
+        c->max_level = std::max((int)c->level_base.size() - 2, (int)c->ctl_host->maxlev);
+        c->nnodes = c->ctl_host->node_count;
+        c->nnodes_true = loop_nodes + 8 * (int64_t)c->ctl_host->local_splits;
+        c->ninternal = (c->nnodes_true - K) / 8;
+        c->nleaves = c->ctl_host->nleaf;
+        if (c->ctl_host->ndrop_nodes > kMaxDropNodes) return build_error(c, AG2_E_CAPACITY);
+        if (c->ctl_host->ndrop_nodes > 0)
+            AG2_LAUNCH(c, k_sort_drops, (unsigned)c->ctl_host->ndrop_nodes, kBlock, 0, c->ctl, c->drop_list, c->nd,
+                       c->perm_final, S.id, c->perm2);
     }
-    c->max_level = std::max((int)c->level_base.size() - 2, (int)c->ctl_host->maxlev);
-    c->nnodes = c->ctl_host->node_count;
-    c->nnodes_true = loop_nodes + 8 * (int64_t)c->ctl_host->local_splits;
-    c->ninternal = (c->nnodes_true - K) / 8;
-    c->nleaves = c->ctl_host->nleaf;
-    if (c->ctl_host->ndrop_nodes > kMaxDropNodes)
-        return set_err(c, AG2_E_CAPACITY, "more than 65536 nodes with out-of-bounds particles");
-    if (c->ctl_host->ndrop_nodes > 0)
-        AG2_LAUNCH(c, k_sort_drops, (unsigned)c->ctl_host->ndrop_nodes, kBlock, 0, c->ctl_host->ndrop_nodes,
-                   c->drop_list, c->nd, c->perm_final, S.id, c->perm2);
 
     // particle state into tree order
     Particles &src = c->st[c->cur];
@@ -1645,31 +1866,42 @@ static int build_tree_once(Ctx *c, bool &local_nomem)
 
     // moments: every leaf at once, then the internal nodes level by level,
     // deepest first (the internal-node list bucketed by level)
-    AG2_LAUNCH(c, k_moments_leaf, grid_for(c->nleaves, kBlock), kBlock, 0, c->nleaves, c->leaves, c->nd, c->S(),
-               c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
-    {
-        const int nlint = c->ctl_host->nlint;
-        AG2_LAUNCH(c, k_lvl_hist, grid_for(nlint, kBlock), kBlock, 0, nlint, c->nd.lint, c->ctl->lvl_cnt);
+    const unsigned gl = capture ? fixed_grid : std::max(1u, grid_for(c->nleaves, kBlock));
+    AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, c->ctl, c->leaves, c->nd, c->S(), c->gas_prefix, c->gas_off,
+               c->gas_uni, c->prm.theta);
+    const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
+    AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint);
+    if (capture) {
+        cudaStreamCaptureStatus st;
+        cudaGraph_t g = nullptr;
+        AG2_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g));
+        cudaGraphConditionalHandle h;
+        AG2_CUDA(c, cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+        AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, h, 1);
+        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil);
+        rc = capture_while(c, h, [&]() -> int {
+            AG2_LAUNCH(c, k_moments_int<true>, fixed_grid, kBlock, 0, 0, c->nd.lil, c->ctl, c->nd, c->S(),
+                       c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+            AG2_LAUNCH(c, k_mlev_next, 1, 32, 0, c->ctl, h, 1);
+            return AG2_OK;
+        });
+        if (rc) return rc;
+    } else {
+        cudaGraphConditionalHandle none = 0;
+        AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, none, 0);
+        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil);
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
         c->lvl_cnt_h.assign(c->ctl_host->lvl_cnt, c->ctl_host->lvl_cnt + AG2_MAX_DEPTH);
-        c->lvl_start_h.assign(AG2_MAX_DEPTH, 0);
-        int32_t acc = 0;
-        for (int L = 0; L < AG2_MAX_DEPTH; L++) {
-            c->lvl_start_h[L] = acc;
-            acc += c->lvl_cnt_h[L];
-        }
-        AG2_CUDA(c, cudaMemcpyAsync(c->ctl->lvl_off, c->lvl_start_h.data(), AG2_MAX_DEPTH * sizeof(int32_t),
-                                    cudaMemcpyHostToDevice, c->stream));
-        AG2_LAUNCH(c, k_bucket, grid_for(nlint, kBlock), kBlock, 0, nlint, c->nd.lint, c->ctl->lvl_off, c->nd.lil);
+        c->lvl_start_h.assign(c->ctl_host->lvl_start, c->ctl_host->lvl_start + AG2_MAX_DEPTH);
         for (int L = AG2_MAX_DEPTH - 1; L >= 0; L--) {
             const int32_t cnt = c->lvl_cnt_h[L];
             if (!cnt) continue;
-            AG2_LAUNCH(c, k_moments_int, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.lil + c->lvl_start_h[L], c->nd,
-                       c->S(), c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+            AG2_LAUNCH(c, k_moments_int<false>, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.lil + c->lvl_start_h[L],
+                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
         }
     }
     phase_mark(c, "build: moments");
-    c->have_tree = true;
+    c->have_tree = true;  // (inside a capture: for the launches that follow it)
     c->tree_theta = c->prm.theta;
     return AG2_OK;
 }

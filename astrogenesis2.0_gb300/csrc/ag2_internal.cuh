@@ -76,7 +76,21 @@ struct Ctx {
     ag2_params prm;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t side_stream = nullptr;  // captures the bodies of a step graph's loops
+    bool capturing = false;              // a step graph is being captured on `stream`
+    // step graphs (ag2_step_graphs): one per state buffer the step starts from
+    bool use_graphs = false;
+    cudaGraphExec_t step_exec[2] = {};
+    unsigned long long step_key = 0;     // parameters the graphs were captured for
+    int64_t graph_launches[2] = {};      // kernels captured outside the loops
+    double *inst_R_pin = nullptr;        // pinned copy of the root half-widths (step graphs)
+    size_t inst_R_pin_cap = 0;
+    int64_t graph_epoch = 0;             // bumped when the particle set, layout or parameters change
     int device = 0;
+    int sms = 152;       // multiprocessors of the device
+    // k_local's launch for captured builds (set before the capture)
+    int loc_lcap = 0, loc_wpb = 0, loc_blocks = 0;
+    size_t loc_smem = 0;
     size_t cap = 0;      // particle capacity
     size_t n = 0;        // particles uploaded
     size_t node_cap = 0; // node pool capacity
@@ -119,6 +133,7 @@ struct Ctx {
     int32_t *hist = nullptr;      // 9 per node of a level
     int32_t *cursor = nullptr;
     size_t hist_cap = 0;
+    bool hist_dirty = false;      // a failed build may have left histogram entries set
     double *gas_prefix = nullptr; // sequential sums k*m_gas (uniform gas mass)
     size_t gas_prefix_cap = 0;
     double *staging = nullptr;    // 6n doubles for upload/download
@@ -180,6 +195,12 @@ struct Ctx {
         int32_t nleaf;          // entries of the leaf list
         int32_t nlocal;         // serial subtree roots for k_local
         int32_t nlint;          // entries of the internal-node list
+        int32_t level;          // level loop: the level being split
+        int32_t cur_nnl;        // ... its split list
+        int32_t cur_nap;        // ... its active slots
+        int32_t mlev;           // moments: the level being finished (-1 when done)
+        int64_t loop_nodes;     // node count at the end of the level loop
+        int32_t lvl_start[AG2_MAX_DEPTH];  // internal-node list segments per level
         int32_t lvl_cnt[AG2_MAX_DEPTH];  // internal nodes per level
         int32_t lvl_off[AG2_MAX_DEPTH];  // bucketing cursors
         int32_t maxlev;         // deepest level of the serial subtrees
@@ -248,7 +269,7 @@ inline bool launch_ok(const dim3 &g) { return g.x > 0 && g.y > 0 && g.z > 0; }
             kern<<<(grid), (block), (smem), (c)->stream>>>(__VA_ARGS__);     \
             (c)->launches++;                                                 \
             cudaError_t _le = cudaGetLastError();                            \
-            if (_le == cudaSuccess && (c)->debug_sync)                       \
+            if (_le == cudaSuccess && (c)->debug_sync && !(c)->capturing)    \
                 _le = cudaStreamSynchronize((c)->stream);                    \
             if (_le != cudaSuccess) return cuda_check(c, _le, #kern);        \
         }                                                                    \
@@ -257,6 +278,9 @@ inline bool launch_ok(const dim3 &g) { return g.x > 0 && g.y > 0 && g.z > 0; }
 // entry points implemented per translation unit
 int build_tree(Ctx *c);
 int ensure_instance_tables(Ctx *c);
+int build_tree_captured(Ctx *c);
+void build_tree_finish_captured(Ctx *c);
+int prepare_captured_build(Ctx *c);
 int ensure_node_capacity(Ctx *c, size_t need);
 int run_forces(Ctx *c);
 int run_sph_density(Ctx *c);

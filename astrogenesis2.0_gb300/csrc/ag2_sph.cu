@@ -235,7 +235,7 @@ int run_sph_density(Ctx *c)
     TreeView t = view(c);
     AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
-    if (c->n_inst == 1 && !c->inst_explicit)  // a single simulation follows ag2_set_params
+    if (c->n_inst == 1 && !c->inst_explicit && !c->capturing)  // a single simulation follows ag2_set_params
         AG2_CUDA(c, cudaMemcpyAsync(c->inst_massInH, &c->prm.massInH, sizeof(double), cudaMemcpyHostToDevice, c->stream));
     AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->inst_massInH, c->nd.flag);
     AG2_LAUNCH(c, k_final, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->nd.flag, c->finalnode, c->nodelist,

@@ -913,9 +913,7 @@ int run_energy(Ctx *c, double *out4)
     const int eb = (int)std::max<int64_t>(1, std::min<int64_t>(256, (6 * (int64_t)c->cap - n) / 3));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    const int blocks = std::min((c->ngroups + 3) / 4, sms * 16);
+    const int blocks = std::min((c->ngroups + 3) / 4, c->sms * 16);
     AG2_LAUNCH(c, k_potential, std::max(blocks, 1), kWalkBlock, 0, a, phi);
     AG2_LAUNCH(c, k_energy_sums, eb, 256, 0, n, S.m, S.vx, S.vy, S.vz, phi, S.U, S.type, part);
     std::vector<double> h(3 * eb);
@@ -945,8 +943,7 @@ int run_forces(Ctx *c)
     const bool gas = c->ngas > 0;
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->inter_grav, 0, 2 * sizeof(unsigned long long), c->stream));
-    int dev_sms = 152;
-    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int dev_sms = c->sms;
     const int ngroups = c->ngroups;
     int blocks = std::min((ngroups + 3) / 4, dev_sms * 16);
     if (blocks < 1) blocks = 1;

@@ -345,6 +345,31 @@ def our_arm(args, wl, d):
     achieved = flop_per_walk / walk_avg_s / 1e12
     peak = ctx.fp32_peak_gflops() / 1e3
 
+    # the same steps replayed from captured CUDA graphs (ag2_step_graphs)
+    graph = None
+    if args.graph_steps > 0:
+        ctx.step_graphs(True)
+        for _ in range(3):  # capture, then warm
+            ctx.step(dt)
+        torch.cuda.synchronize()
+        gl0 = ctx.launches()
+        gev = []
+        for _ in range(args.graph_steps):
+            if flush is not None:
+                with torch.cuda.stream(stream):
+                    flush.fill_(1.0)
+            e = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            e[0].record(stream)
+            ctx.step(dt)
+            e[1].record(stream)
+            gev.append(e)
+        torch.cuda.synchronize()
+        tg = sum(a.elapsed_time(b) for a, b in gev) / 1e3
+        graph = {"value": n * args.graph_steps * D.world / max_over_ranks(tg, D), "unit": UNIT,
+                 "steps": args.graph_steps, "ms_per_step": tg / args.graph_steps * 1e3,
+                 "gpu_launches": ctx.launches() - gl0}
+        ctx.step_graphs(False)
+
     # energy drift of the FP32 form over --drift-steps further steps (untimed)
     drift = None
     if args.drift_steps > 0 and 0.0 < wl["e0"] < 0.6:
@@ -473,6 +498,7 @@ def our_arm(args, wl, d):
             "speedup_vs_plain": value / plain if plain else None,
             "force_error": force_error,
             "energy_drift": drift,
+            "step_graph": graph,
         }
         if per_launch:
             out["one_sim_per_launch"] = per_launch
@@ -708,6 +734,7 @@ def main():
     ap.add_argument("--ref-walk-fraction", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
+    ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rates", default="10,50,200")
     args = ap.parse_args()

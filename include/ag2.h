@@ -139,6 +139,16 @@ int ag2_scale_positions(ag2_ctx *ctx, double factor);
  * Hubble factor, kick. */
 int ag2_step(ag2_ctx *ctx, double dt, double hubble_factor, int with_visual_density,
              double visualDensityRadius);
+/* Run every later ag2_step as a replay of a CUDA graph captured from it (enable
+ * = 1) or as separate launches (0, the default).  The graph holds the whole
+ * step; the build's data-dependent parts (the level loop, the moments levels)
+ * are conditional WHILE nodes whose conditions the device sets, so a step
+ * needs no host round trip.  Graphs are captured again when the particle set,
+ * the instance layout, the parameters, the stream, dt, the Hubble factor or a
+ * pool size change.  The node pool is sized for twice the last tree; a tree
+ * that outgrows it fails the step with AG2_E_NOMEM (redo it after a plain
+ * ag2_build_tree, which grows the pool). */
+int ag2_step_graphs(ag2_ctx *ctx, int enable);
 
 /* Time the FP32 walk's compiled variants (register budget per thread, hence
  * warps resident per SM) on the current tree and keep the fastest for later
