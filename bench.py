@@ -64,7 +64,7 @@ CLOCK_Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,
 
 
 class ClockSampler:
-    """nvidia-smi sampling every 200 ms, started before the warm-up so that its
+    """nvidia-smi sampling every 50 ms, started before the warm-up so that its
     start-up never overlaps the timed window; only samples taken inside the
     window [mark_start, mark_stop] are reported."""
 
@@ -75,7 +75,7 @@ class ClockSampler:
         self.t0 = self.t1 = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={CLOCK_Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                       "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
                                       stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
@@ -104,7 +104,7 @@ class ClockSampler:
             self.p.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        inside = [l for t, l in self.lines if self.t0 is not None and self.t0 - 0.2 <= t <= (self.t1 or t) + 0.2]
+        inside = [l for t, l in self.lines if self.t0 is not None and self.t0 - 0.05 <= t <= (self.t1 or t) + 0.05]
         for line in inside:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 7:
@@ -722,14 +722,14 @@ def one_sim_per_launch(d, wl, steps, stream):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="merger4m", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--error-samples", type=int, default=2048)
+    ap.add_argument("--error-samples", type=int, default=65536)
     ap.add_argument("--cpu-walk-fraction", type=int, default=8)
     ap.add_argument("--ref-walk-fraction", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
