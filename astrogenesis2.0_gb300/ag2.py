@@ -22,7 +22,7 @@ OK = 0
 E_INVALID, E_CUDA, E_NOMEM, E_COINCIDENT, E_DEPTH, E_STACK, E_NAN, E_CAPACITY = range(-1, -9, -1)
 PREC_FP64, PREC_FP32 = 0, 1
 FIELDS = {"pos": 0, "vel": 1, "acc": 2, "mass": 3, "h": 4, "rho": 5, "P": 6, "T": 7, "U": 8, "dUdt": 9,
-          "vdens": 10}
+          "vdens": 10, "tstep": 11, "tnext": 12}
 VECTOR_FIELDS = {"pos", "vel", "acc"}
 
 # every exported symbol of include/ag2.h
@@ -34,6 +34,7 @@ EXPORTS = [
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
     "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
     "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy", "ag2_step_graphs",
+    "ag2_block_init", "ag2_block_step",
 ]
 
 
@@ -95,6 +96,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_diagnostics.argtypes = [P, P]
     L.ag2_energy.argtypes = [P, P]
     L.ag2_step_graphs.argtypes = [P, I]
+    L.ag2_block_init.argtypes = [P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    L.ag2_block_step.argtypes = [P, ctypes.c_double, I, ctypes.c_double, dp, ctypes.POINTER(ctypes.c_int64)]
     L.ag2_fp32_peak_probe.argtypes = [P, dp]
     L.ag2_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.ag2_root_radius_noalloc.argtypes = [P, ctypes.c_int64, P, P]
@@ -260,6 +263,17 @@ class Context:
         out = np.empty(8)
         self._check(self.L.ag2_diagnostics(self.h, _ptr(out)))
         return {"mass": out[0], "ekin": out[1], "momentum": out[2:5], "angmom": out[5:8]}
+
+    def block_init(self, eta: float, min_dt: float, max_dt: float, global_time: float = 0.0):
+        """Per-particle power-of-two time steps from the current acc."""
+        self._check(self.L.ag2_block_init(self.h, eta, min_dt, max_dt, global_time))
+
+    def block_step(self, H0: float = 0.0, visual_density: bool = False, visual_radius: float = 0.0):
+        """One block step; returns (global time, number of particles integrated)."""
+        t, k = ctypes.c_double(), ctypes.c_int64()
+        self._check(self.L.ag2_block_step(self.h, H0, 1 if visual_density else 0, visual_radius, ctypes.byref(t),
+                                          ctypes.byref(k)))
+        return t.value, k.value
 
     def step_graphs(self, enable: bool = True):
         """Run later steps as replays of a captured CUDA graph."""

@@ -81,6 +81,7 @@ __global__ void k_unpack(int n, const double *pos, const double *vel, const doub
     s.U[i] = U ? U[i] : 0.0;
     s.dUdt[i] = 0.0;
     s.h[i] = s.rho[i] = s.P[i] = s.T[i] = s.vdens[i] = 0.0;
+    s.tstep[i] = s.tnext[i] = 0.0;
     s.type[i] = type[i];
     s.id[i] = i;
 }
@@ -96,6 +97,8 @@ __device__ double *field1(Particles &s, int f)
     case AG2_U: return s.U;
     case AG2_DUDT: return s.dUdt;
     case AG2_VDENS: return s.vdens;
+    case AG2_TSTEP: return s.tstep;
+    case AG2_TNEXT: return s.tnext;
     }
     return nullptr;
 }
@@ -144,7 +147,7 @@ __global__ void k_scatter_in(int n, Particles s, int f, const double *in)
 int alloc_particles(Ctx *c, Particles &p, size_t cap)
 {
     double **d[] = {&p.px, &p.py, &p.pz, &p.vx, &p.vy, &p.vz, &p.ax, &p.ay, &p.az, &p.m,
-                    &p.U,  &p.dUdt, &p.h, &p.rho, &p.P, &p.T, &p.vdens};
+                    &p.U,  &p.dUdt, &p.h, &p.rho, &p.P, &p.T, &p.vdens, &p.tstep, &p.tnext};
     for (double **q : d)
         if (cudaMalloc(q, cap * sizeof(double)) != cudaSuccess)
             return set_err(c, AG2_E_NOMEM, "particle allocation failed");
@@ -156,7 +159,7 @@ int alloc_particles(Ctx *c, Particles &p, size_t cap)
 void free_particles(Particles &p)
 {
     double *d[] = {p.px, p.py, p.pz, p.vx, p.vy, p.vz, p.ax, p.ay, p.az, p.m, p.U, p.dUdt, p.h, p.rho, p.P, p.T,
-                   p.vdens};
+                   p.vdens, p.tstep, p.tnext};
     for (double *q : d) cudaFree(q);
     cudaFree(p.type);
     cudaFree(p.id);
@@ -395,6 +398,7 @@ int ag2_destroy(ag2_ctx *c)
     for (auto &x : c->step_exec)
         if (x) cudaGraphExecDestroy(x);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);
+    if (c->blk_key) cudaFree(c->blk_key);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -469,7 +473,7 @@ int ag2_upload_device(ag2_ctx *c, size_t n, const double *pos, const double *vel
 
 int ag2_set_field(ag2_ctx *c, int f, const double *src, int src_is_device)
 {
-    if (!c || !src || f < AG2_POS || f > AG2_VDENS) return set_err(c, AG2_E_INVALID, "bad field");
+    if (!c || !src || f < AG2_POS || f > AG2_TNEXT) return set_err(c, AG2_E_INVALID, "bad field");
     size_t cnt = (f <= AG2_ACC ? 3 : 1) * c->n;
     if (!c->n) return AG2_OK;
     const double *in = src;
@@ -486,7 +490,7 @@ int ag2_set_field(ag2_ctx *c, int f, const double *src, int src_is_device)
 
 int ag2_download(ag2_ctx *c, int f, double *dst, int dst_is_device)
 {
-    if (!c || !dst || f < AG2_POS || f > AG2_VDENS) return set_err(c, AG2_E_INVALID, "bad field");
+    if (!c || !dst || f < AG2_POS || f > AG2_TNEXT) return set_err(c, AG2_E_INVALID, "bad field");
     size_t cnt = (f <= AG2_ACC ? 3 : 1) * c->n;
     if (!c->n) return AG2_OK;
     double *out = dst_is_device ? dst : c->staging;
@@ -682,6 +686,18 @@ static int run_step_graph(Ctx *c, double dt, double hubble, int with_visual, dou
     build_tree_finish_captured(c);
     if (hubble != 1.0) c->have_tree = false;
     return AG2_OK;
+}
+
+int ag2_block_init(ag2_ctx *c, double eta, double min_dt, double max_dt, double global_time)
+{
+    if (!c) return AG2_E_INVALID;
+    return run_block_init(c, eta, min_dt, max_dt, global_time);
+}
+
+int ag2_block_step(ag2_ctx *c, double H0, int with_visual, double Rv, double *global_time, int64_t *active)
+{
+    if (!c) return AG2_E_INVALID;
+    return run_block_step(c, H0, with_visual, Rv, global_time, active);
 }
 
 int ag2_step_graphs(ag2_ctx *c, int enable)

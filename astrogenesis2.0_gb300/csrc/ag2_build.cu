@@ -651,6 +651,8 @@ __global__ void k_reorder(int n, const int32_t *__restrict__ perm, Particles s, 
     d.P[i] = s.P[p];
     d.T[i] = s.T[p];
     d.vdens[i] = s.vdens[p];
+    d.tstep[i] = s.tstep[p];
+    d.tnext[i] = s.tnext[p];
     d.type[i] = s.type[p];
     d.id[i] = s.id[p];
 }

@@ -36,6 +36,7 @@ struct Particles {
     double *vx, *vy, *vz;
     double *ax, *ay, *az;
     double *m, *U, *dUdt, *h, *rho, *P, *T, *vdens;
+    double *tstep, *tnext;  // block time steps: the particle's step and its next integration time
     uint8_t *type;
     int32_t *id;
 };
@@ -84,6 +85,12 @@ struct Ctx {
     unsigned long long step_key = 0;     // parameters the graphs were captured for
     int64_t graph_launches[2] = {};      // kernels captured outside the loops
     double *inst_R_pin = nullptr;        // pinned copy of the root half-widths (step graphs)
+    // block time steps (ag2_block_init / ag2_block_step)
+    bool blk_ready = false;
+    double blk_eta = 0, blk_dmin = 0, blk_dmax = 0, blk_t = 0;
+    long long *blk_key = nullptr;  // device: earliest next integration time (ordered key)
+    int32_t *blk_count = nullptr;  // device: due particles
+    const uint8_t *walk_active = nullptr;  // per slot: walk it (null = every particle)
     size_t inst_R_pin_cap = 0;
     int64_t graph_epoch = 0;             // bumped when the particle set, layout or parameters change
     int device = 0;
@@ -294,6 +301,8 @@ int sync_ctl(Ctx *c);  // copy ctl to host (synchronises the stream)
 int run_direct_sum(Ctx *c, size_t ns, const int64_t *ids_host, double *out_host);
 int run_diagnostics(Ctx *c, double *out8);
 int run_energy(Ctx *c, double *out4);
+int run_block_init(Ctx *c, double eta, double dmin, double dmax, double t);
+int run_block_step(Ctx *c, double H0, int with_visual, double Rv, double *t_out, int64_t *active_out);
 int run_fma_probe(Ctx *c, double *gflops);
 int run_autotune(Ctx *c, int *chosen);
 

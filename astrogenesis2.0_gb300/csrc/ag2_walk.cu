@@ -51,6 +51,7 @@ struct WalkArgs {
     const double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz, *radius;
     const int4 *groups;  // (first slot, lanes, instance = root node, 0)
     int ngroups;
+    const uint8_t *active;  // per slot: walk it (block time steps); null = every particle
     double theta, e0, G;
     Ctx::Ctl *ctl;
 };
@@ -165,7 +166,8 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
         const int i = gd.x + lane;
         const bool live = lane < gd.y;
         const int root = gd.z;
-        const bool valid = live && a.m[i] != 0.0;
+        const bool act = live && (!a.active || a.active[i]);  // block steps walk the due particles only
+        const bool valid = act && a.m[i] != 0.0;
         double xi = 0, yi = 0, zi = 0, hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
         bool gas_i = false;
         int myleaf = -1;
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
             atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
             atomicExch(&a.ctl->err_info, grp);
         }
-        if (live) {
+        if (act) {
             a.ax[i] = valid ? acc.x : 0.0;
             a.ay[i] = valid ? acc.y : 0.0;
             a.az[i] = valid ? acc.z : 0.0;
@@ -428,7 +430,8 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         const int i = gd.x + lane;
         const bool live = lane < gd.y;
         const int root = gd.z;
-        const bool valid = live && a.m[i] != 0.0;
+        const bool act = live && (!a.active || a.active[i]);  // block steps walk the due particles only
+        const bool valid = act && a.m[i] != 0.0;
         // Group set-up in FP64 (positions, group centre, float offsets).  No FP64
         // value stays live past this block: on this part FP64 instructions issue
         // at 1/64 of the FP32 rate, so the compiler must not be able to
@@ -736,7 +739,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
             atomicExch(&a.ctl->err_info, grp);
         }
-        if (live) {
+        if (act) {
             a.ax[i] = valid ? (double)sx - (double)kx : 0.0;
             a.ay[i] = valid ? (double)sy - (double)ky : 0.0;
             a.az[i] = valid ? (double)sz - (double)kz : 0.0;
@@ -890,6 +893,7 @@ static WalkArgs walk_args(Ctx *c)
     a.gas = c->nd.gas; a.mvx = c->nd.mvx; a.mvy = c->nd.mvy; a.mvz = c->nd.mvz;
     a.radius = c->nd.radius;
     a.groups = c->groups;
+    a.active = c->walk_active;
     a.ngroups = c->ngroups;
     a.theta = c->prm.theta;
     a.e0 = c->prm.e0;

@@ -65,7 +65,9 @@ enum ag2_field {
     AG2_T = 7,     /* n  */
     AG2_U = 8,     /* n  internal energy */
     AG2_DUDT = 9,  /* n  */
-    AG2_VDENS = 10 /* n  visualDensity */
+    AG2_VDENS = 10, /* n  visualDensity */
+    AG2_TSTEP = 11, /* n  block time step of the particle (ag2_block_init) */
+    AG2_TNEXT = 12  /* n  its next integration time */
 };
 
 typedef struct ag2_params {
@@ -149,6 +151,19 @@ int ag2_step(ag2_ctx *ctx, double dt, double hubble_factor, int with_visual_dens
  * that outgrows it fails the step with AG2_E_NOMEM (redo it after a plain
  * ag2_build_tree, which grows the pool). */
 int ag2_step_graphs(ag2_ctx *ctx, int enable);
+/* Block time steps (Simulation.cpp:188-341 with minTimeStep < maxTimeStep).
+ * ag2_block_init gives every particle the step eta*sqrt(e0/|a|) clamped to
+ * [min_dt, max_dt] and floored to a power of two (min_dt when a = 0), from the
+ * current acc (after the initial ag2_forces), and its next integration time
+ * global_time + step.  Each ag2_block_step then: renews the steps of particles
+ * whose time has come; advances the global time to the earliest next
+ * integration time; kicks and drifts the particles due then; builds the tree,
+ * visual density (with_visual) and gas density over all particles; walks the
+ * due particles only; closes them (Ueuler for gas, position *= exp(H0*step),
+ * kick) and schedules their next time.  *global_time and *active return the new
+ * time and the number of due particles.  AG2_TSTEP / AG2_TNEXT read the state. */
+int ag2_block_init(ag2_ctx *ctx, double eta, double min_dt, double max_dt, double global_time);
+int ag2_block_step(ag2_ctx *ctx, double H0, int with_visual, double Rv, double *global_time, int64_t *active);
 
 /* Time the FP32 walk's compiled variants (register budget per thread, hence
  * warps resident per SM) on the current tree and keep the fastest for later

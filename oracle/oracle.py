@@ -184,3 +184,70 @@ def id_hash(ids) -> np.ndarray:
         z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
         z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
     return z ^ (z >> np.uint64(31))
+
+
+# ---- block time steps (Simulation.cpp:188-341), restated over the port -------
+
+
+def block_dt(acc, eta: float, e0: float, dmin: float, dmax: float) -> np.ndarray:
+    """Per-particle step (Simulation.cpp:196-206): eta*sqrt(e0/|a|) clamped to
+    [dmin, dmax], floored to a power of two, not below dmin; dmin for a = 0."""
+    acc = np.asarray(acc, np.float64)
+    a = np.sqrt(acc[:, 0] * acc[:, 0] + acc[:, 1] * acc[:, 1] + acc[:, 2] * acc[:, 2])  # vec3::length
+    ts = np.full(a.shape, dmin)
+    pos = a > 0
+    t = eta * np.sqrt(e0 / a[pos])
+    t = np.where(t < dmin, dmin, np.where(dmax < t, dmax, t))  # std::clamp
+    t = np.maximum(2.0 ** np.floor(np.log2(t)), dmin)  # std::max(std::pow(2, std::floor(std::log2(t))), min)
+    ts[pos] = t
+    return ts
+
+
+def _kick(vel, acc, ts, idx):
+    """TimeIntegration::Kick for the particles idx (skipped where acc has a NaN)."""
+    ok = idx[~np.isnan(acc[idx]).any(axis=1)]
+    vel[ok] = vel[ok] + acc[ok] * ts[ok, None] / 2
+    return vel
+
+
+def block_steps(world: World, type_, eta: float, dmin: float, dmax: float, e0: float, theta: float,
+                massInH: float, steps: int, t: float = 0.0, H0: float = 0.0, threads: int = 1):
+    """`steps` iterations of the reference's block-time-step loop
+    (Simulation.cpp:188-341) on the port, starting from the world's current acc
+    (after its initial forces).  Returns [(global time, particles integrated)]
+    and the final (step, next time) arrays."""
+    type_ = np.asarray(type_)
+    ts = block_dt(world.get("acc"), eta, e0, dmin, dmax)
+    tn = t + ts
+    log = []
+    for _ in range(steps):
+        due = t >= tn
+        if due.any():
+            ts[due] = block_dt(world.get("acc")[due], eta, e0, dmin, dmax)
+            tn[due] = t + ts[due]
+        t = float(tn.min())
+        act = np.nonzero(tn == t)[0].astype(np.int32)
+        acc, vel, pos = world.get("acc"), world.get("vel"), world.get("pos")
+        vel = _kick(vel, acc, ts, act)
+        pos[act] = pos[act] + vel[act] * ts[act, None]
+        world.set("vel", vel)
+        world.set("pos", pos)
+        world.build(threads)
+        if (type_ == 2).any():
+            world.gas_density(massInH)
+        world.forces_subset(e0, theta, act, threads)
+        acc, vel, pos = world.get("acc"), world.get("vel"), world.get("pos")
+        U, du = world.get("U"), world.get("dUdt")
+        g = act[type_[act] == 2]
+        gok = g[~np.isnan(du[g])]
+        U[gok] = U[gok] + du[gok] * ts[gok]
+        du[g] = 0.0
+        pos[act] = pos[act] * np.exp(H0 * ts[act])[:, None]
+        vel = _kick(vel, acc, ts, act)
+        tn[act] = tn[act] + ts[act]
+        world.set("U", U)
+        world.set("dUdt", du)
+        world.set("pos", pos)
+        world.set("vel", vel)
+        log.append((t, int(act.size)))
+    return log, ts, tn
