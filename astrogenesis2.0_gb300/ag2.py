@@ -34,8 +34,12 @@ EXPORTS = [
     "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
     "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
     "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy", "ag2_step_graphs",
-    "ag2_block_init", "ag2_block_step",
+    "ag2_block_init", "ag2_block_step", "ag2_set_tags", "ag2_get_tags", "ag2_snapshot_size",
+    "ag2_snapshot_encode", "ag2_snapshot_write", "ag2_snapshot_wait", "ag2_ic_count", "ag2_load_ics",
 ]
+
+# file formats of ag2_snapshot_* / ag2_load_ics (the reference's format names)
+FORMATS = {"ag": 0, "agc": 1, "age": 2, "gadget": 3, "makeGal": 4}
 
 
 class Params(ctypes.Structure):
@@ -107,6 +111,15 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_phase_times.argtypes = [P, I, P, P]
     L.ag2_launch_count.argtypes = [P]
     L.ag2_launch_count.restype = ctypes.c_int64
+    L.ag2_set_tags.argtypes = [P, P, P, P, I]
+    L.ag2_get_tags.argtypes = [P, P, P, P, I]
+    L.ag2_snapshot_size.argtypes = [P, I, ctypes.c_int64, ctypes.POINTER(ctypes.c_size_t)]
+    L.ag2_snapshot_encode.argtypes = [P, I, ctypes.c_int64, D, D, D, P, ctypes.c_size_t,
+                                      ctypes.POINTER(ctypes.c_size_t)]
+    L.ag2_snapshot_write.argtypes = [P, I, ctypes.c_int64, D, D, D, ctypes.c_char_p, I]
+    L.ag2_snapshot_wait.argtypes = [P]
+    L.ag2_ic_count.argtypes = [ctypes.c_char_p, I, ctypes.POINTER(ctypes.c_int64)]
+    L.ag2_load_ics.argtypes = [P, ctypes.c_char_p, I, P]
     _lib = L
     return L
 
@@ -321,6 +334,61 @@ class Context:
     def launches(self) -> int:
         return int(self.L.ag2_launch_count(self.h))
 
+    # -- snapshot and initial-condition files (DataManager) --------------------
+    def set_tags(self, id=None, galaxy_part=None, sfr=None):
+        """Particle::id, galaxyPart and sfr in upload order (None: unchanged)."""
+        a = None if id is None else np.ascontiguousarray(id, np.uint32)
+        b = None if galaxy_part is None else np.ascontiguousarray(galaxy_part, np.uint8)
+        c = None if sfr is None else np.ascontiguousarray(sfr, np.float64)
+        for x in (a, b, c):
+            if x is not None and x.size != self.n:
+                raise ValueError("tags need one value per particle")
+        self._check(self.L.ag2_set_tags(self.h, _ptr(a), _ptr(b), _ptr(c), 0))
+
+    def tags(self) -> dict:
+        out = {"id": np.empty(self.n, np.uint32), "gp": np.empty(self.n, np.uint8), "sfr": np.empty(self.n)}
+        self._check(self.L.ag2_get_tags(self.h, _ptr(out["id"]), _ptr(out["gp"]), _ptr(out["sfr"]), 0))
+        return out
+
+    def snapshot_size(self, fmt: str, count: int | None = None) -> int:
+        """Bytes of the snapshot image (an upper bound for gadget)."""
+        cap = ctypes.c_size_t()
+        self._check(self.L.ag2_snapshot_size(self.h, FORMATS[fmt], self.n if count is None else count,
+                                             ctypes.byref(cap)))
+        return cap.value
+
+    def snapshot_bytes(self, fmt: str, count: int | None = None, delta_time: float = 0.0, end_time: float = 0.0,
+                       current_time: float = 0.0, out: np.ndarray | None = None):
+        """DataManager::saveData's file image of the first `count` particles:
+        bytes, or its length when encoded into `out` (a uint8 array, e.g.
+        pinned memory)."""
+        count = self.n if count is None else count
+        buf = np.empty(max(self.snapshot_size(fmt, count), 1), np.uint8) if out is None else out
+        ln = ctypes.c_size_t()
+        self._check(self.L.ag2_snapshot_encode(self.h, FORMATS[fmt], count, delta_time, end_time, current_time,
+                                               _ptr(buf), buf.nbytes, ctypes.byref(ln)))
+        return buf[: ln.value].tobytes() if out is None else ln.value
+
+    def snapshot_write(self, path: str, fmt: str, count: int | None = None, delta_time: float = 0.0,
+                       end_time: float = 0.0, current_time: float = 0.0, wait: bool = True):
+        """Write the snapshot file; with wait=False the file is written in the
+        background (snapshot_wait collects the status)."""
+        count = self.n if count is None else count
+        self._check(self.L.ag2_snapshot_write(self.h, FORMATS[fmt], count, delta_time, end_time, current_time,
+                                              str(path).encode(), 0 if wait else 1))
+
+    def snapshot_wait(self):
+        self._check(self.L.ag2_snapshot_wait(self.h))
+
+    def load_ics(self, path: str, fmt: str):
+        """DataManager::loadICs into the context; returns the header's
+        (deltaTime, endTime, currentTime) or (0, 0, time)."""
+        t = np.zeros(3)
+        self._check(self.L.ag2_load_ics(self.h, str(path).encode(), FORMATS[fmt], _ptr(t)))
+        self.n = int(self.L.ag2_count(self.h))
+        return tuple(t)
+
+
     def topology(self) -> dict:
         nn, _, _ = self.node_count()
         t = {
@@ -333,3 +401,13 @@ class Context:
                  "radius"]
         self._check(self.L.ag2_topology(self.h, *[_ptr(t[k]) for k in order]))
         return t
+
+
+def ic_count(path: str, fmt: str) -> int:
+    """Particle count in an initial-condition file's header."""
+    L = load()
+    n = ctypes.c_int64()
+    rc = L.ag2_ic_count(str(path).encode(), FORMATS[fmt], ctypes.byref(n))
+    if rc != OK:
+        raise AG2Error(rc, "cannot read the header of " + str(path))
+    return n.value

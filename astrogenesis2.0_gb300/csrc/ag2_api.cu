@@ -197,6 +197,8 @@ bool realloc_dev(T *&p, size_t n)
     return cudaMalloc((void **)&p, (n ? n : 1) * sizeof(T)) == cudaSuccess;
 }
 
+}  // namespace
+
 int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const double *mass, const double *U,
                   const uint8_t *type)
 {
@@ -215,8 +217,6 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
     if (c->ctl_host->err_code == AG2_E_NAN) return set_err(c, AG2_E_NAN, "non-finite particle position");
     return AG2_OK;
 }
-
-}  // namespace
 
 // Upload the instance tables and walk groups when the instance layout changed.
 int ensure_instance_tables(Ctx *c)
@@ -313,7 +313,6 @@ int ensure_instance_tables(Ctx *c)
 
 using namespace ag2;
 
-struct ag2_ctx : public ag2::Ctx {};
 
 extern "C" {
 
@@ -366,6 +365,8 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
          cudaMalloc(&c->leaves, (cap + kLeafListSpare) * 4) == cudaSuccess &&
          cudaMalloc(&c->lroots, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->pkey, 6 * cap * sizeof(int64_t)) == cudaSuccess &&
+         cudaMalloc(&c->tag_id, cap * 4) == cudaSuccess && cudaMalloc(&c->tag_gp, cap) == cudaSuccess &&
+         cudaMalloc(&c->tag_sfr, cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->ctl, sizeof(Ctx::Ctl)) == cudaSuccess &&
          cudaMallocHost(&c->ctl_host, sizeof(Ctx::Ctl)) == cudaSuccess;
     if (ok) ok = ensure_node_capacity(c, 4 * cap + 1024) == AG2_OK;
@@ -384,6 +385,7 @@ int ag2_destroy(ag2_ctx *c)
 {
     if (!c) return AG2_E_INVALID;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    io_release(c);
     free_particles(c->st[0]);
     free_particles(c->st[1]);
     free_nodes(c->nd);
@@ -454,7 +456,8 @@ int ag2_upload(ag2_ctx *c, size_t n, const double *pos, const double *vel, const
     AG2_CUDA(c, cudaMemcpyAsync(spare.m, mass, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     if (U) AG2_CUDA(c, cudaMemcpyAsync(spare.U, U, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     AG2_CUDA(c, cudaMemcpyAsync(c->staging_u8, type, n, cudaMemcpyHostToDevice, c->stream));
-    return upload_common(c, n, pos_d, vel_d, spare.m, U ? spare.U : nullptr, c->staging_u8);
+    int rc = upload_common(c, n, pos_d, vel_d, spare.m, U ? spare.U : nullptr, c->staging_u8);
+    return rc ? rc : io_reset_tags(c, n);
 }
 
 int ag2_upload_device(ag2_ctx *c, size_t n, const double *pos, const double *vel, const double *mass,
@@ -468,7 +471,8 @@ int ag2_upload_device(ag2_ctx *c, size_t n, const double *pos, const double *vel
         c->have_tree = false;
         return AG2_OK;
     }
-    return upload_common(c, n, pos, vel, mass, U, type);
+    int rc = upload_common(c, n, pos, vel, mass, U, type);
+    return rc ? rc : io_reset_tags(c, n);
 }
 
 int ag2_set_field(ag2_ctx *c, int f, const double *src, int src_is_device)

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ag2.h"
@@ -90,6 +91,28 @@ struct Ctx {
     double blk_eta = 0, blk_dmin = 0, blk_dmax = 0, blk_t = 0;
     long long *blk_key = nullptr;  // device: earliest next integration time (ordered key)
     int32_t *blk_count = nullptr;  // device: due particles
+
+    // Per-particle values that ride along unchanged, in upload order:
+    // Particle::id, galaxyPart (1 disk, 2 bulge, 3 halo) and sfr
+    uint32_t *tag_id = nullptr;
+    uint8_t *tag_gp = nullptr;
+    double *tag_sfr = nullptr;
+    // snapshot / initial-condition files: the file image on the device (with
+    // slack after its end), its pinned host copy, scratch (inverse permutation,
+    // per-block counts) and the background writer of the last snapshot
+    uint8_t *io_dev = nullptr;
+    size_t io_dev_cap = 0;
+    uint8_t *io_host = nullptr;
+    size_t io_host_cap = 0;
+    int32_t *io_scratch = nullptr;
+    size_t io_scratch_cap = 0;
+    int64_t *io_len_dev = nullptr;   // image length computed on the device
+    int64_t *io_len_host = nullptr;  // pinned
+    cudaStream_t io_stream = nullptr;
+    cudaEvent_t io_event = nullptr;
+    std::thread io_thread;
+    int io_status = 0;
+    std::string io_err;
     const uint8_t *walk_active = nullptr;  // per slot: walk it (null = every particle)
     size_t inst_R_pin_cap = 0;
     int64_t graph_epoch = 0;             // bumped when the particle set, layout or parameters change
@@ -304,6 +327,8 @@ int run_energy(Ctx *c, double *out4);
 int run_block_init(Ctx *c, double eta, double dmin, double dmax, double t);
 int run_block_step(Ctx *c, double H0, int with_visual, double Rv, double *t_out, int64_t *active_out);
 int run_fma_probe(Ctx *c, double *gflops);
+int io_reset_tags(Ctx *c, size_t n);
+void io_release(Ctx *c);
 int run_autotune(Ctx *c, int *chosen);
 
 // physical constants of the reference (Constants.h:14-15, Particle.h:40)
@@ -313,3 +338,7 @@ constexpr double kProton = 1.6726219e-27;
 constexpr double kPi = 3.14159265358979323846;
 
 }  // namespace ag2
+
+// the opaque handle of the C interface
+struct ag2_ctx : public ag2::Ctx {};
+

@@ -32,10 +32,13 @@
 // visualDensity` and `uint8_t type`.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <filesystem>
 #include <iostream>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "ag2.h"
@@ -259,5 +262,55 @@ public:
         particle->dUdt = 0;
     }
 };
+
+// DataManager's formats by the names of its outputDataFormat / inputDataFormat
+// keys (DataManager.cpp:100-110, 446-580); -1 for anything else ("hdf5" is not
+// implemented by the reference either).
+inline int format_code(const std::string &name)
+{
+    if (name == "ag") return AG2_FMT_AG;
+    if (name == "agc") return AG2_FMT_AGC;
+    if (name == "age") return AG2_FMT_AGE;
+    if (name == "gadget") return AG2_FMT_GADGET;
+    if (name == "makeGal") return AG2_FMT_MAKEGAL;
+    return -1;
+}
+
+// DataManager::saveData (DataManager.cpp:86-118) for an engine whose particles
+// are resident in a context: creates outputPath if needed and writes
+// outputPath + std::to_string(timeStep) + "." + outputFormat holding the first
+// numberOfParticles particles; with async the file is written in the
+// background (ag2_snapshot_wait collects the status).
+inline int save_snapshot(ag2_ctx *ctx, const std::string &outputPath, const std::string &outputFormat, int timeStep,
+                         int numberOfParticles, double deltaTime, double endTime, double currentTime,
+                         bool async = true)
+{
+    const int fmt = format_code(outputFormat);
+    if (fmt < 0 || fmt == AG2_FMT_MAKEGAL) {
+        std::cerr << "Unknown output data format: " << outputFormat << std::endl;
+        return last_status_ref() = AG2_E_FORMAT;
+    }
+    std::error_code ec;
+    std::filesystem::create_directories(outputPath, ec);
+    const std::string file = outputPath + std::to_string(timeStep) + "." + outputFormat;
+    const int64_t count = std::min<int64_t>(numberOfParticles, (int64_t)ag2_count(ctx));
+    const int rc = ag2_snapshot_write(ctx, fmt, count, deltaTime, endTime, currentTime, file.c_str(), async ? 1 : 0);
+    if (rc != AG2_OK) std::cerr << "Error opening datafile: " << file << " (" << ag2_last_error_string(ctx) << ")" << std::endl;
+    return last_status_ref() = rc;
+}
+
+// DataManager::loadICs (DataManager.cpp:434-1332) into a context.  The
+// reference opens "../../input_data/" + inputPath; pass the resolved path.
+inline int load_ics(ag2_ctx *ctx, const std::string &path, const std::string &inputFormat)
+{
+    const int fmt = format_code(inputFormat);
+    if (fmt < 0) {
+        std::cout << "invalid input data format: " << inputFormat << std::endl;
+        return last_status_ref() = AG2_E_FORMAT;
+    }
+    const int rc = ag2_load_ics(ctx, path.c_str(), fmt, nullptr);
+    if (rc != AG2_OK) std::cerr << "Error reading initial conditions " << path << ": " << ag2_last_error_string(ctx) << std::endl;
+    return last_status_ref() = rc;
+}
 
 }  // namespace ag2host

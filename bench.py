@@ -251,6 +251,90 @@ def config_block(args, wl, d, walk=None, split_threshold=100):
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+# bytes a snapshot encode moves per particle in HBM: the fields the record
+# holds (read) plus the record (written) plus the inverse permutation (read the
+# tree-order ids, write and read the inverse)
+IO_READ_BYTES = {"age": 24 + 24 + 5 * 8 + 1 + 1 + 4, "ag": 24 + 4 * 8 + 1 + 1 + 4, "agc": 24 + 3 * 8 + 1 + 1}
+IO_REC_BYTES = {"age": 94, "ag": 62, "agc": 26}
+
+
+def io_leg(ctx, d, reps, fmt="age"):
+    """Snapshot writer and initial-condition loader (DataManager::saveData /
+    loadICs) on the bench's particles: device encode and decode times (phase
+    events on the context's stream), end-to-end rates through the C-ABI with a
+    pinned host buffer and a file, and the numpy restatement timed on one core
+    as the CPU baseline."""
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    import snapio
+
+    n = ctx.n
+    size = ctx.snapshot_size(fmt)
+    buf = torch.empty(size, dtype=torch.uint8).pin_memory().numpy()
+    ctx.phase_timing(True)
+    enc, cpy, wall = [], [], []
+    for k in range(reps + 1):
+        t0 = time.perf_counter()
+        ln = ctx.snapshot_bytes(fmt, None, 1.0, 2.0, 3.0, out=buf)
+        t1 = time.perf_counter()
+        ph = dict(ctx.phase_times())
+        if k:
+            enc.append(ph["snapshot encode"])
+            cpy.append(ph["snapshot copy"])
+            wall.append(t1 - t0)
+    assert ln == size
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "snap." + fmt)
+        t0 = time.perf_counter()
+        ctx.snapshot_write(path, fmt, None, 1.0, 2.0, 3.0, wait=False)
+        t_queue = time.perf_counter() - t0
+        ctx.snapshot_wait()
+        t_write = time.perf_counter() - t0
+        ic_copy, ic_dec, ic_wall = [], [], []
+        for k in range(reps + 1):
+            t0 = time.perf_counter()
+            ctx.load_ics(path, fmt)
+            t1 = time.perf_counter()
+            ph = dict(ctx.phase_times())
+            if k:
+                ic_copy.append(ph["ic copy"])
+                ic_dec.append(ph["ic decode"])
+                ic_wall.append(t1 - t0)
+    ctx.phase_timing(False)
+    # the numpy restatement on a sample, one core
+    ns = min(n, 1 << 20)
+    p = {"pos": np.asarray(d["pos"][:ns]).reshape(-1, 3), "vel": np.asarray(d["vel"][:ns]).reshape(-1, 3),
+         "mass": d["mass"][:ns], "T": np.zeros(ns), "P": np.zeros(ns), "vdens": np.zeros(ns), "U": d["U"][:ns],
+         "sfr": np.zeros(ns), "type": d["type"][:ns].astype(np.uint8), "gp": np.ones(ns, np.uint8),
+         "id": np.arange(ns, dtype=np.uint32)}
+    t0 = time.perf_counter()
+    img = snapio.encode(snapio.NAMES[fmt], p, ns, 1.0, 2.0, 3.0)
+    t_cpu_enc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    snapio.decode(snapio.NAMES[fmt], img)
+    t_cpu_dec = time.perf_counter() - t0
+    med = lambda v: float(np.median(v))  # noqa: E731
+    hbm = n * (IO_READ_BYTES[fmt] + IO_REC_BYTES[fmt] + 12) / (med(enc) * 1e-3) / 1e9
+    return {
+        "format": fmt, "particles": n, "file_bytes": size,
+        "snapshot": {"encode_ms": med(enc), "copy_ms": med(cpy), "e2e_ms": med(wall) * 1e3,
+                     "e2e_gbs": size / med(wall) / 1e9, "d2h_gbs": size / (med(cpy) * 1e-3) / 1e9,
+                     "file_async_return_ms": t_queue * 1e3, "file_write_ms": t_write * 1e3,
+                     "roofline": {"bound": "hbm", "achieved": hbm, "peak": HBM_PEAK_GBS, "unit": "GB/s",
+                                  "frac": hbm / HBM_PEAK_GBS,
+                                  "bytes_per_particle": IO_READ_BYTES[fmt] + IO_REC_BYTES[fmt] + 12,
+                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}},
+        "load": {"h2d_ms": med(ic_copy), "decode_ms": med(ic_dec), "e2e_ms": med(ic_wall) * 1e3,
+                 "e2e_gbs": size / med(ic_wall) / 1e9, "h2d_gbs": size / (med(ic_copy) * 1e-3) / 1e9},
+        "cpu_baseline": {"unit": "GB/s", "encode": len(img) / t_cpu_enc / 1e9, "decode": len(img) / t_cpu_dec / 1e9,
+                         "cores": 1, "kind": "port",
+                         "sample": f"numpy restatement (oracle/snapio.py) on the first {ns} particles"},
+    }
+
+
 def our_arm(args, wl, d):
     import numpy as np
     import torch
@@ -448,6 +532,8 @@ def our_arm(args, wl, d):
                "h2d_bytes_per_step": int(n * (24 + 24 + 8 + 8 + 1 + 24)),
                "d2h_bytes_per_step": int(n * (24 + 24 + 24 + 8))}
 
+    io = io_leg(ctx, d, args.io_reps) if args.io_reps > 0 and D.rank == 0 else None
+
     # independent simulations: each one stepped on its own (its own context and
     # launches), with the plain FP64 walk and with the FP32 walk
     per_launch = None
@@ -499,6 +585,7 @@ def our_arm(args, wl, d):
             "force_error": force_error,
             "energy_drift": drift,
             "step_graph": graph,
+            "io": io,
         }
         if per_launch:
             out["one_sim_per_launch"] = per_launch
@@ -735,6 +822,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--graph-steps", type=int, default=10)
+    ap.add_argument("--io-reps", type=int, default=3)
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rates", default="10,50,200")
     args = ap.parse_args()

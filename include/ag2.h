@@ -44,7 +44,9 @@ enum ag2_status {
     AG2_E_DEPTH = -5,       /* octree deeper than AG2_MAX_DEPTH levels */
     AG2_E_STACK = -6,       /* walk stack overflow (reported by the kernel, no fault) */
     AG2_E_NAN = -7,         /* non-finite particle position */
-    AG2_E_CAPACITY = -8     /* more particles than the context was created for */
+    AG2_E_CAPACITY = -8,    /* more particles than the context was created for */
+    AG2_E_FORMAT = -9,      /* unknown format, or a file the reference's reader rejects or reads past its end */
+    AG2_E_IO = -10          /* a file could not be opened, read or written */
 };
 
 #define AG2_MAX_DEPTH 96
@@ -229,6 +231,60 @@ int ag2_fp32_peak_probe(ag2_ctx *ctx, double *gflops);
  * nothing. */
 #define AG2_NOALLOC_MAX_PARTICLES 8355840
 int ag2_root_radius_noalloc(const double *pos, int64_t n, double *radius, void *stream);
+
+/* Snapshot and initial-condition files of the reference's DataManager
+ * (File/DataManager.h:13-91, DataManager.cpp:86-1337).  The formats are the
+ * values of its outputDataFormat / inputDataFormat keys: */
+enum ag2_format {
+    AG2_FMT_AG = 0,      /* "ag": FP64 records (position, mass, T, visualDensity, sfr, type, galaxyPart, id) */
+    AG2_FMT_AGC = 1,     /* "agc": FP32 records (position, visualDensity, sfr, T, type, galaxyPart) */
+    AG2_FMT_AGE = 2,     /* "age": FP64 records (position, velocity, mass, T, P, visualDensity, U, type, galaxyPart, id) */
+    AG2_FMT_GADGET = 3,  /* "gadget": Gadget-2 format 1 (kpc, km/s, 1e10 Msun, U / 1e6) */
+    AG2_FMT_MAKEGAL = 4  /* "makeGal": Gadget-2 format 2 with block labels (input only) */
+};
+
+/* Per-particle values that the hot path carries along unchanged, in upload
+ * order: Particle::id, Particle::galaxyPart (1 disk, 2 bulge, 3 halo) and
+ * Particle::sfr.  ag2_upload sets id = upload index, galaxyPart = 1, sfr = 0;
+ * ag2_load_ics sets what the file holds.  NULL arguments are left alone. */
+int ag2_set_tags(ag2_ctx *ctx, const uint32_t *id, const uint8_t *galaxy_part, const double *sfr, int src_is_device);
+int ag2_get_tags(ag2_ctx *ctx, uint32_t *id, uint8_t *galaxy_part, double *sfr, int dst_is_device);
+
+/* DataManager::saveData (DataManager.cpp:86-424) of the first `count`
+ * particles in upload order (numParticlesOutput; count <= ag2_count).  The
+ * file image is encoded on the device from the resident state, byte for byte
+ * the reference's layout; the 4 padding bytes of the ag/agc/age header, which
+ * the reference leaves uninitialised, are zero.  Gadget ignores delta_time and
+ * end_time and stores current_time as the header's time.
+ * ag2_snapshot_size: bytes of the image (exact for ag/agc/age, an upper bound
+ * for gadget, whose particle lists depend on type and galaxyPart).
+ * ag2_snapshot_encode: the image into host memory dst (dst_cap bytes), *len =
+ * its length; synchronous.
+ * ag2_snapshot_write: the image into the file `path`.  With async = 1 the call
+ * returns once the encode and the device-to-host copy are queued; a background
+ * thread waits for the copy and writes the file while later calls run on the
+ * device.  With ag2_phase_timing on, ag2_snapshot_encode records the phases
+ * "snapshot encode" and "snapshot copy", ag2_load_ics "ic copy" and "ic decode".  ag2_snapshot_wait joins it and returns the write's status; the next
+ * snapshot, ag2_load_ics and ag2_destroy join it first. */
+int ag2_snapshot_size(ag2_ctx *ctx, int format, int64_t count, size_t *bytes);
+int ag2_snapshot_encode(ag2_ctx *ctx, int format, int64_t count, double delta_time, double end_time,
+                        double current_time, void *dst, size_t dst_cap, size_t *len);
+int ag2_snapshot_write(ag2_ctx *ctx, int format, int64_t count, double delta_time, double end_time,
+                       double current_time, const char *path, int async);
+int ag2_snapshot_wait(ag2_ctx *ctx);
+
+/* DataManager::loadICs (DataManager.cpp:434-1332) into the context: the file
+ * is read once into pinned memory, copied to the device as it is, and decoded
+ * there into the particle arrays (as ag2_upload does, plus T, P,
+ * visualDensity and the tags where the format holds them), in file order.
+ * The reference's own units conversions apply (gadget and makeGal: kpc, km/s,
+ * 1e10 Msun, U * 1e6).  The reference's makeGal reader shuffles the particles
+ * with an unseeded generator and Simulation::init shuffles again; neither
+ * shuffle is done here.  times3 (may be NULL) receives the header's
+ * deltaTime, endTime and currentTime (ag/agc/age) or 0, 0, time (gadget,
+ * makeGal).  ag2_ic_count reads the particle count of a file's header. */
+int ag2_ic_count(const char *path, int format, int64_t *n);
+int ag2_load_ics(ag2_ctx *ctx, const char *path, int format, double *times3);
 
 /* Number of kernels this library launched since the context was created. */
 int64_t ag2_launch_count(const ag2_ctx *ctx);

@@ -23,6 +23,9 @@
 #include "Simulation.h"
 #include "Tree.h"
 #include "TimeIntegration.h"
+#include "DataManager.h"
+
+#include <unistd.h>
 
 struct orc_world {
     Simulation *sim = nullptr;
@@ -309,6 +312,78 @@ void orc_direct_sum(int n, const double *pos, const double *mass, double e0, dou
         out[3 * k + 1] = probe.acc.y;
         out[3 * k + 2] = probe.acc.z;
     }
+}
+
+// DataManager::saveData on particles given as arrays (upload order): writes
+// <dir><timeStep>.<format> exactly as the reference does.
+int orc_ref_save(const char *dir, const char *format, int n, int count, const double *pos, const double *vel,
+                 const double *mass, const double *T, const double *P, const double *vdens, const double *U,
+                 const double *sfr, const uint8_t *type, const uint8_t *gp, const uint32_t *id, int timeStep,
+                 double dt, double endTime, double t)
+{
+    DataManager dm(dir);
+    dm.outputFormat = format;
+    std::vector<Particle *> ps(n);
+    for (int i = 0; i < n; i++) {
+        Particle *q = new Particle();
+        q->position = vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        q->velocity = vec3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+        q->mass = mass[i];
+        q->T = T[i];
+        q->P = P[i];
+        q->visualDensity = vdens[i];
+        q->U = U[i];
+        q->sfr = sfr[i];
+        q->type = type[i];
+        q->galaxyPart = gp[i];
+        q->id = id[i];
+        ps[i] = q;
+    }
+    dm.saveData(ps, timeStep, 0, count, dt, endTime, t);
+    for (Particle *q : ps) delete q;
+    return 0;
+}
+
+// DataManager::loadICs of <workdir>/../../input_data/<name>: the reader opens
+// "../../input_data/" + inputPath relative to the working directory, which is
+// switched to workdir for the call.  Copies up to cap particles out, returns
+// their number and sets *ok to the reader's return value (its makeGal branch
+// fills the particles and then returns false, DataManager.cpp:580-809, 1331).
+int orc_ref_load(const char *workdir, const char *name, const char *format, int cap, double *pos, double *vel,
+                 double *mass, double *T, double *P, double *vdens, double *U, double *sfr, uint8_t *type,
+                 uint8_t *gp, uint32_t *id, int *ok_out)
+{
+    char old[4096];
+    if (!getcwd(old, sizeof old) || chdir(workdir) != 0) return -2;
+    DataManager dm("");
+    dm.inputPath = name;
+    dm.inputFormat = format;
+    Simulation *sim = new Simulation();
+    std::vector<Particle *> ps;
+    const bool ok = dm.loadICs(ps, sim);
+    if (chdir(old) != 0) return -2;
+    *ok_out = ok ? 1 : 0;
+    const int n = (int)ps.size();
+    for (int i = 0; i < n && i < cap; i++) {
+        const Particle *q = ps[i];
+        pos[3 * i] = q->position.x;
+        pos[3 * i + 1] = q->position.y;
+        pos[3 * i + 2] = q->position.z;
+        vel[3 * i] = q->velocity.x;
+        vel[3 * i + 1] = q->velocity.y;
+        vel[3 * i + 2] = q->velocity.z;
+        mass[i] = q->mass;
+        T[i] = q->T;
+        P[i] = q->P;
+        vdens[i] = q->visualDensity;
+        U[i] = q->U;
+        sfr[i] = q->sfr;
+        type[i] = q->type;
+        gp[i] = q->galaxyPart;
+        id[i] = q->id;
+    }
+    for (Particle *q : ps) delete q;
+    return n;
 }
 
 } // extern "C"
