@@ -767,9 +767,15 @@ __device__ __forceinline__ double div_back(double x, double m, double q)
 }
 
 // node record shared by leaves and internal nodes: moments, FP32 walk records
+// what the FP32 walk records need beyond a node's moments
+struct RecArgs {
+    double theta;
+    const double *inst_R;  // root half-width per instance (walk_scale)
+};
+
 __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particles &P, const Sums &tot, double mass,
                                            double cx, double cy, double cz, double gas, double mvx, double mvy,
-                                           double mvz, int32_t ng, uint8_t cmask, bool leaf, int32_t lp, double theta)
+                                           double mvz, int32_t ng, uint8_t cmask, bool leaf, int32_t lp, RecArgs ra)
 {
     nd.tm[nid] = tot.m;
     nd.tmx[nid] = tot.mx;
@@ -792,20 +798,25 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     nd.mvy[nid] = mvy;
     nd.mvz[nid] = mvz;
     nd.ngas[nid] = ng;
-    // FP32 walk record: COM split into hi + lo floats
-    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
-    const float lx = (float)(cx - (double)hx), ly = (float)(cy - (double)hy), lz = (float)(cz - (double)hz);
-    nd.wA[nid] = make_float4(hx, hy, hz, (float)mass);
+    // FP32 walk record, lengths in the instance's scaled units (walk_scale):
+    // COM split into hi + lo floats, mass * ls^2 (the walk's accelerations come
+    // out in the caller's units), (radius/theta)^2, gasMass * ls^2 (the FP32
+    // SPH pair's scaled mass); velocities as they are
+    const double ls = walk_scale(ra.inst_R[nd.inst[nid]]), ls2 = ls * ls;
+    const double sx = cx * ls, sy = cy * ls, sz = cz * ls;
+    const float hx = (float)sx, hy = (float)sy, hz = (float)sz;
+    const float lx = (float)(sx - (double)hx), ly = (float)(sy - (double)hy), lz = (float)(sz - (double)hz);
+    nd.wA[nid] = make_float4(hx, hy, hz, (float)(mass * ls2));
     float mac = -1.0f;
     if (!leaf) {
-        const double q = nd.radius[nid] / theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
+        const double q = nd.radius[nid] * ls / ra.theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
         mac = (float)(q * q);
     }
     nd.wB[nid] = make_float4(lx, ly, lz, mac);
     if (leaf && lp >= 0)
-        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)gas);
+        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)(gas * ls2));
     else
-        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)gas);
+        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)(gas * ls2));
 }
 
 // Moments from the node's own mass set: the centre of mass and gas velocity as
@@ -846,7 +857,7 @@ __device__ __forceinline__ void finish_sums(Nodes &nd, int64_t nid, uint8_t mode
 template <class Idx>
 __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Particles &P, Idx idx,
                                              const double *gas_prefix, const int32_t *gas_off,
-                                             const uint8_t *gas_uni, double theta)
+                                             const uint8_t *gas_uni, RecArgs ra)
 {
     const int32_t cnt = nd.count[nid], ndrop = nd.ndrop[nid];
     const uint8_t mode = nd.mode[nid];
@@ -895,7 +906,7 @@ __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Parti
                 cx = cy = cz = 0.0;
             }
         }
-        store_node(nd, nid, P, t, mp, cx, cy, cz, t.g, mvx, mvy, mvz, t.ng, 0, true, i, theta);
+        store_node(nd, nid, P, t, mp, cx, cy, cz, t.g, mvx, mvy, mvz, t.ng, 0, true, i, ra);
         return;
     }
     Sums tot, own;  // tot: whole routed range; own: the reference's mass set
@@ -945,7 +956,7 @@ __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Parti
     } else {
         finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
     }
-    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, 0, true, lp, theta);
+    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, 0, true, lp, ra);
 }
 
 // Internal-node moments after its children's: sums over the children in octant
@@ -954,7 +965,7 @@ __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Parti
 template <class Idx>
 __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const Particles &P, Idx idx,
                                                  const double *gas_prefix, const int32_t *gas_off,
-                                                 const uint8_t *gas_uni, double theta)
+                                                 const uint8_t *gas_uni, RecArgs ra)
 {
     const int32_t cnt = nd.count[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
     const uint8_t mode = nd.mode[nid];
@@ -972,21 +983,21 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
     if (mode == MODE_PAR) own = tot;  // the parallel path sums escapers too (Node.cpp:477-499)
     double mass, cx, cy, cz, gas, mvx, mvy, mvz;
     finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
-    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, theta);
+    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, ra);
 }
 
 // Leaves (every level at once), on the state in tree order.  -1 entries pad
 // the list's per-warp stretches.
 __global__ void __launch_bounds__(kBlock) k_moments_leaf(const Ctx::Ctl *ctl, const int32_t *__restrict__ list,
                                                          Nodes nd, Particles P, const double *gas_prefix,
-                                                         const int32_t *gas_off, const uint8_t *gas_uni, double theta)
+                                                         const int32_t *gas_off, const uint8_t *gas_uni, RecArgs ra)
 {
     const int nleaf = ctl->nleaf;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nleaf; t += gridDim.x * blockDim.x) {
         const int64_t nid = list[t];
         if (nid < 0) continue;
         const int32_t start = nd.start[nid];
-        moments_leaf(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+        moments_leaf(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, ra);
     }
 }
 
@@ -996,7 +1007,7 @@ template <bool kDev>
 __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list,
                                                         const Ctx::Ctl *ctl, Nodes nd, Particles P,
                                                         const double *gas_prefix, const int32_t *gas_off,
-                                                        const uint8_t *gas_uni, double theta)
+                                                        const uint8_t *gas_uni, RecArgs ra)
 {
     if (kDev) {
         const int L = ctl->mlev;
@@ -1007,7 +1018,7 @@ __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt_lvl; t += gridDim.x * blockDim.x) {
         const int64_t nid = list[t];
         const int32_t start = nd.start[nid];
-        moments_internal(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, theta);
+        moments_internal(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, ra);
     }
 }
 
@@ -1870,7 +1881,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     // deepest first (the internal-node list bucketed by level)
     const unsigned gl = capture ? fixed_grid : std::max(1u, grid_for(c->nleaves, kBlock));
     AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, c->ctl, c->leaves, c->nd, c->S(), c->gas_prefix, c->gas_off,
-               c->gas_uni, c->prm.theta);
+               c->gas_uni, RecArgs{c->prm.theta, c->inst_R});
     const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
     AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint);
     if (capture) {
@@ -1883,7 +1894,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil);
         rc = capture_while(c, h, [&]() -> int {
             AG2_LAUNCH(c, k_moments_int<true>, fixed_grid, kBlock, 0, 0, c->nd.lil, c->ctl, c->nd, c->S(),
-                       c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+                       c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{c->prm.theta, c->inst_R});
             AG2_LAUNCH(c, k_mlev_next, 1, 32, 0, c->ctl, h, 1);
             return AG2_OK;
         });
@@ -1899,7 +1910,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             const int32_t cnt = c->lvl_cnt_h[L];
             if (!cnt) continue;
             AG2_LAUNCH(c, k_moments_int<false>, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.lil + c->lvl_start_h[L],
-                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, c->prm.theta);
+                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{c->prm.theta, c->inst_R});
         }
     }
     phase_mark(c, "build: moments");

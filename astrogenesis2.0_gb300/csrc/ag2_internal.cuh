@@ -275,6 +275,19 @@ __host__ __device__ inline int64_t okey(double x)
     return b >= 0 ? (int64_t)b : (int64_t)(b ^ 0x7FFFFFFFFFFFFFFFLL);
 }
 
+// Power-of-two length scale of an instance's FP32 walk: 2^-e for the root
+// half-width R = f * 2^e, f in [0.5, 1) (1 when R is 0 or not finite).  The
+// walk records and the walk's offsets are in units of 2^e: scaling by a power
+// of two is exact, and it keeps r^2, (radius/theta)^2 and h^4 inside FP32's
+// range in any unit system (the reference works in SI, positions ~1e20 m).
+__host__ __device__ inline double walk_scale(double R)
+{
+    if (!(R > 0.0) || !(R < 1.0e308)) return 1.0;
+    int e = 0;
+    frexp(R, &e);
+    return ldexp(1.0, -e);
+}
+
 // entries of the leaf list beyond one per particle: the unused tails of the
 // build's per-warp stretches
 constexpr size_t kLeafListSpare = size_t(1) << 22;

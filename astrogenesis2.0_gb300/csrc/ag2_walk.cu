@@ -52,6 +52,7 @@ struct WalkArgs {
     const int4 *groups;  // (first slot, lanes, instance = root node, 0)
     int ngroups;
     const uint8_t *active;  // per slot: walk it (block time steps); null = every particle
+    const double *inst_R;   // root half-width per instance: the FP32 walk's length scale (walk_scale)
     double theta, e0, G;
     Ctx::Ctl *ctl;
 };
@@ -132,6 +133,41 @@ __device__ __forceinline__ void sph_pair(F gm, F dx, F dy, F dz, F r, F vx, F vy
     fy += -gm * MU * gy;
     fz += -gm * MU * gz;
     du += F(0.5) * gm * (pr + MU) * (vx * gx + vy * gy + vz * gz);
+    if (isnan(fx) || isnan(fy) || isnan(fz)) return;
+    f.x += fx;
+    f.y += fy;
+    f.z += fz;
+}
+
+// The FP32 walk's form of sph_pair: the same terms regrouped around q = r/h
+// so that no intermediate leaves FP32's range in SI units.  Lengths (d, r, h)
+// are in the instance's scaled units, gm2 = gasMass * ls^2 and pr2 = pr *
+// ls^2; velocities and c as they are.  With s = g(q) / (pi h^4 r) the
+// reference's force -gm pr d s - gm MU d s is -(d/r) g(q)/pi K and its du term
+// 0.5 gm (pr + MU) (v . d) s is 0.5 (v . d/r) g(q)/pi K, where
+// K = gm (pr + MU) / h^4 = gm2 (pr2 + MU ls^2) / h'^4 (the scales cancel), and
+// mu = h (v . d) / (r^2 + 0.01 h^2) = (v . d/h) / (q^2 + 0.01).
+__device__ __forceinline__ void sph_pair32(float gm2, float dx, float dy, float dz, float r, float vx, float vy,
+                                           float vz, float ih, float pr2, float c, float ls2, Vec3<float> &f, float &du)
+{
+    if (r == 0.0f) return;
+    const float q = r * ih;
+    float g;
+    if (q < 1.0f)
+        g = -3.0f * q + 2.25f * q * q;
+    else if (q < 2.0f)
+        g = -0.75f * (2.0f - q) * (2.0f - q);
+    else
+        return;
+    const float vd = vx * dx + vy * dy + vz * dz;
+    const float mu = vd * ih / (q * q + 0.01f);
+    float MU = 0.0f;
+    if (vd < 0.0f) MU = -0.5f * c * mu + mu * mu;
+    const float ih2 = ih * ih;
+    const float K = gm2 * (pr2 + MU * ls2) * (ih2 * ih2);
+    const float t = g * (1.0f / (float)kPi) * K / r;
+    du += 0.5f * vd * t;
+    const float fx = -dx * t, fy = -dy * t, fz = -dz * t;
     if (isnan(fx) || isnan(fy) || isnan(fz)) return;
     f.x += fx;
     f.y += fy;
@@ -353,8 +389,8 @@ __device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
 // that is added to the compensated accumulator once per flush.
 template <bool kGeneral>
 __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane, float ox, float oy, float oz,
-                                           float G, float eps02, double e0, float &sx, float &sy, float &sz, float &kx,
-                                           float &ky, float &kz, unsigned long long &cnt_g)
+                                           float eps02, double e0, double ls, float &sx, float &sy, float &sz,
+                                           float &kx, float &ky, float &kz, unsigned long long &cnt_g)
 {
     float bx = 0.f, by = 0.f, bz = 0.f;
     int mine = 0;
@@ -367,11 +403,13 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
         const float ir = rsqrtf(r2);
         float e2 = eps02;
         if (kGeneral) {
+            // the general law decides on the distance in the caller's units
             double de2 = 0.0;
-            if (take && general_eps2((double)(r2 * ir), e0, &de2))
-                e2 = (float)de2;
+            if (take && general_eps2((double)(r2 * ir) / ls, e0, &de2))
+                e2 = (float)(de2 * ls * ls);
         }
-        float sc = __fdividef(G * P.w * ir, r2 + e2);
+        // P.w = G m ls^2: the sum comes out in the caller's units
+        float sc = __fdividef(P.w * ir, r2 + e2);
         sc = take ? sc : 0.f;
         bx = fmaf(dx, sc, bx);
         by = fmaf(dy, sc, by);
@@ -419,7 +457,6 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
     WarpSmem &W = sm_all[threadIdx.x >> 5];
     const int ngroups = a.ngroups;
     const float G = (float)a.G;
-    const float eps02 = (float)(a.e0 * a.e0);
     unsigned long long cnt_g = 0, cnt_s = 0;
     for (;;) {
         int grp = 0;
@@ -432,6 +469,10 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         const int root = gd.z;
         const bool act = live && (!a.active || a.active[i]);  // block steps walk the due particles only
         const bool valid = act && a.m[i] != 0.0;
+        // the instance's length scale: offsets, r^2, e0^2, h are in its units
+        const double ls = walk_scale(a.inst_R[root]);
+        const float eps02 = (float)(a.e0 * a.e0 * ls * ls);
+        const float ls2f = (float)(ls * ls);
         // Group set-up in FP64 (positions, group centre, float offsets).  No FP64
         // value stays live past this block: on this part FP64 instructions issue
         // at 1/64 of the FP32 rate, so the compiler must not be able to
@@ -461,37 +502,39 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 gy = 0.5 * (ly + uy);
                 gz = 0.5 * (lz + uz);
             }
-            ghx = (float)gx;
-            ghy = (float)gy;
-            ghz = (float)gz;
-            glx = (float)(gx - (double)ghx);
-            gly = (float)(gy - (double)ghy);
-            glz = (float)(gz - (double)ghz);
-            ox = (float)(xi - gx);
-            oy = (float)(yi - gy);
-            oz = (float)(zi - gz);
+            const double sgx = gx * ls, sgy = gy * ls, sgz = gz * ls;
+            ghx = (float)sgx;
+            ghy = (float)sgy;
+            ghz = (float)sgz;
+            glx = (float)(sgx - (double)ghx);
+            gly = (float)(sgy - (double)ghy);
+            glz = (float)(sgz - (double)ghz);
+            ox = (float)((xi - gx) * ls);
+            oy = (float)((yi - gy) * ls);
+            oz = (float)((zi - gz) * ls);
             // opaque copies: the walk below sees plain floats
             asm volatile("" : "+f"(ghx), "+f"(ghy), "+f"(ghz), "+f"(glx), "+f"(gly), "+f"(glz));
             asm volatile("" : "+f"(ox), "+f"(oy), "+f"(oz));
         }
         int myleaf = -1;
-        float hi_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
+        float hi_ = 0, ih_ = 0, pr = 0, cs = 0, vxi = 0, vyi = 0, vzi = 0;
         bool gas_i = false;
         if (live) {
             int pn = a.pnode[i];
             myleaf = (pn >= 0 && a.leafpos[pn] == i) ? pn : -1;
             if (kGas && a.type[i] == 2) {
                 gas_i = true;
-                hi_ = (float)a.h[i];
+                hi_ = (float)(a.h[i] * ls);
+                ih_ = 1.0f / hi_;
                 double rho = a.rho[i], P = a.P[i];
-                pr = (float)(P / (rho * rho) + P / (rho * rho));
+                pr = (float)((P / (rho * rho) + P / (rho * rho)) * ls * ls);
                 cs = (float)sqrt(kGamma * P / rho);
                 vxi = (float)a.vx[i];
                 vyi = (float)a.vy[i];
                 vzi = (float)a.vz[i];
             }
         }
-        asm volatile("" : "+f"(hi_), "+f"(pr), "+f"(cs), "+f"(vxi), "+f"(vyi), "+f"(vzi));
+        asm volatile("" : "+f"(hi_), "+f"(ih_), "+f"(pr), "+f"(cs), "+f"(vxi), "+f"(vyi), "+f"(vzi));
         const float h2x4 = 4.0f * hi_ * hi_;
         // group bounding box (half-extents about the group centre, with slack for
         // rounding) and the largest SPH reach of its gas lanes
@@ -567,7 +610,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 if (kGas) D = a.wD[c];
                 const float cx = (A.x - ghx) + (B.x - glx), cy = (A.y - ghy) + (B.y - gly),
                             cz = (A.z - ghz) + (B.z - glz);
-                W.cpos[lane] = make_float4(cx, cy, cz, A.w);
+                W.cpos[lane] = make_float4(cx, cy, cz, G * A.w);
                 W.cmac[lane] = B.w;
                 {
                     // r^2 at or below `tiny`, or within the guard band around the
@@ -694,8 +737,8 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                             const float4 Pc = W.cpos[j];
                             const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
                             const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-                            sph_pair<float>(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, hi_, pr, cs, side,
-                                            du);
+                            sph_pair32(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, ih_, pr, cs, ls2f,
+                                       side, du);
                             cnt_s++;
                         }
                     }
@@ -726,12 +769,12 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             __syncwarp();
             if (overflow) break;
             if (nl > kList - kBatch) {
-                flush_list<kGeneral>(W, nl, lane, ox, oy, oz, G, eps02, a.e0, sx, sy, sz, kx, ky, kz, cnt_g);
+                flush_list<kGeneral>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
                 nl = 0;
                 __syncwarp();
             }
         }
-        if (nl > 0) flush_list<kGeneral>(W, nl, lane, ox, oy, oz, G, eps02, a.e0, sx, sy, sz, kx, ky, kz, cnt_g);
+        if (nl > 0) flush_list<kGeneral>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
         kahan_add(sx, kx, side.x);
         kahan_add(sy, ky, side.y);
         kahan_add(sz, kz, side.z);
@@ -865,12 +908,13 @@ __global__ void __launch_bounds__(256) k_energy_sums(int n, const double *m, con
         for (int q = 0; q < 3; q++) part[3 * blockIdx.x + q] = sh[q][0];
 }
 
-__global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double *radius, float4 *wB, double theta)
+__global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double *radius, const int32_t *inst,
+                             const double *inst_R, float4 *wB, double theta)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     if (first[j] < 0) return;
-    double q = radius[j] / theta;
+    double q = radius[j] * walk_scale(inst_R[inst[j]]) / theta;
     wB[j].w = (float)(q * q);
 }
 
@@ -894,6 +938,7 @@ static WalkArgs walk_args(Ctx *c)
     a.radius = c->nd.radius;
     a.groups = c->groups;
     a.active = c->walk_active;
+    a.inst_R = c->inst_R;
     a.ngroups = c->ngroups;
     a.theta = c->prm.theta;
     a.e0 = c->prm.e0;
@@ -937,7 +982,7 @@ int run_forces(Ctx *c)
     if (c->n == 0) return AG2_OK;
     if (c->prm.theta != c->tree_theta) {
         AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.radius,
-                   c->nd.wB, c->prm.theta);
+                   c->nd.inst, c->inst_R, c->nd.wB, c->prm.theta);
         c->tree_theta = c->prm.theta;
     }
     WalkArgs a = walk_args(c);

@@ -1,0 +1,94 @@
+"""The walks in the reference's own unit system.  The reference integrates in
+SI (Units.h, Constants.h: metres, kilograms, G = 6.6743e-11; its Config.ini
+uses e0 = 1e19 m), where positions are ~1e20, r^2 ~1e40 and node masses
+~1e40: outside FP32's range unless the FP32 walk works in scaled units.  The
+FP32 walk keeps its accuracy contract against the FP64 walk in SI, and SI
+results equal the same galaxy's code-unit results converted."""
+import numpy as np
+import pytest
+
+import ics
+
+pytestmark = pytest.mark.gpu
+
+KPC = 3.08567758149137e19  # Units.h
+MSUN = 1.98847e30
+G_SI = 6.6743e-11
+L, M = KPC, 1e10 * MSUN
+V = np.sqrt(G_SI * M / L)  # velocity unit of G = 1 code units
+
+
+def _galaxy():
+    return ics.disk_galaxy(n_dm=24000, n_star=12000, n_gas=6000, seed=11)
+
+
+def _to_si(d):
+    return {"pos": d["pos"] * L, "vel": d["vel"] * V, "mass": d["mass"] * M, "U": d["U"] * V * V,
+            "type": d["type"], "massInH": d["massInH"] * M}
+
+
+def _run(d, G, e0, precision, offset=None):
+    import ag2
+
+    c = ag2.Context(len(d["mass"]), G=G, e0=e0, theta=0.5, massInH=d["massInH"], precision=precision)
+    pos = d["pos"] if offset is None else d["pos"] + offset
+    c.upload(pos, d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    c.build_tree()
+    c.sph_density()
+    c.forces()
+    out = {k: c.download(k) for k in ("acc", "dUdt", "h")}
+    c.close()
+    return out
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+def _check_contract(r32, r64, gas):
+    e = rel(r32["acc"], r64["acc"])
+    assert np.all(np.isfinite(r32["acc"]))
+    assert np.median(e) <= 1e-5 and np.quantile(e, 0.999) <= 1e-3, (np.median(e), np.quantile(e, 0.999))
+    du32, du64 = r32["dUdt"][gas], r64["dUdt"][gas]
+    assert np.all(np.isfinite(du32)) and np.abs(du64).max() > 0
+    assert np.abs(du32 - du64).max() <= 1e-3 * np.abs(du64).max()
+
+
+def test_fp32_walk_in_si_units():
+    d = _to_si(_galaxy())
+    gas = d["type"] == 2
+    r64 = _run(d, G_SI, 0.02 * L, "fp64")
+    r32 = _run(d, G_SI, 0.02 * L, "fp32")
+    np.testing.assert_array_equal(r32["h"], r64["h"])
+    _check_contract(r32, r64, gas)
+
+
+def test_si_equals_code_units():
+    """Same galaxy, code units (G = 1, kpc, 1e10 Msun) against SI: the FP64
+    walk's gravity agrees to rounding, and both FP32 walks keep the contract.
+    (Gas particles are left out of the first comparison: this galaxy's gas
+    masses equal the star masses and massInH is 64 of them, so the density
+    climb's strict comparisons against massInH meet exact ties, which the two
+    unit systems round differently, Node.cpp:743-751.)"""
+    dc = _galaxy()
+    ds = _to_si(dc)
+    gas = dc["type"] == 2
+    c64 = _run(dc, 1.0, 0.02, "fp64")
+    s64 = _run(ds, G_SI, 0.02 * L, "fp64")
+    e = rel(s64["acc"], c64["acc"] * (V * V / L))[~gas]
+    assert np.median(e) <= 1e-12 and np.quantile(e, 0.99) <= 1e-9, (np.median(e), np.quantile(e, 0.99))
+    s32 = _run(ds, G_SI, 0.02 * L, "fp32")
+    c32 = _run(dc, 1.0, 0.02, "fp32")
+    _check_contract(s32, s64, gas)
+    _check_contract(c32, c64, gas)
+
+
+def test_fp32_walk_far_from_origin_in_si():
+    """A galaxy 100 Mpc from the origin: the hi/lo float centres keep the
+    offsets, in scaled units."""
+    d = _to_si(_galaxy())
+    off = np.array([1.0e3, -2.0e3, 0.5e3]) * 1e2 * KPC
+    gas = d["type"] == 2
+    r64 = _run(d, G_SI, 0.02 * L, "fp64", offset=off)
+    r32 = _run(d, G_SI, 0.02 * L, "fp32", offset=off)
+    _check_contract(r32, r64, gas)
