@@ -718,19 +718,20 @@ struct Sums {
     }
     __device__ void add_node(const Nodes &nd, int64_t c)
     {
-        if (nd.tfirst[c] < first_id) {
-            first_id = nd.tfirst[c];
-            first_m = nd.tfirstm[c];
+        const NodeSum t = nd.tsum[c];
+        if (t.first_id < first_id) {
+            first_id = t.first_id;
+            first_m = t.first_m;
         }
-        m += nd.tm[c];
-        mx += nd.tmx[c];
-        my += nd.tmy[c];
-        mz += nd.tmz[c];
-        g += nd.tg[c];
-        gvx += nd.tgvx[c];
-        gvy += nd.tgvy[c];
-        gvz += nd.tgvz[c];
-        ng += nd.tng[c];
+        m += t.m;
+        mx += t.mx;
+        my += t.my;
+        mz += t.mz;
+        g += t.g;
+        gvx += t.gvx;
+        gvy += t.gvy;
+        gvz += t.gvz;
+        ng += t.ng;
     }
 };
 
@@ -777,17 +778,19 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
                                            double cx, double cy, double cz, double gas, double mvx, double mvy,
                                            double mvz, int32_t ng, uint8_t cmask, bool leaf, int32_t lp, RecArgs ra)
 {
-    nd.tm[nid] = tot.m;
-    nd.tmx[nid] = tot.mx;
-    nd.tmy[nid] = tot.my;
-    nd.tmz[nid] = tot.mz;
-    nd.tg[nid] = tot.g;
-    nd.tgvx[nid] = tot.gvx;
-    nd.tgvy[nid] = tot.gvy;
-    nd.tgvz[nid] = tot.gvz;
-    nd.tng[nid] = tot.ng;
-    nd.tfirst[nid] = tot.first_id;
-    nd.tfirstm[nid] = tot.first_m;
+    NodeSum ts;
+    ts.m = tot.m;
+    ts.mx = tot.mx;
+    ts.my = tot.my;
+    ts.mz = tot.mz;
+    ts.g = tot.g;
+    ts.gvx = tot.gvx;
+    ts.gvy = tot.gvy;
+    ts.gvz = tot.gvz;
+    ts.first_m = tot.first_m;
+    ts.ng = tot.ng;
+    ts.first_id = tot.first_id;
+    nd.tsum[nid] = ts;
     nd.childmask[nid] = cmask;
     nd.mass[nid] = mass;
     nd.comx[nid] = cx;
@@ -1494,7 +1497,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
     G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
-    G(tm) G(tmx) G(tmy) G(tmz) G(tg) G(tgvx) G(tgvy) G(tgvz) G(tng) G(tfirst) G(tfirstm) G(wA) G(wB) G(wD) G(flag)
+    G(tsum) G(wA) G(wB) G(wD) G(flag)
     G(rho) G(nlx) G(lint) G(lil)
 #undef G
     if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;

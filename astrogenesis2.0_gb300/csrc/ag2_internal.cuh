@@ -42,6 +42,15 @@ struct Particles {
     int32_t *id;
 };
 
+// Sums of a node's whole routed range: mass, mass-weighted position, gas mass
+// and gas momentum, the mass of its lowest upload index, gas count and that
+// index.  80 bytes, written and read whole.
+struct alignas(16) NodeSum {
+    double m, mx, my, mz, g, gvx, gvy, gvz;
+    double first_m;
+    int32_t ng, first_id;
+};
+
 struct Nodes {
     // topology (written by the level-wise build)
     int32_t *start, *count, *ndrop, *first, *parent, *leafpos;
@@ -56,11 +65,9 @@ struct Nodes {
     // moments (reference semantics, FP64)
     double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz;
     int32_t *ngas;
-    // sums over the whole routed range (bottom-up helper)
-    double *tm, *tmx, *tmy, *tmz, *tg, *tgvx, *tgvy, *tgvz;
-    int32_t *tng;
-    int32_t *tfirst;     // lowest upload index in the routed range
-    double *tfirstm;     // its mass
+    // sums over the whole routed range (bottom-up helper), one record per node
+    // so a node's eight children are one contiguous read
+    NodeSum *tsum;
     // walk records (FP32 view)
     float4 *wA;  // com_hi.xyz, mass
     float4 *wB;  // com_lo.xyz, mac radius^2 (leaf: -1)
@@ -265,13 +272,15 @@ void phase_finish(Ctx *c);
 // to +0) iff key(a) < key(b)
 __host__ __device__ inline int64_t okey(double x)
 {
-    x = x + 0.0;  // -0.0 -> +0.0
     long long b;
 #ifdef __CUDA_ARCH__
     b = __double_as_longlong(x);
 #else
     __builtin_memcpy(&b, &x, 8);
 #endif
+    // -0.0 -> +0.0 on the bit pattern (x + 0.0 would spend an FP64 add, which
+    // this part issues at 1/64 of the FP32 rate)
+    if (b == (long long)0x8000000000000000ULL) b = 0;
     return b >= 0 ? (int64_t)b : (int64_t)(b ^ 0x7FFFFFFFFFFFFFFFLL);
 }
 

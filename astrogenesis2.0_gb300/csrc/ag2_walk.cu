@@ -147,11 +147,12 @@ __device__ __forceinline__ void sph_pair(F gm, F dx, F dy, F dz, F r, F vx, F vy
 // 0.5 gm (pr + MU) (v . d) s is 0.5 (v . d/r) g(q)/pi K, where
 // K = gm (pr + MU) / h^4 = gm2 (pr2 + MU ls^2) / h'^4 (the scales cancel), and
 // mu = h (v . d) / (r^2 + 0.01 h^2) = (v . d/h) / (q^2 + 0.01).
-__device__ __forceinline__ void sph_pair32(float gm2, float dx, float dy, float dz, float r, float vx, float vy,
+__device__ __forceinline__ void sph_pair32(float gm2, float dx, float dy, float dz, float r2, float vx, float vy,
                                            float vz, float ih, float pr2, float c, float ls2, Vec3<float> &f, float &du)
 {
-    if (r == 0.0f) return;
-    const float q = r * ih;
+    if (r2 == 0.0f) return;
+    const float ir = rsqrtf(r2);
+    const float q = r2 * ir * ih;
     float g;
     if (q < 1.0f)
         g = -3.0f * q + 2.25f * q * q;
@@ -160,12 +161,12 @@ __device__ __forceinline__ void sph_pair32(float gm2, float dx, float dy, float 
     else
         return;
     const float vd = vx * dx + vy * dy + vz * dz;
-    const float mu = vd * ih / (q * q + 0.01f);
+    const float mu = __fdividef(vd * ih, q * q + 0.01f);
     float MU = 0.0f;
     if (vd < 0.0f) MU = -0.5f * c * mu + mu * mu;
     const float ih2 = ih * ih;
     const float K = gm2 * (pr2 + MU * ls2) * (ih2 * ih2);
-    const float t = g * (1.0f / (float)kPi) * K / r;
+    const float t = g * (1.0f / (float)kPi) * K * ir;
     du += 0.5f * vd * t;
     const float fx = -dx * t, fy = -dy * t, fz = -dz * t;
     if (isnan(fx) || isnan(fy) || isnan(fz)) return;
@@ -397,7 +398,7 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
 #pragma unroll 4
     for (int j = 0; j < cnt; j++) {
         const float4 P = W.lpos[j];
-        const bool take = (W.lmask[j] >> lane) & 1u;
+        bool take = (W.lmask[j] >> lane) & 1u;
         const float dx = P.x - ox, dy = P.y - oy, dz = P.z - oz;
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const float ir = rsqrtf(r2);
@@ -405,8 +406,13 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
         if (kGeneral) {
             // the general law decides on the distance in the caller's units
             double de2 = 0.0;
-            if (take && general_eps2((double)(r2 * ir) / ls, e0, &de2))
-                e2 = (float)(de2 * ls * ls);
+            if (take) {
+                if (general_eps2((double)(r2 * ir) / ls, e0, &de2))
+                    e2 = (float)(de2 * ls * ls);
+                else
+                    take = false;  // the reference returns without a force (Node.cpp:285-305)
+            }
+            mine += take ? 1 : 0;
         }
         // P.w = G m ls^2: the sum comes out in the caller's units
         float sc = __fdividef(P.w * ir, r2 + e2);
@@ -414,12 +420,16 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
         bx = fmaf(dx, sc, bx);
         by = fmaf(dy, sc, by);
         bz = fmaf(dz, sc, bz);
-        mine += take ? 1 : 0;
     }
     kahan_add(sx, kx, bx);
     kahan_add(sy, ky, by);
     kahan_add(sz, kz, bz);
-    cnt_g += (unsigned long long)mine;
+    if (kGeneral) {
+        cnt_g += (unsigned long long)mine;
+    } else {
+        // every set mask bit is one interaction: count them lane-parallel
+        for (int j = lane; j < cnt; j += 32) cnt_g += (unsigned long long)__popc(W.lmask[j]);
+    }
 }
 
 // Rare path of the FP32 walk: an opening test within the guard band of the
@@ -736,9 +746,8 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                         if (D.w > 0.0f) {
                             const float4 Pc = W.cpos[j];
                             const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
-                            const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-                            sph_pair32(D.w, -dx, -dy, -dz, r, vxi - D.x, vyi - D.y, vzi - D.z, ih_, pr, cs, ls2f,
-                                       side, du);
+                            sph_pair32(D.w, -dx, -dy, -dz, dx * dx + dy * dy + dz * dz, vxi - D.x, vyi - D.y,
+                                       vzi - D.z, ih_, pr, cs, ls2f, side, du);
                             cnt_s++;
                         }
                     }
