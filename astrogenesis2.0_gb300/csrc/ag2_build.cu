@@ -1104,6 +1104,7 @@ constexpr int kLocalWarps = 8;      // warps per thread block of k_local (fewer 
 constexpr int kPoolChunk = 512;     // nodes per warp-private pool chunk
 constexpr int kLeafChunk = 256;     // leaf-list entries per warp-private stretch
 constexpr int kIntChunk = 128;      // internal-node-list entries per warp-private stretch
+constexpr int kCoop = 16;           // frontier nodes of more particles are done by the whole warp
 
 // Shared memory of one warp for subtrees of up to `cap` particles (cap a
 // multiple of 8).  Per particle: keys 3 x 8 B and particle index 4 B (fixed
@@ -1172,31 +1173,21 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
             int16_t *const fsc = cur ? FS1 : FS0, *const fsn = cur ? FS0 : FS1;
             int16_t *const fcc = cur ? FC1 : FC0, *const fcn = cur ? FC0 : FC1;
             int16_t *const lc = cur ? L1 : L0, *const ln = cur ? L0 : L1;
-            // (a) digits and split decision, one lane per frontier node
-            for (int f = lane; f < nf; f += 32) {
-                const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
-                const int64_t *bk = nd.bkey + 9 * (int64_t)v;
-                const int64_t b0 = bk[0], b1 = bk[1], b2 = bk[2], b3 = bk[3], b4 = bk[4], b5 = bk[5], b6 = bk[6],
-                              b7 = bk[7], b8 = bk[8];
-                int16_t *hh = FH + 9 * f;
-#pragma unroll
-                for (int d = 0; d < 9; d++) hh[d] = 0;
-                for (int j = ls; j < ls + cnt; j++) {
-                    const int q = lc[j];
-                    const int64_t x = KX[q], y = KY[q], z = KZ[q];
-                    int d;
-                    // inclusive bounds and octant of Node.cpp:606-608, 706-716, as in k_digit
-                    if (x < b0 || x > b3 || y < b1 || y > b4 || z < b2 || z > b5)
-                        d = 8;
-                    else
-                        d = (x > b6 ? 1 : 0) | (y > b7 ? 2 : 0) | (z > b8 ? 4 : 0);
-                    DIG[j] = (uint8_t)d;
-                    hh[d]++;
-                }
+            // (a) digits and split decision.  A frontier node of more than kCoop
+            // particles is done by the whole warp, 32 particles at a time with
+            // the digit counts from ballots; the others take one lane each.
+            auto digit_of = [&](int q, const int64_t *b) -> int {
+                const int64_t x = KX[q], y = KY[q], z = KZ[q];
+                // inclusive bounds and octant of Node.cpp:606-608, 706-716, as in k_digit
+                if (x < b[0] || x > b[3] || y < b[1] || y > b[4] || z < b[2] || z > b[5]) return 8;
+                return (x > b[6] ? 1 : 0) | (y > b[7] ? 2 : 0) | (z > b[8] ? 4 : 0);
+            };
+            auto decide = [&](int f, int32_t v, int32_t ls, int32_t cnt, int16_t *hh) {
+                // hh holds the digit counts: counts -> starts, drops, split decision
                 const int32_t ndrop = hh[8], reached = cnt - ndrop;
                 int32_t acc = ls;
 #pragma unroll
-                for (int d = 0; d < 9; d++) {  // counts -> starts
+                for (int d = 0; d < 9; d++) {
                     const int32_t cd = hh[d];
                     hh[d] = (int16_t)acc;
                     acc += cd;
@@ -1216,6 +1207,52 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
                     flag = -2;
                 }
                 FF[f] = flag;
+            };
+            for (int f0 = 0; f0 < nf; f0 += 32) {
+                unsigned bigm = __ballot_sync(full, f0 + lane < nf && fcc[f0 + lane] > kCoop);
+                while (bigm) {
+                    const int f = f0 + __ffs(bigm) - 1;
+                    bigm &= bigm - 1;
+                    const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
+                    int64_t b[9];
+#pragma unroll
+                    for (int k = 0; k < 9; k++) b[k] = nd.bkey[9 * (int64_t)v + k];
+                    int cn[9];
+#pragma unroll
+                    for (int d = 0; d < 9; d++) cn[d] = 0;
+                    for (int j0 = ls; j0 < ls + cnt; j0 += 32) {
+                        const int j = j0 + lane;
+                        int d = 15;
+                        if (j < ls + cnt) {
+                            d = digit_of(lc[j], b);
+                            DIG[j] = (uint8_t)d;
+                        }
+#pragma unroll
+                        for (int e = 0; e < 9; e++) cn[e] += __popc(__ballot_sync(full, d == e));
+                    }
+                    if (lane == 0) {
+                        int16_t *hh = FH + 9 * f;
+#pragma unroll
+                        for (int d = 0; d < 9; d++) hh[d] = (int16_t)cn[d];
+                        decide(f, v, ls, cnt, hh);
+                    }
+                }
+            }
+            for (int f = lane; f < nf; f += 32) {
+                const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
+                if (cnt > kCoop) continue;
+                int64_t b[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) b[k] = nd.bkey[9 * (int64_t)v + k];
+                int16_t *hh = FH + 9 * f;
+#pragma unroll
+                for (int d = 0; d < 9; d++) hh[d] = 0;
+                for (int j = ls; j < ls + cnt; j++) {
+                    const int d = digit_of(lc[j], b);
+                    DIG[j] = (uint8_t)d;
+                    hh[d]++;
+                }
+                decide(f, v, ls, cnt, hh);
             }
             __syncwarp();
             // (b) 8-child blocks of this level's splits, from the warp's pool
@@ -1331,15 +1368,10 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
             }
             __syncwarp();
             // (c) partition by digit into the other order; leaves and drop tails settle
-            // (the digit starts serve as cursors: afterwards hh[d] is the end of digit d)
-            for (int f = lane; f < nf; f += 32) {
-                const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
-                int16_t *hh = FH + 9 * f;
-                for (int j = ls; j < ls + cnt; j++) {
-                    const int d = DIG[j];
-                    ln[hh[d]] = lc[j];
-                    hh[d]++;
-                }
+            // (the digit starts serve as cursors: afterwards hh[d] is the end of digit d).
+            // Nodes of more than kCoop particles: the whole warp, a stable
+            // partition of 32 at a time (ranks among the lanes of equal digit).
+            auto settle = [&](int f, int32_t v, int32_t ls, int32_t cnt, const int16_t *hh) {
                 // the out-of-bounds tail in upload order (the level loop's k_sort_drops rule)
                 const int32_t tb = hh[7], te = ls + cnt;
                 for (int a = tb + 1; a < te; a++) {
@@ -1357,6 +1389,41 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
                     perm_final[s0 + p] = PID[ln[p]];
                     pnode[s0 + p] = v;
                 }
+            };
+            for (int f0 = 0; f0 < nf; f0 += 32) {
+                unsigned bigm = __ballot_sync(full, f0 + lane < nf && fcc[f0 + lane] > kCoop);
+                while (bigm) {
+                    const int f = f0 + __ffs(bigm) - 1;
+                    bigm &= bigm - 1;
+                    const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
+                    int16_t *hh = FH + 9 * f;
+                    for (int j0 = ls; j0 < ls + cnt; j0 += 32) {
+                        const int j = j0 + lane;
+                        const bool valid = j < ls + cnt;
+                        const int d = valid ? (int)DIG[j] : 15;
+                        const unsigned peers = __match_any_sync(full, d);
+                        const int rank = __popc(peers & lt);
+                        const int dst = valid ? hh[d] + rank : 0;
+                        __syncwarp();
+                        if (valid) {
+                            ln[dst] = lc[j];
+                            if (rank == 0) hh[d] = (int16_t)(dst + __popc(peers));
+                        }
+                        __syncwarp();
+                    }
+                    if (lane == 0) settle(f, v, ls, cnt, hh);
+                }
+            }
+            for (int f = lane; f < nf; f += 32) {
+                const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
+                if (cnt > kCoop) continue;
+                int16_t *hh = FH + 9 * f;
+                for (int j = ls; j < ls + cnt; j++) {
+                    const int d = DIG[j];
+                    ln[hh[d]] = lc[j];
+                    hh[d]++;
+                }
+                settle(f, v, ls, cnt, hh);
             }
             __syncwarp();
             // (d) children: 8 lanes per split node, coalesced; non-empty ones form the next frontier
