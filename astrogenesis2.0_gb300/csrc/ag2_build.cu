@@ -805,21 +805,23 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     // COM split into hi + lo floats, mass * ls^2 (the walk's accelerations come
     // out in the caller's units), (radius/theta)^2, gasMass * ls^2 (the FP32
     // SPH pair's scaled mass); velocities as they are
-    const double ls = walk_scale(ra.inst_R[nd.inst[nid]]), ls2 = ls * ls;
-    const double sx = cx * ls, sy = cy * ls, sz = cz * ls;
+    const int k = walk_scale_exp(ra.inst_R[nd.inst[nid]]);
+    const double sx = scale2(cx, k), sy = scale2(cy, k), sz = scale2(cz, k);
     const float hx = (float)sx, hy = (float)sy, hz = (float)sz;
     const float lx = (float)(sx - (double)hx), ly = (float)(sy - (double)hy), lz = (float)(sz - (double)hz);
-    nd.wA[nid] = make_float4(hx, hy, hz, (float)(mass * ls2));
+    nd.wA[nid] = make_float4(hx, hy, hz, (float)scale2(mass, 2 * k));
     float mac = -1.0f;
     if (!leaf) {
-        const double q = nd.radius[nid] * ls / ra.theta;  // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2
-        mac = (float)(q * q);
+        // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2; FP32 is
+        // enough for the threshold the FP32 walk tests with its guard band
+        const float q = (float)scale2(nd.radius[nid], k) / (float)ra.theta;
+        mac = q * q;
     }
     nd.wB[nid] = make_float4(lx, ly, lz, mac);
     if (leaf && lp >= 0)
-        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)(gas * ls2));
+        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)scale2(gas, 2 * k));
     else
-        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)(gas * ls2));
+        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)scale2(gas, 2 * k));
 }
 
 // Moments from the node's own mass set: the centre of mass and gas velocity as
@@ -979,7 +981,7 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
         const int64_t c = first + o;
         if (nd.count[c] == 0) continue;
         own.add_node(nd, c);
-        if (nd.mass[c] != 0.0) cmask |= (uint8_t)(1u << o);
+        if ((dbits(nd.mass[c]) << 1) != 0) cmask |= (uint8_t)(1u << o);  // mass != 0, on the bits
     }
     tot = own;
     for (int32_t k = cnt - ndrop; k < cnt; k++) tot.add_particle(P, idx(k));

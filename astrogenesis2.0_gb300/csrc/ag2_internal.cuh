@@ -289,12 +289,43 @@ __host__ __device__ inline int64_t okey(double x)
 // walk records and the walk's offsets are in units of 2^e: scaling by a power
 // of two is exact, and it keeps r^2, (radius/theta)^2 and h^4 inside FP32's
 // range in any unit system (the reference works in SI, positions ~1e20 m).
-__host__ __device__ inline double walk_scale(double R)
+__host__ __device__ inline int64_t dbits(double x)
 {
-    if (!(R > 0.0) || !(R < 1.0e308)) return 1.0;
-    int e = 0;
-    frexp(R, &e);
-    return ldexp(1.0, -e);
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(x);
+#else
+    int64_t b;
+    __builtin_memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+__host__ __device__ inline double bits_d(int64_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(b);
+#else
+    double x;
+    __builtin_memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+// the exponent k of the scale 2^k (integer operations only: this part issues
+// FP64 at 1/64 of the FP32 rate)
+__host__ __device__ inline int walk_scale_exp(double R)
+{
+    const int64_t b = dbits(R);
+    const int ef = (int)((b >> 52) & 0x7ff);
+    if (b <= 0 || ef == 0 || ef == 0x7ff) return 0;  // R <= 0, subnormal, inf or NaN: scale 1
+    return 1022 - ef;  // R = f 2^e, f in [0.5, 1), e = ef - 1022
+}
+__host__ __device__ inline double walk_scale(double R) { return bits_d((int64_t)(1023 + walk_scale_exp(R)) << 52); }
+// x * 2^k exactly; on the exponent bits when x and the result are normal
+__host__ __device__ inline double scale2(double x, int k)
+{
+    const int64_t b = dbits(x);
+    const int ef = (int)((b >> 52) & 0x7ff);
+    if (ef > 0 && ef < 0x7ff && ef + k > 0 && ef + k < 0x7ff) return bits_d(b + ((int64_t)k << 52));
+    return x * ldexp(1.0, k);  // zero, subnormal, inf, NaN, or a result outside the normal range
 }
 
 // entries of the leaf list beyond one per particle: the unused tails of the

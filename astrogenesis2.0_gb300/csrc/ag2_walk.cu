@@ -923,8 +923,8 @@ __global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double 
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     if (first[j] < 0) return;
-    double q = radius[j] * walk_scale(inst_R[inst[j]]) / theta;
-    wB[j].w = (float)(q * q);
+    const float q = (float)scale2(radius[j], walk_scale_exp(inst_R[inst[j]])) / (float)theta;
+    wB[j].w = q * q;
 }
 
 }  // namespace
