@@ -355,7 +355,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->refnode, cap * 4) == cudaSuccess && cudaMalloc(&c->slot_of, cap * 4) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->drop_list, 65536 * 4) == cudaSuccess && cudaMalloc(&c->digit, cap) == cudaSuccess &&
+         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->drop_list, 65536 * 4) == cudaSuccess && cudaMalloc(&c->digit, 2 * cap) == cudaSuccess &&
          cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&
          cudaMalloc(&c->pinst, cap * 4) == cudaSuccess &&

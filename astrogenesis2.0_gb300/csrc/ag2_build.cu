@@ -270,7 +270,8 @@ struct LevelBufs {
     int64_t *kx_next, *ky_next, *kz_next;
     int32_t *perm_final;     // per slot, written when the particle there settles
     int32_t *pnode;          // per slot: node the settled particle ends in
-    uint8_t *digit;          // per active-list entry
+    const uint8_t *digit;    // per slot: octant digit of the particle there in its node of this level
+    uint8_t *digit_next;     // ... of the next level (written as particles move there)
     int32_t *hist, *cursor;  // 9 per split-list entry
     const int32_t *nl;       // this level's split list (node ids)
     int32_t *nl_next;
@@ -285,6 +286,16 @@ struct LevelBufs {
 struct LevelPair {
     LevelBufs b[2];
 };
+
+// Octant digit of ordered keys against a node's 9 bound keys: 0..7, or 8 when
+// outside the node's inclusive bounds (Node.cpp:606-608, 706-716).  The level
+// loop computes a particle's digit for the next level where it moves the
+// particle into its child (k_scatter), and level 0's in k_level0.
+__device__ __forceinline__ int octant_digit(const int64_t *k, int64_t kx, int64_t ky, int64_t kz)
+{
+    if (kx < k[0] || kx > k[3] || ky < k[1] || ky > k[4] || kz < k[2] || kz > k[5]) return 8;
+    return (kx > k[6] ? 1 : 0) | (ky > k[7] ? 2 : 0) | (kz > k[8] ? 4 : 0);
+}
 
 // Level 0: the slots of an instance whose root is split are active (the
 // coordinates become ordered keys, in slot order); the slot of a one-particle
@@ -305,10 +316,15 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
         if (nk == 1) {
             act = true;
             perm[i] = i;
-            posnode[i] = nd.nlx[k];
-            const_cast<int64_t *>(b.kx)[i] = okey(px[i]);
-            const_cast<int64_t *>(b.ky)[i] = okey(py[i]);
-            const_cast<int64_t *>(b.kz)[i] = okey(pz[i]);
+            const int j = nd.nlx[k];
+            posnode[i] = j;
+            const int64_t kx = okey(px[i]), ky = okey(py[i]), kz = okey(pz[i]);
+            const_cast<int64_t *>(b.kx)[i] = kx;
+            const_cast<int64_t *>(b.ky)[i] = ky;
+            const_cast<int64_t *>(b.kz)[i] = kz;
+            const int d = octant_digit(nd.bkey + 9 * (int64_t)k, kx, ky, kz);
+            const_cast<uint8_t *>(b.digit)[i] = (uint8_t)d;
+            agg_inc(b.hist, 9 * j + d);
         } else {
             b.perm_final[i] = i;
             b.pnode[i] = k;  // one-particle root, or a serial root for k_local
@@ -321,28 +337,6 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
     }
     const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
     if (act) const_cast<int32_t *>(b.ap)[q] = i;
-}
-
-// digit of every active slot against its node's bounds
-__global__ void __launch_bounds__(kBlock) k_digit(LevelPair lp, Nodes nd, const Ctx::Ctl *ctl)
-{
-    const int nap = ctl->cur_nap;
-    const LevelBufs &b = lp.b[ctl->level & 1];
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nap; t += gridDim.x * blockDim.x) {
-    const int i = b.ap[t];
-    const int j = b.posnode[i];
-    const int64_t *k = nd.bkey + 9 * (int64_t)b.nl[j];
-    const int64_t kx = b.kx[i], ky = b.ky[i], kz = b.kz[i];
-    int d;
-    // inclusive bounds of Node::getOctant / insert(Particle*) (Node.cpp:606-608, 706-708)
-    if (kx < k[0] || kx > k[3] || ky < k[1] || ky > k[4] || kz < k[2] || kz > k[5]) {
-        d = 8;
-    } else {
-        d = (kx > k[6] ? 1 : 0) | (ky > k[7] ? 2 : 0) | (kz > k[8] ? 4 : 0);  // Node.cpp:714-716
-    }
-    b.digit[t] = (uint8_t)d;
-    agg_inc(b.hist, 9 * j + d);
-    }
 }
 
 // Split decisions and children of the nodes of this level's split list.  Eight
@@ -514,16 +508,24 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
         const int j = b.posnode[i];
         const int32_t nid = b.nl[j];
         const int32_t p = b.perm[i];
-        const int d = b.digit[t];
+        const int d = b.digit[i];
         const int np = agg_inc(b.cursor, 9 * j + d);
         const int32_t first = nd.first[nid];
         if (first >= 0 && d < 8) {
             const int32_t child = first + d;
             const uint8_t cn = nd.needs[child];
             if (cn) {  // split again: by the next level (1) or by k_local (2), which reads the keys there
-                b.kx_next[np] = b.kx[i];
-                b.ky_next[np] = b.ky[i];
-                b.kz_next[np] = b.kz[i];
+                const int64_t kx = b.kx[i], ky = b.ky[i], kz = b.kz[i];
+                b.kx_next[np] = kx;
+                b.ky_next[np] = ky;
+                b.kz_next[np] = kz;
+                if (cn == 1) {
+                    // its digit in the child for the next level, and the child's histogram
+                    // (k_nodes of this level has left the histogram zero)
+                    const int d2 = octant_digit(nd.bkey + 9 * (int64_t)child, kx, ky, kz);
+                    b.digit_next[np] = (uint8_t)d2;
+                    agg_inc(b.hist, 9 * nd.nlx[child] + d2);
+                }
             }
             if (cn == 1) {
                 b.perm_next[np] = p;
@@ -1656,7 +1658,8 @@ static LevelBufs level_bufs(Ctx *c, int w)
     b.kz_next = key + (3 * (w ^ 1) + 2) * cap;
     b.perm_final = c->perm_final;
     b.pnode = c->pnode;
-    b.digit = c->digit;
+    b.digit = c->digit + (size_t)w * cap;
+    b.digit_next = c->digit + (size_t)(w ^ 1) * cap;
     b.hist = c->hist;
     b.cursor = c->cursor;
     b.nl = c->nl[w];
@@ -1805,7 +1808,10 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     if (!capture) {
         if ((rc = ensure_instance_tables(c)) != AG2_OK) return rc;
         if ((rc = prepare_gas_tables(c, n)) != AG2_OK) return rc;
-        if ((rc = ensure_hist(c, 1)) != AG2_OK) return rc;
+        // the histogram holds a level's split list (at most n/2 nodes plus the roots);
+        // it is sized before the level loop, which fills the next level's while it
+        // consumes this one's
+        if ((rc = ensure_hist(c, std::max<size_t>(c->n, 1))) != AG2_OK) return rc;
         if (c->hist_dirty) {
             AG2_CUDA(c, cudaMemsetAsync(c->hist, 0, c->hist_cap * sizeof(int32_t), c->stream));
             c->hist_dirty = false;
@@ -1859,7 +1865,6 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         AG2_CUDA(c, cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
         AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 0, (int)AG2_MAX_DEPTH, h, 1);
         rc = capture_while(c, h, [&]() -> int {
-            AG2_LAUNCH(c, k_digit, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
             AG2_LAUNCH(c, k_nodes, fixed_grid, kBlock, 0, lpair, thresh, (int64_t)c->node_cap, c->nd, c->ctl,
                        (int)AG2_MAX_DEPTH);
             AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
@@ -1878,12 +1883,10 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         c->root_radius = c->inst_R_h[0];
         int nnl = c->ctl_host->cur_nnl, nap = c->ctl_host->cur_nap;
         while (nnl > 0) {
-            if ((rc = ensure_hist(c, (size_t)nnl)) != AG2_OK) return rc;
             if ((rc = ensure_node_capacity(c, (size_t)(c->level_base.back() + 8 * (int64_t)nnl))) != AG2_OK) return rc;
             lpair.b[0] = level_bufs(c, 0);
             lpair.b[1] = level_bufs(c, 1);
             lpair.b[0].local_ok = lpair.b[1].local_ok = local_ok;
-            AG2_LAUNCH(c, k_digit, grid_for(nap, kBlock), kBlock, 0, lpair, c->nd, c->ctl);
             AG2_LAUNCH(c, k_nodes, grid_for((size_t)nnl * 8, kBlock), kBlock, 0, lpair, thresh, (int64_t)c->node_cap,
                        c->nd, c->ctl, (int)AG2_MAX_DEPTH);
             AG2_LAUNCH(c, k_scatter, grid_for(nap, kBlock), kBlock, 0, lpair, c->nd, c->ctl);
