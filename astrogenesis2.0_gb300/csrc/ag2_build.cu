@@ -1114,8 +1114,8 @@ constexpr int kCoop = 16;           // frontier nodes of more particles are done
 // multiple of 8).  Per particle: keys 3 x 8 B and particle index 4 B (fixed
 // slots), position -> slot 2 x 2 B, digit 1 B.  Per frontier node (at most one
 // per particle): node 2 x 4 B, start and count 2 x 2 x 2 B, first child 4 B,
-// digit starts 9 x 2 B.
-__host__ __device__ constexpr size_t local_smem_bytes(int cap) { return (size_t)cap * 72; }
+// digit starts 9 x 2 B, parent of a next-frontier node 4 B.
+__host__ __device__ constexpr size_t local_smem_bytes(int cap) { return (size_t)cap * 76; }
 
 __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__restrict__ roots, int cap,
                                                             Nodes nd, Ctx::Ctl *ctl, const int64_t *__restrict__ pkey,
@@ -1140,6 +1140,7 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
     int16_t *const FC0 = L1 + 3 * cap, *const FC1 = L1 + 4 * cap;
     int16_t *const FH = L1 + 5 * cap;  // 9 per frontier node
     uint8_t *DIG = reinterpret_cast<uint8_t *>(FH + 9 * cap);
+    int32_t *FPAR = reinterpret_cast<int32_t *>(DIG + cap);  // parent of each next-frontier node
 
     const int nroots = ctl->nlocal;
     unsigned long long pool = 0, pool_end = 0;  // warp-private node pool [pool, pool_end)
@@ -1430,20 +1431,23 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
                 settle(f, v, ls, cnt, hh);
             }
             __syncwarp();
-            // (d) children: 8 lanes per split node, coalesced; non-empty ones form the next frontier
+            // (d) children: 8 lanes per split node, coalesced; non-empty ones form the
+            // next frontier.  Their FP64 centres and bounds come after, 32 at a
+            // time over that compact list, so no FP64 instruction runs for an
+            // empty child (this part issues FP64 at 1/64 of the FP32 rate).
             int nn = 0;
             for (int f0 = 0; f0 < nf; f0 += 4) {
                 const int f = f0 + (lane >> 3), o = lane & 7;
                 const int32_t ff = f < nf ? FF[f] : -1;
                 bool join = false;
-                int32_t c = 0, cs = 0, cc = 0;
+                int32_t c = 0, cs = 0, cc = 0, v = 0;
                 if (ff >= 0) {
-                    const int32_t v = fnc[f];
+                    v = fnc[f];
                     const int16_t *hh = FH + 9 * f;
                     c = ff + o;
                     cs = o ? hh[o - 1] : fsc[f];
                     cc = hh[o] - cs;
-                    const double rc = nd.radius[v] / 2;  // Node.cpp:640
+                    const double rc = scale2(nd.radius[v], -1);  // radius / 2 (Node.cpp:640), on the exponent
                     nd.start[c] = s0 + cs;
                     nd.count[c] = cc;
                     nd.ndrop[c] = 0;
@@ -1455,16 +1459,7 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
                     nd.mode[c] = cc ? MODE_SER : MODE_EMPTY;
                     nd.needs[c] = 0;
                     nd.leafpos[c] = -1;
-                    if (cc > 0) {  // child o: centre c + r*(+-0.5) (Node.cpp:630-642)
-                        const double x = __dadd_rn(nd.cx[v], (o & 1) ? rc : -rc);
-                        const double y = __dadd_rn(nd.cy[v], (o & 2) ? rc : -rc);
-                        const double z = __dadd_rn(nd.cz[v], (o & 4) ? rc : -rc);
-                        nd.cx[c] = x;
-                        nd.cy[c] = y;
-                        nd.cz[c] = z;
-                        set_bounds_v(nd, c, x, y, z, rc);
-                        join = true;
-                    }
+                    join = cc > 0;
                 }
                 const unsigned bj = __ballot_sync(full, join);
                 if (join) {
@@ -1472,8 +1467,23 @@ __global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__res
                     fnn[q] = c;
                     fsn[q] = (int16_t)cs;
                     fcn[q] = (int16_t)cc;
+                    FPAR[q] = v;
+                    DIG[q] = (uint8_t)o;  // the digits of this level are consumed
                 }
                 nn += __popc(bj);
+            }
+            __syncwarp();
+            for (int q = lane; q < nn; q += 32) {  // child o: centre c + r*(+-0.5) (Node.cpp:630-642)
+                const int32_t c = fnn[q], v = FPAR[q];
+                const int o = DIG[q];
+                const double rc = scale2(nd.radius[v], -1);
+                const double x = __dadd_rn(nd.cx[v], (o & 1) ? rc : -rc);
+                const double y = __dadd_rn(nd.cy[v], (o & 2) ? rc : -rc);
+                const double z = __dadd_rn(nd.cz[v], (o & 4) ? rc : -rc);
+                nd.cx[c] = x;
+                nd.cy[c] = y;
+                nd.cz[c] = z;
+                set_bounds_v(nd, c, x, y, z, rc);
             }
             __syncwarp();
             if (nn) deepest = max(deepest, level + 1);
