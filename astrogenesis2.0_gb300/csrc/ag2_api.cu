@@ -171,7 +171,7 @@ void free_nodes(Nodes &d)
     void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs, d.childmask,
                   d.cx,    d.cy,    d.cz,    d.bkey,  d.mass,   d.comx,    d.comy, d.comz, d.gas,   d.mvx,
                   d.mvy,   d.mvz,   d.ngas,  d.tsum,
-                  d.wA,   d.wB,      d.wD,   d.flag, d.rho,
+                  d.wA,   d.wB,      d.wC,   d.wD,   d.flag, d.rho,
                   d.radius, d.inst, d.nlx, d.lint, d.lil};
     for (void *q : ps) cudaFree(q);
     d = Nodes{};

@@ -820,6 +820,7 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
         mac = q * q;
     }
     nd.wB[nid] = make_float4(lx, ly, lz, mac);
+    nd.wC[nid] = make_int4(nd.first[nid], nd.leafpos[nid], (int)cmask, 0);  // one load for the walk's child staging
     if (leaf && lp >= 0)
         nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)scale2(gas, 2 * k));
     else
@@ -1578,7 +1579,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
     G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
-    G(tsum) G(wA) G(wB) G(wD) G(flag)
+    G(tsum) G(wA) G(wB) G(wC) G(wD) G(flag)
     G(rho) G(nlx) G(lint) G(lil)
 #undef G
     if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;

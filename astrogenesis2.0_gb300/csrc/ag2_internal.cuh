@@ -72,6 +72,7 @@ struct Nodes {
     float4 *wA;  // com_hi.xyz, mass
     float4 *wB;  // com_lo.xyz, mac radius^2 (leaf: -1)
     float4 *wD;  // gas velocity (mVel or the leaf particle's velocity), gasMass
+    int4 *wC;    // first child (-1 leaf), leaf particle slot (-1 none), child mask, 0
     // SPH / visual density scratch
     uint8_t *flag;
     double *rho;

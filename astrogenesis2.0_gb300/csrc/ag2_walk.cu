@@ -45,6 +45,7 @@ struct WalkArgs {
     const int32_t *pnode;
     double *ax, *ay, *az, *dUdt;
     const float4 *wA, *wB, *wD;
+    const int4 *wC;
     const int32_t *first, *leafpos;
     const uint8_t *childmask;
     const int8_t *level;
@@ -362,6 +363,7 @@ struct alignas(16) WarpSmem {
     unsigned char ccm[kBatch];  // child mask of the child
     unsigned char ccls[kBatch]; // group-level class: 0 per-lane, 1 every lane opens, 2 every lane accepts
     unsigned cself[kBatch];     // lane whose own leaf this child is (bit), else 0
+    unsigned bkeep[kBatch];     // lanes that evaluate batch slot j, less the one whose own leaf it is
     unsigned char mq[kBatch];   // batch slot of the q-th child the lanes decide one by one
     float4 lpos[kList];      // accepted nodes: relative com, mass
     unsigned lmask[kList];   // lanes that accepted them
@@ -614,8 +616,9 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 const int c = W.bchild[lane];
                 const float4 A = a.wA[c];
                 const float4 B = a.wB[c];
-                const int f = a.first[c];
-                const unsigned char ccm = a.childmask[c];
+                const int4 C4 = a.wC[c];
+                const int f = C4.x;
+                const unsigned char ccm = (unsigned char)C4.z;
                 float4 D;
                 if (kGas) D = a.wD[c];
                 const float cx = (A.x - ghx) + (B.x - glx), cy = (A.y - ghy) + (B.y - gly),
@@ -640,10 +643,11 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 // per-lane test is needed.  NaN centres fall through.
                 unsigned selfm = 0u;
                 if (B.w < 0.0f) {
-                    const int lp = a.leafpos[c] - gd.x;
+                    const int lp = C4.y - gd.x;
                     if (lp >= 0 && lp < 32) selfm = 1u << lp;
                 }
                 W.cself[lane] = selfm;
+                W.bkeep[lane] = W.bmask[lane] & ~selfm;
                 const float ax_ = fabsf(cx), ay_ = fabsf(cy), az_ = fabsf(cz);
                 const float nx = fmaxf(ax_ - hbx, 0.f), ny = fmaxf(ay_ - hby, 0.f), nz = fmaxf(az_ - hbz, 0.f);
                 const float fx = ax_ + hbx, fy = ay_ + hby, fz = az_ + hbz;
@@ -668,7 +672,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 const int j = lane;
                 const unsigned char cls = j < nc ? W.ccls[j] : (unsigned char)255;
                 const unsigned bm = j < nc ? W.bmask[j] : 0u;
-                const unsigned keep = bm & ~(j < nc ? W.cself[j] : 0u);
+                const unsigned keep = j < nc ? W.bkeep[j] : 0u;
                 const bool opn = cls == 1;
                 const bool acc = cls == 2 && keep != 0u;
                 const unsigned om = __ballot_sync(0xffffffffu, opn);
@@ -705,18 +709,18 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
 #pragma unroll 2
                 for (int q = 0; q < nm; q++) {
                     const int j = W.mq[q];
+                    const unsigned bit = 1u << q;
                     // the lanes that evaluate this child, except the one whose own leaf it is
-                    const bool in = ((W.bmask[j] & ~W.cself[j]) >> lane) & 1u;
-                    if (in) {
+                    if ((W.bkeep[j] >> lane) & 1u) {
                         const float4 Pc = W.cpos[j];
                         const float4 T = W.cthr[j];
                         const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                         const bool acc = r2 > T.w, opn = r2 > T.y && r2 < T.z;
-                        accb |= (acc ? 1u : 0u) << q;
-                        opnb |= (opn ? 1u : 0u) << q;
-                        rqb |= (acc || opn ? 0u : 1u) << q;
-                        if (kGas && gas_i && acc && r2 < h2x4) sphb |= 1u << q;
+                        if (acc) accb |= bit;
+                        if (opn) opnb |= bit;
+                        if (!(acc || opn)) rqb |= bit;
+                        if (kGas && gas_i && acc && r2 < h2x4) sphb |= bit;
                     }
                 }
                 // the rare tests decided in FP64 (near zero distance, or the guard band)
@@ -940,7 +944,7 @@ static WalkArgs walk_args(Ctx *c)
     a.type = S.type;
     a.pnode = c->pnode;
     a.ax = S.ax; a.ay = S.ay; a.az = S.az; a.dUdt = S.dUdt;
-    a.wA = c->nd.wA; a.wB = c->nd.wB; a.wD = c->nd.wD;
+    a.wA = c->nd.wA; a.wB = c->nd.wB; a.wD = c->nd.wD; a.wC = c->nd.wC;
     a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.childmask = c->nd.childmask; a.level = c->nd.level;
     a.mass = c->nd.mass; a.comx = c->nd.comx; a.comy = c->nd.comy; a.comz = c->nd.comz;
     a.gas = c->nd.gas; a.mvx = c->nd.mvx; a.mvy = c->nd.mvy; a.mvz = c->nd.mvz;
