@@ -47,7 +47,7 @@ def _stale(target: str, deps: list[str]) -> bool:
 # results must not depend on which variant (with or without SPH, register
 # budget) the compiler contracted differently, and the reference (x86-64
 # without -march) does not contract either.  Intended FMAs are written as fmaf.
-FILE_FLAGS = {"ag2_walk.cu": ["-fmad=false"]}
+FILE_FLAGS = {"ag2_walk.cu": ["-fmad=false", "-ftz=true"]}
 
 
 def _compile(src: str, headers: list[str]) -> str:

@@ -389,8 +389,13 @@ __device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
 
 // Force loop over the interaction list: every lane evaluates every entry and
 // keeps it when its bit is set (predicated, no branches), summing into a batch
-// that is added to the compensated accumulator once per flush.
-template <bool kGeneral>
+// that is added to the compensated accumulator once per flush.  With kOneRsq
+// the factor 1 / (r (r^2 + e^2)) is one reciprocal square root of
+// r^2 (r^2 + e^2)^2 instead of a reciprocal square root and a reciprocal; the
+// caller takes it when e0^2 (scaled) exceeds 3e-9, where every distance the
+// list holds (r^2 above 1e-12 e0^2, smaller ones go to the FP64 path) keeps
+// that product above 1e-12 e0^6 > 2.7e-37, inside FP32's normal range.
+template <bool kGeneral, bool kOneRsq = false>
 __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane, float ox, float oy, float oz,
                                            float eps02, double e0, double ls, float &sx, float &sy, float &sz,
                                            float &kx, float &ky, float &kz, unsigned long long &cnt_g)
@@ -417,7 +422,13 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
             mine += take ? 1 : 0;
         }
         // P.w = G m ls^2: the sum comes out in the caller's units
-        float sc = __fdividef(P.w * ir, r2 + e2);
+        float sc;
+        if (kOneRsq && !kGeneral) {
+            const float t = r2 + e2;
+            sc = P.w * rsqrtf(r2 * t * t);
+        } else {
+            sc = __fdividef(P.w * ir, r2 + e2);
+        }
         sc = take ? sc : 0.f;
         bx = fmaf(dx, sc, bx);
         by = fmaf(dy, sc, by);
@@ -601,12 +612,10 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 nc = t ? __shfl_sync(0xffffffffu, incl, t - 1) : 0;
                 if (take) {
                     int q = incl - k;
-                    for (int o = 0; o < 8; o++)
-                        if ((cmk >> o) & 1u) {
-                            W.bchild[q] = ek.x + o;
-                            W.bmask[q] = (unsigned)ek.y;
-                            q++;
-                        }
+                    for (unsigned m = cmk; m; m &= m - 1u, q++) {  // the set octants only
+                        W.bchild[q] = ek.x + __ffs(m) - 1;
+                        W.bmask[q] = (unsigned)ek.y;
+                    }
                 }
                 sp -= t;
             }
@@ -782,12 +791,20 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             __syncwarp();
             if (overflow) break;
             if (nl > kList - kBatch) {
-                flush_list<kGeneral>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
+                if (eps02 > 3e-9f)
+                    flush_list<kGeneral, true>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
+                else
+                    flush_list<kGeneral>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
                 nl = 0;
                 __syncwarp();
             }
         }
-        if (nl > 0) flush_list<kGeneral>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
+        if (nl > 0) {
+            if (eps02 > 3e-9f)
+                flush_list<kGeneral, true>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
+            else
+                flush_list<kGeneral>(W, nl, lane, ox, oy, oz, eps02, a.e0, ls, sx, sy, sz, kx, ky, kz, cnt_g);
+        }
         kahan_add(sx, kx, side.x);
         kahan_add(sy, ky, side.y);
         kahan_add(sz, kz, side.z);
