@@ -612,10 +612,13 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 nc = t ? __shfl_sync(0xffffffffu, incl, t - 1) : 0;
                 if (take) {
                     int q = incl - k;
-                    for (unsigned m = cmk; m; m &= m - 1u, q++) {  // the set octants only
-                        W.bchild[q] = ek.x + __ffs(m) - 1;
-                        W.bmask[q] = (unsigned)ek.y;
-                    }
+#pragma unroll
+                    for (int o = 0; o < 8; o++)
+                        if ((cmk >> o) & 1u) {
+                            W.bchild[q] = ek.x + o;
+                            W.bmask[q] = (unsigned)ek.y;
+                            q++;
+                        }
                 }
                 sp -= t;
             }
