@@ -365,6 +365,9 @@ struct alignas(16) WarpSmem {
     unsigned cself[kBatch];     // lane whose own leaf this child is (bit), else 0
     unsigned bkeep[kBatch];     // lanes that evaluate batch slot j, less the one whose own leaf it is
     unsigned char mq[kBatch];   // batch slot of the q-th child the lanes decide one by one
+    float4 mpos[kBatch];        // ... its cpos, cthr and lane mask, in that order (no indirection in the loop)
+    float4 mthr[kBatch];
+    unsigned mkeep[kBatch];
     float4 lpos[kList];      // accepted nodes: relative com, mass
     unsigned lmask[kList];   // lanes that accepted them
     double xd[3][32];        // FP64 positions of the group (read only by the exact re-check)
@@ -714,18 +717,23 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             // lanes that accept / open that child, and the entries are placed at once
             if (mixed) {
                 const unsigned below = (1u << lane) - 1u;
-                if ((mixed >> lane) & 1u) W.mq[__popc(mixed & below)] = (unsigned char)lane;
+                if ((mixed >> lane) & 1u) {
+                    const int q = __popc(mixed & below);
+                    W.mq[q] = (unsigned char)lane;
+                    W.mpos[q] = W.cpos[lane];
+                    W.mthr[q] = W.cthr[lane];
+                    W.mkeep[q] = W.bkeep[lane];
+                }
                 __syncwarp();
                 const int nm = __popc(mixed);
                 unsigned accb = 0u, opnb = 0u, sphb = 0u, rqb = 0u;
 #pragma unroll 2
                 for (int q = 0; q < nm; q++) {
-                    const int j = W.mq[q];
                     const unsigned bit = 1u << q;
                     // the lanes that evaluate this child, except the one whose own leaf it is
-                    if ((W.bkeep[j] >> lane) & 1u) {
-                        const float4 Pc = W.cpos[j];
-                        const float4 T = W.cthr[j];
+                    if ((W.mkeep[q] >> lane) & 1u) {
+                        const float4 Pc = W.mpos[q];
+                        const float4 T = W.mthr[q];
                         const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
                         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                         const bool acc = r2 > T.w, opn = r2 > T.y && r2 < T.z;
