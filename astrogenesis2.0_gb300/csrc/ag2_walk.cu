@@ -761,18 +761,75 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                         if (kGas && gas_i && (decision == 1 || decision == 3) && r2 < h2x4) sphb |= 1u << q;
                     }
                 }
-                // SPH pairs of the gas lanes (rare): a separate pass keeps the loop above small
+                // SPH pairs (gas lane p, mixed child q): a separate pass keeps the loop
+                // above small.  The pairs are spread over all lanes, 32 at a time (gas
+                // lanes are few, so a loop per lane would leave most lanes idle); each
+                // lane then adds its own pairs' contributions in its bit order, as that
+                // loop would, so the sums are the same bits.
                 if (kGas && __any_sync(0xffffffffu, sphb != 0u)) {
+                    const int cp = __popc(sphb);
+                    int incl = cp;
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    const int ex = incl - cp;  // this lane's first pair
+                    const int total = __shfl_sync(0xffffffffu, incl, 31);
 #pragma unroll 1
-                    for (unsigned bq = sphb; bq; bq &= bq - 1u) {
-                        const int j = W.mq[__ffs(bq) - 1];
-                        const float4 D = W.cgas[j];
-                        if (D.w > 0.0f) {
-                            const float4 Pc = W.cpos[j];
-                            const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
-                            sph_pair32(D.w, -dx, -dy, -dz, dx * dx + dy * dy + dz * dz, vxi - D.x, vyi - D.y,
-                                       vzi - D.z, ih_, pr, cs, ls2f, side, du);
-                            cnt_s++;
+                    for (int k0 = 0; k0 < total; k0 += 32) {
+                        const int k = k0 + lane;
+                        int p = 0;  // owner: the last lane whose first pair is at or before k
+#pragma unroll
+                        for (int st = 16; st > 0; st >>= 1) {
+                            const int e = __shfl_sync(0xffffffffu, ex, p + st);
+                            if (e <= k) p += st;
+                        }
+                        const unsigned pb = __shfl_sync(0xffffffffu, sphb, p);
+                        const int pe = __shfl_sync(0xffffffffu, ex, p);
+                        const float pox = __shfl_sync(0xffffffffu, ox, p), poy = __shfl_sync(0xffffffffu, oy, p),
+                                    poz = __shfl_sync(0xffffffffu, oz, p), pih = __shfl_sync(0xffffffffu, ih_, p),
+                                    ppr = __shfl_sync(0xffffffffu, pr, p), pcs = __shfl_sync(0xffffffffu, cs, p),
+                                    pvx = __shfl_sync(0xffffffffu, vxi, p), pvy = __shfl_sync(0xffffffffu, vyi, p),
+                                    pvz = __shfl_sync(0xffffffffu, vzi, p);
+                        Vec3<float> f = {0.f, 0.f, 0.f};
+                        float dd = 0.f;
+                        if (k < total) {
+                            // the (k - pe)-th set bit of the owner's mask
+                            int rem = k - pe, q = 0;
+                            unsigned m = pb;
+#pragma unroll
+                            for (int w = 16; w > 0; w >>= 1) {
+                                const int c = __popc(m & ((1u << w) - 1u));
+                                if (rem >= c) {
+                                    rem -= c;
+                                    m >>= w;
+                                    q += w;
+                                }
+                            }
+                            const int j = W.mq[q];
+                            const float4 D = W.cgas[j];
+                            if (D.w > 0.0f) {
+                                const float4 Pc = W.cpos[j];
+                                const float dx = Pc.x - pox, dy = Pc.y - poy, dz = Pc.z - poz;
+                                sph_pair32(D.w, -dx, -dy, -dz, dx * dx + dy * dy + dz * dz, pvx - D.x, pvy - D.y,
+                                           pvz - D.z, pih, ppr, pcs, ls2f, f, dd);
+                                cnt_s++;
+                            }
+                        }
+                        // this lane's pairs in the chunk sit in lanes [wb, we)
+                        const int wb = max(ex - k0, 0), we = min(ex + cp - k0, 32);
+                        const int mine = max(we - wb, 0);
+                        const int most = (int)__reduce_max_sync(0xffffffffu, (unsigned)mine);
+                        for (int s = 0; s < most; s++) {
+                            const int w = (wb + s) & 31;
+                            const float rx = __shfl_sync(0xffffffffu, f.x, w), ry = __shfl_sync(0xffffffffu, f.y, w),
+                                        rz = __shfl_sync(0xffffffffu, f.z, w), rd = __shfl_sync(0xffffffffu, dd, w);
+                            if (s < mine) {
+                                side.x += rx;
+                                side.y += ry;
+                                side.z += rz;
+                                du += rd;
+                            }
                         }
                     }
                 }
