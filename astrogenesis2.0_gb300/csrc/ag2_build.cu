@@ -95,16 +95,24 @@ __global__ void k_slot_of(int n, const int32_t *__restrict__ id, int32_t *__rest
 }
 
 // first level: task (first caller index, count, destination) over particles
-__global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const double *px, const double *py,
-                                 const double *pz, const int32_t *slot_of, double *buf)
+// |x| of every particle once, in tree order (coalesced; the FP64 square root
+// is the costly part on this part)
+__global__ void k_dist(int n, const double *__restrict__ px, const double *__restrict__ py,
+                       const double *__restrict__ pz, double *__restrict__ dist)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dist[i] = dist0(px[i], py[i], pz[i]);
+}
+
+__global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const double *__restrict__ dist,
+                                 const int32_t *slot_of, double *buf)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntask) return;
     const int4 q = task[t];
     double s = 0.0, s2 = 0.0;
     for (int j = 0; j < q.y; j++) {
-        const int i = slot_of[q.x + j];
-        const double d = dist0(px[i], py[i], pz[i]);
+        const double d = dist[slot_of[q.x + j]];
         s = __dadd_rn(s, d);
         s2 = __dadd_rn(s2, __dmul_rn(d, d));
     }
@@ -146,14 +154,14 @@ __global__ void k_width_thr(int n_inst, const int64_t *first, const int32_t *fin
 }
 
 // R = max |x| over |x| <= thr (Tree.cpp:107-116); a NaN threshold keeps R = 0
-__global__ void k_width_max(int n, const double *px, const double *py, const double *pz, const int32_t *pinst,
-                            const double *thr, double *R)
+__global__ void k_width_max(int n, const double *__restrict__ dist, const int32_t *pinst, const double *thr,
+                            double *R)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int k = i < n ? pinst[i] : -1;
     unsigned long long best = 0ull;
     if (i < n) {
-        const double d = dist0(px[i], py[i], pz[i]);
+        const double d = dist[i];
         if (d <= thr[k] && d > 0.0) best = (unsigned long long)__double_as_longlong(d);
     }
     const unsigned peers = __match_any_sync(0xffffffffu, k);
@@ -1836,11 +1844,12 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     AG2_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(Ctx::Ctl), c->stream));
     if (n > 0) {
         AG2_LAUNCH(c, k_slot_of, grid_for(n, kBlock), kBlock, 0, n, S.id, c->slot_of);
+        AG2_LAUNCH(c, k_dist, grid_for(n, kBlock), kBlock, 0, n, S.px, S.py, S.pz, c->rdist);
         for (size_t l = 0; l + 1 < c->wsum_level.size(); l++) {
             const int nt = c->wsum_level[l + 1] - c->wsum_level[l];
             const int4 *tk = c->wsum_task + c->wsum_level[l];
             if (l == 0)
-                AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, S.px, S.py, S.pz, c->slot_of,
+                AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->rdist, c->slot_of,
                            c->width_part);
             else
                 AG2_LAUNCH(c, k_wsum_sums, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->width_part);
@@ -1849,8 +1858,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     AG2_LAUNCH(c, k_width_thr, grid_for(K, kBlock), kBlock, 0, K, c->inst_first, c->wsum_final, c->width_part,
                c->width_thr, c->inst_R);
     if (n > 0)
-        AG2_LAUNCH(c, k_width_max, grid_for(n, kBlock), kBlock, 0, n, S.px, S.py, S.pz, c->pinst, c->width_thr,
-                   c->inst_R);
+        AG2_LAUNCH(c, k_width_max, grid_for(n, kBlock), kBlock, 0, n, c->rdist, c->pinst, c->width_thr, c->inst_R);
     phase_mark(c, "build: root width");
     if (!capture && (rc = ensure_node_capacity(c, (size_t)K + 1024)) != AG2_OK) return rc;
     const int thresh = c->prm.split_threshold;
