@@ -157,12 +157,31 @@ __global__ void k_width_thr(int n_inst, const int64_t *first, const int32_t *fin
 __global__ void k_width_max(int n, const double *__restrict__ dist, const int32_t *pinst, const double *thr,
                             double *R)
 {
+    __shared__ int32_t kmin, kmax;
+    __shared__ unsigned long long bbest;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int k = i < n ? pinst[i] : -1;
     unsigned long long best = 0ull;
     if (i < n) {
         const double d = dist[i];
         if (d <= thr[k] && d > 0.0) best = (unsigned long long)__double_as_longlong(d);
+    }
+    if (threadIdx.x == 0) {
+        kmin = INT32_MAX;
+        kmax = -1;
+        bbest = 0ull;
+    }
+    __syncthreads();
+    if (k >= 0) {
+        atomicMin_block(&kmin, k);
+        atomicMax_block(&kmax, k);
+    }
+    __syncthreads();
+    if (kmin == kmax) {  // one instance in the block (the usual case): one global atomic per block
+        if (best) atomicMax_block(&bbest, best);
+        __syncthreads();
+        if (threadIdx.x == 0 && bbest) atomicMax((unsigned long long *)&R[kmin], bbest);
+        return;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, k);
     best = group_reduce(peers, best, [](unsigned long long a, unsigned long long b) { return a > b ? a : b; });
@@ -314,7 +333,15 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
 {
     __shared__ int32_t sh[kBlock / 32 + 1];
     __shared__ int32_t sbase;
+    __shared__ int32_t jmin, jmax, bh[9];
+    if (threadIdx.x == 0) {
+        jmin = INT32_MAX;
+        jmax = -1;
+    }
+    if (threadIdx.x < 9) bh[threadIdx.x] = 0;
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int hj = -1, hd = 0;  // this particle's histogram entry
     bool act = false;
     int32_t *perm = const_cast<int32_t *>(b.perm);
     int32_t *posnode = const_cast<int32_t *>(b.posnode);
@@ -332,7 +359,10 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
             const_cast<int64_t *>(b.kz)[i] = kz;
             const int d = octant_digit(nd.bkey + 9 * (int64_t)k, kx, ky, kz);
             const_cast<uint8_t *>(b.digit)[i] = (uint8_t)d;
-            agg_inc(b.hist, 9 * j + d);
+            hj = j;
+            hd = d;
+            atomicMin_block(&jmin, j);
+            atomicMax_block(&jmax, j);
         } else {
             b.perm_final[i] = i;
             b.pnode[i] = k;  // one-particle root, or a serial root for k_local
@@ -342,6 +372,14 @@ __global__ void __launch_bounds__(kBlock) k_level0(int n, const int32_t *__restr
                 const_cast<int64_t *>(b.kz)[i] = okey(pz[i]);
             }
         }
+    }
+    __syncthreads();
+    if (jmin == jmax) {  // one root in the block (the usual case): block counts, one atomic per digit
+        if (hj >= 0) atomicAdd_block(&bh[hd], 1);
+        __syncthreads();
+        if (threadIdx.x < 9 && bh[threadIdx.x]) atomicAdd(&b.hist[9 * jmin + threadIdx.x], bh[threadIdx.x]);
+    } else if (hj >= 0) {
+        agg_inc(b.hist, 9 * hj + hd);
     }
     const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
     if (act) const_cast<int32_t *>(b.ap)[q] = i;
