@@ -336,15 +336,21 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
 
 // ---- FP32-offset walk --------------------------------------------------------
 
-__device__ __forceinline__ double warp_min(double v)
+// warp min / max of ordered integer keys (okey), on the integer pipe
+__device__ __forceinline__ long long warp_kmin(long long v)
 {
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-__device__ __forceinline__ double warp_max(double v)
+__device__ __forceinline__ long long warp_kmax(long long v)
 {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
+}
+// the double of an ordered key (okey's inverse; -0 comes back as +0)
+__device__ __forceinline__ double unkey(long long k)
+{
+    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFLL));
 }
 
 // Shared-memory layout per warp: the stack, the batch of up to 32 children
@@ -496,6 +502,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         const bool act = live && (!a.active || a.active[i]);  // block steps walk the due particles only
         const bool valid = act && a.m[i] != 0.0;
         // the instance's length scale: offsets, r^2, e0^2, h are in its units
+        const int lsk = walk_scale_exp(a.inst_R[root]);
         const double ls = walk_scale(a.inst_R[root]);
         const float eps02 = (float)(a.e0 * a.e0 * ls * ls);
         const float ls2f = (float)(ls * ls);
@@ -514,30 +521,29 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             W.xd[0][lane] = xi;
             W.xd[1][lane] = yi;
             W.xd[2][lane] = zi;
+            // the group's box: min and max of ordered integer keys (no FP64
+            // compare; this part issues FP64 at 1/64 of the FP32 rate)
             double gx = 0, gy = 0, gz = 0;
-            double lx = valid ? xi : 1e300, ly = valid ? yi : 1e300, lz = valid ? zi : 1e300;
-            double ux = valid ? xi : -1e300, uy = valid ? yi : -1e300, uz = valid ? zi : -1e300;
-            lx = warp_min(lx);
-            ly = warp_min(ly);
-            lz = warp_min(lz);
-            ux = warp_max(ux);
-            uy = warp_max(uy);
-            uz = warp_max(uz);
-            if (lx <= ux) {
-                gx = 0.5 * (lx + ux);
-                gy = 0.5 * (ly + uy);
-                gz = 0.5 * (lz + uz);
+            const long long kx = okey(xi), ky = okey(yi), kz = okey(zi);
+            const long long klx = warp_kmin(valid ? kx : LLONG_MAX), kly = warp_kmin(valid ? ky : LLONG_MAX),
+                            klz = warp_kmin(valid ? kz : LLONG_MAX);
+            const long long kux = warp_kmax(valid ? kx : LLONG_MIN), kuy = warp_kmax(valid ? ky : LLONG_MIN),
+                            kuz = warp_kmax(valid ? kz : LLONG_MIN);
+            if (klx <= kux) {
+                gx = scale2(unkey(klx) + unkey(kux), -1);
+                gy = scale2(unkey(kly) + unkey(kuy), -1);
+                gz = scale2(unkey(klz) + unkey(kuz), -1);
             }
-            const double sgx = gx * ls, sgy = gy * ls, sgz = gz * ls;
+            const double sgx = scale2(gx, lsk), sgy = scale2(gy, lsk), sgz = scale2(gz, lsk);
             ghx = (float)sgx;
             ghy = (float)sgy;
             ghz = (float)sgz;
             glx = (float)(sgx - (double)ghx);
             gly = (float)(sgy - (double)ghy);
             glz = (float)(sgz - (double)ghz);
-            ox = (float)((xi - gx) * ls);
-            oy = (float)((yi - gy) * ls);
-            oz = (float)((zi - gz) * ls);
+            ox = (float)scale2(xi - gx, lsk);
+            oy = (float)scale2(yi - gy, lsk);
+            oz = (float)scale2(zi - gz, lsk);
             // opaque copies: the walk below sees plain floats
             asm volatile("" : "+f"(ghx), "+f"(ghy), "+f"(ghz), "+f"(glx), "+f"(gly), "+f"(glz));
             asm volatile("" : "+f"(ox), "+f"(oy), "+f"(oz));
@@ -550,10 +556,11 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             myleaf = (pn >= 0 && a.leafpos[pn] == i) ? pn : -1;
             if (kGas && a.type[i] == 2) {
                 gas_i = true;
-                hi_ = (float)(a.h[i] * ls);
+                hi_ = (float)scale2(a.h[i], lsk);
                 ih_ = 1.0f / hi_;
                 double rho = a.rho[i], P = a.P[i];
-                pr = (float)((P / (rho * rho) + P / (rho * rho)) * ls * ls);
+                const double q = P / (rho * rho);
+                pr = (float)scale2(q + q, 2 * lsk);  // P/rho^2 + P/rho^2 (Node.cpp:97), in scaled units
                 cs = (float)sqrt(kGamma * P / rho);
                 vxi = (float)a.vx[i];
                 vyi = (float)a.vy[i];
