@@ -438,10 +438,11 @@ __device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane,
         } else {
             sc = __fdividef(P.w * ir, r2 + e2);
         }
-        sc = take ? sc : 0.f;
-        bx = fmaf(dx, sc, bx);
-        by = fmaf(dy, sc, by);
-        bz = fmaf(dz, sc, bz);
+        if (take) {  // predicated accumulation
+            bx = fmaf(dx, sc, bx);
+            by = fmaf(dy, sc, by);
+            bz = fmaf(dz, sc, bz);
+        }
     }
     kahan_add(sx, kx, bx);
     kahan_add(sy, ky, by);
