@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 __syncwarp();
                 const int nm = __popc(mixed);
                 unsigned accb = 0u, opnb = 0u, sphb = 0u, rqb = 0u;
-#pragma unroll 2
+#pragma unroll 4
                 for (int q = 0; q < nm; q++) {
                     const unsigned bit = 1u << q;
                     // the lanes that evaluate this child, except the one whose own leaf it is
