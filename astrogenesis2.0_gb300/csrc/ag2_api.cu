@@ -235,10 +235,15 @@ int ensure_instance_tables(Ctx *c)
         c->inst_first_h = {0, (int64_t)c->n};
         c->inst_massInH_h = {c->prm.massInH};
     }
-    AG2_CUDA(c, cudaMemcpyAsync(c->inst_first, c->inst_first_h.data(), (K + 1) * sizeof(int64_t),
-                                cudaMemcpyHostToDevice, c->stream));
     AG2_CUDA(c, cudaMemcpyAsync(c->inst_massInH, c->inst_massInH_h.data(), K * sizeof(double), cudaMemcpyHostToDevice,
                                 c->stream));
+    if (c->inst_first_h == c->inst_tab_first) {  // same layout (an upload of the same particles): tables stand
+        c->inst_dirty = false;
+        c->gas_stats_dirty = true;
+        return AG2_OK;
+    }
+    AG2_CUDA(c, cudaMemcpyAsync(c->inst_first, c->inst_first_h.data(), (K + 1) * sizeof(int64_t),
+                                cudaMemcpyHostToDevice, c->stream));
     // root-width summation tasks (ag2_build.cu): one sequential task per instance
     // up to 4096 particles, a 64-ary tree of sequential runs above
     {
@@ -304,6 +309,7 @@ int ensure_instance_tables(Ctx *c)
     c->ngroups = (int32_t)g.size();
     if (c->n) AG2_LAUNCH(c, k_pinst, K, 256, 0, c->inst_first, c->pinst);
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors above go out of scope
+    c->inst_tab_first = c->inst_first_h;
     c->inst_dirty = false;
     c->gas_stats_dirty = true;
     return AG2_OK;

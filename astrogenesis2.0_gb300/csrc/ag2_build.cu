@@ -1677,6 +1677,12 @@ static int prepare_gas_tables(Ctx *c, int n)
         total += (size_t)cnt[k] + 1;
         c->ngas += cnt[k];
     }
+    // the tables are sequential partial sums k * m_gas (one thread per instance):
+    // an upload that keeps every instance's gas count and mass keeps them
+    if (cnt == c->gas_tab_cnt && lo == c->gas_tab_lo && hi == c->gas_tab_hi && total <= c->gas_prefix_cap) {
+        c->gas_stats_dirty = false;
+        return AG2_OK;
+    }
     if (total > c->gas_prefix_cap) {
         if (c->gas_prefix) cudaFree(c->gas_prefix);
         c->gas_prefix = nullptr;
@@ -1689,6 +1695,9 @@ static int prepare_gas_tables(Ctx *c, int n)
     AG2_LAUNCH(c, k_gas_prefix, grid_for(K, kBlock), kBlock, 0, K, c->gas_cnt, c->gas_kmin, c->gas_uni, c->gas_off,
                c->gas_prefix);
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors above go out of scope
+    c->gas_tab_cnt = cnt;
+    c->gas_tab_lo = lo;
+    c->gas_tab_hi = hi;
     c->gas_stats_dirty = false;
     return AG2_OK;
 }

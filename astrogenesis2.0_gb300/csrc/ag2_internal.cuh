@@ -186,6 +186,10 @@ struct Ctx {
     int32_t gas_table_n = -1;
     bool gas_uniform = false;
     bool gas_stats_dirty = true;  // masses or types changed since the last statistics
+    // what the gasMass tables in gas_prefix were built for (gas count and mass key
+    // per instance): a table is a sequential sum, rebuilt only when these change
+    std::vector<int32_t> gas_tab_cnt;
+    std::vector<long long> gas_tab_lo, gas_tab_hi;
     int32_t ngas = 0;
     double gas_mass_min = 0.0, gas_mass_max = 0.0;
     double tree_theta = 0.0;      // opening angle baked into the walk records
@@ -209,6 +213,7 @@ struct Ctx {
     size_t groups_cap = 0;
     bool inst_dirty = true;         // instance tables need uploading
     bool inst_explicit = false;     // layout from ag2_set_instances (keeps its massInH)
+    std::vector<int64_t> inst_tab_first;  // layout the device instance tables and walk groups describe
     // gasMass tables: instance k's sequential partial sums start at gas_off[k]
     int32_t *gas_off = nullptr;     // device
     uint8_t *gas_uni = nullptr;     // device: instance's gas particles share one mass

@@ -436,15 +436,16 @@ __global__ void k_ic_gadget(GadLayout L, const uint8_t *__restrict__ img, IcOut 
     out.tsfr[i] = 0.0;
 }
 
-// T, P and visualDensity from the loader's scratch into the freshly uploaded
-// state (upload order = tree order right after an upload)
+// T, P and visualDensity from the loader's scratch (upload order) into the
+// freshly uploaded state (slot i holds upload index s.id[i])
 __global__ void k_ic_fields(int64_t n, const double *T, const double *P, const double *vd, Particles s)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    s.T[i] = T[i];
-    if (P) s.P[i] = P[i];
-    s.vdens[i] = vd[i];
+    const int u = s.id[i];
+    s.T[i] = T[u];
+    if (P) s.P[i] = P[u];
+    s.vdens[i] = vd[u];
 }
 
 __global__ void k_tags_reset(int64_t n, uint32_t *tid, uint8_t *tgp, double *tsfr)
