@@ -301,7 +301,8 @@ int ensure_instance_tables(Ctx *c)
         for (int64_t s = b; s < e; s += 32) g.push_back(make_int4((int)s, (int)std::min<int64_t>(32, e - s), k, 0));
     }
     if (g.size() > c->groups_cap) {
-        if (!realloc_dev(c->groups, g.size())) return set_err(c, AG2_E_NOMEM, "group table allocation failed");
+        if (!realloc_dev(c->groups, g.size()) || !realloc_dev(c->retry_groups, g.size()))
+            return set_err(c, AG2_E_NOMEM, "group table allocation failed");
         c->groups_cap = g.size();
     }
     if (!g.empty())
@@ -397,7 +398,7 @@ int ag2_destroy(ag2_ctx *c)
     free_nodes(c->nd);
     void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->slot_of, c->rdist, c->finalnode,
                   c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
-                  c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->inst_first, c->inst_R,
+                  c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->retry_groups, c->inst_first, c->inst_R,
                   c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax,
                   c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);

@@ -209,6 +209,7 @@ struct Ctx {
     double *inst_massInH = nullptr; // device
     int32_t *pinst = nullptr;       // device, instance of each slot
     int4 *groups = nullptr;         // device walk groups: (first slot, lanes, instance, 0)
+    int32_t *retry_groups = nullptr; // device, groups_cap: groups for the FP32 walk's retry pass
     int32_t ngroups = 0;
     size_t groups_cap = 0;
     bool inst_dirty = true;         // instance tables need uploading
@@ -234,6 +235,8 @@ struct Ctx {
         long long gas_key_min, gas_key_max;
         unsigned long long inter_grav, inter_sph;
         int32_t list_count;
+        int32_t retry_count;    // FP32 walk: groups sent to the retry pass
+        int32_t retry_claim;    // ... and claimed by it
         int32_t ndrop_nodes;
         int32_t next_active;    // active slots at the next level
         int32_t nleaf;          // entries of the leaf list

@@ -34,7 +34,12 @@ namespace ag2 {
 namespace {
 
 constexpr int kWalkBlock = 128;  // 4 warps
-constexpr int kStack = 512;      // entries per warp
+constexpr int kStack = 512;      // stack entries per warp (FP64 walk, potential, FP32 retry pass)
+// The FP32 walk's first pass uses half that: six blocks fit an SM (shared
+// memory) instead of five.  The deepest stack measured on the bench workloads
+// is under 50 entries; a group that would overflow leaves its sums, goes to a
+// retry list and is walked again by a second launch with the full stack.
+constexpr int kStackFast = 256;
 constexpr float kGuard = 1e-5f;
 constexpr int kWalkVariants = 3;
 
@@ -53,6 +58,7 @@ struct WalkArgs {
     const int4 *groups;  // (first slot, lanes, instance = root node, 0)
     int ngroups;
     const uint8_t *active;  // per slot: walk it (block time steps); null = every particle
+    int32_t *retry_groups;  // groups the FP32 walk's first pass sends to the retry pass
     const double *inst_R;   // root half-width per instance: the FP32 walk's length scale (walk_scale)
     double theta, e0, G;
     Ctx::Ctl *ctl;
@@ -358,7 +364,8 @@ __device__ __forceinline__ double unkey(long long k)
 // + the lanes that accepted it) that the force loop consumes.
 constexpr int kBatch = 32;
 constexpr int kList = 96;
-struct alignas(16) WarpSmem {
+template <int kStk>
+struct alignas(16) WarpSmemT {
     float4 cpos[kBatch];     // com - group centre (lane-invariant part), mass
     float4 cgas[kBatch];     // gas velocity, gasMass
     float cmac[kBatch];      // (radius/theta)^2, or -1 for a leaf
@@ -377,8 +384,8 @@ struct alignas(16) WarpSmem {
     float4 lpos[kList];      // accepted nodes: relative com, mass
     unsigned lmask[kList];   // lanes that accepted them
     double xd[3][32];        // FP64 positions of the group (read only by the exact re-check)
-    int2 stk[kStack];        // (first child of a node to open, lane mask)
-    unsigned char stkcm[kStack];
+    int2 stk[kStk];          // (first child of a node to open, lane mask)
+    unsigned char stkcm[kStk];
 };
 
 // 32 x 32 bit transpose across the warp: lane i holds row i (bit j = column
@@ -404,8 +411,8 @@ __device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
 // caller takes it when e0^2 (scaled) exceeds 3e-9, where every distance the
 // list holds (r^2 above 1e-12 e0^2, smaller ones go to the FP64 path) keeps
 // that product above 1e-12 e0^6 > 2.7e-37, inside FP32's normal range.
-template <bool kGeneral, bool kOneRsq = false>
-__device__ __forceinline__ void flush_list(const WarpSmem &W, int cnt, int lane, float ox, float oy, float oz,
+template <bool kGeneral, bool kOneRsq = false, class WS>
+__device__ __forceinline__ void flush_list(const WS &W, int cnt, int lane, float ox, float oy, float oz,
                                            float eps02, double e0, double ls, float &sx, float &sy, float &sz,
                                            float &kx, float &ky, float &kz, unsigned long long &cnt_g)
 {
@@ -482,20 +489,26 @@ __device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, co
     return decision;
 }
 
-template <bool kGeneral, bool kGas, int kMinBlocks>
+// kRetry: the second pass over the groups the first one could not hold in its
+// stack (a.retry_groups, ctl->retry_count of them), with the full stack.
+template <bool kGeneral, bool kGas, int kMinBlocks, bool kRetry = false>
 __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
 {
-    __shared__ WarpSmem sm_all[kWalkBlock / 32];
+    constexpr int kStk = kRetry ? kStack : kStackFast;
+    using WS = WarpSmemT<kStk>;
+    __shared__ WS sm_all[kWalkBlock / 32];
     const int lane = threadIdx.x & 31;
-    WarpSmem &W = sm_all[threadIdx.x >> 5];
-    const int ngroups = a.ngroups;
+    WS &W = sm_all[threadIdx.x >> 5];
+    const int ngroups = kRetry ? a.ctl->retry_count : a.ngroups;
     const float G = (float)a.G;
     unsigned long long cnt_g = 0, cnt_s = 0;
     for (;;) {
         int grp = 0;
-        if (lane == 0) grp = atomicAdd(&a.ctl->list_count, 1);
+        if (lane == 0) grp = atomicAdd(kRetry ? &a.ctl->retry_claim : &a.ctl->list_count, 1);
         grp = __shfl_sync(0xffffffffu, grp, 0);
         if (grp >= ngroups) break;
+        if (kRetry) grp = a.retry_groups[grp];
+        const unsigned long long cg0 = cnt_g, cs0 = cnt_s;  // a group sent to the retry pass counts there
         const int4 gd = a.groups[grp];
         const int i = gd.x + lane;
         const bool live = lane < gd.y;
@@ -702,7 +715,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 const unsigned am = __ballot_sync(0xffffffffu, acc);
                 mixed = __ballot_sync(0xffffffffu, cls == 0);
                 const unsigned below = (1u << lane) - 1u;
-                if (sp + __popc(om) > kStack) {
+                if (sp + __popc(om) > kStk) {
                     overflow = true;
                 } else {
                     if (opn) {
@@ -853,7 +866,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 }
                 nl += __popc(hab);
                 const int nop = __popc(hob);
-                if (sp + nop > kStack) {
+                if (sp + nop > kStk) {
                     overflow = true;
                 } else {
                     if (ho) {
@@ -884,9 +897,18 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         kahan_add(sx, kx, side.x);
         kahan_add(sy, ky, side.y);
         kahan_add(sz, kz, side.z);
-        if (overflow && lane == 0) {
-            atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
-            atomicExch(&a.ctl->err_info, grp);
+        if (overflow) {
+            if (!kRetry) {  // the retry pass walks this group again with the full stack
+                if (lane == 0) a.retry_groups[atomicAdd(&a.ctl->retry_count, 1)] = grp;
+                cnt_g = cg0;
+                cnt_s = cs0;
+                __syncwarp();
+                continue;
+            }
+            if (lane == 0) {
+                atomicExch(&a.ctl->err_code, (int)AG2_E_STACK);
+                atomicExch(&a.ctl->err_info, grp);
+            }
         }
         if (act) {
             a.ax[i] = valid ? (double)sx - (double)kx : 0.0;
@@ -1044,6 +1066,7 @@ static WalkArgs walk_args(Ctx *c)
     a.radius = c->nd.radius;
     a.groups = c->groups;
     a.active = c->walk_active;
+    a.retry_groups = c->retry_groups;
     a.inst_R = c->inst_R;
     a.ngroups = c->ngroups;
     a.theta = c->prm.theta;
@@ -1097,6 +1120,7 @@ int run_forces(Ctx *c)
     const bool general = !(c->prm.e0 > 0.0 && c->prm.e0 < 0.6);
     const bool gas = c->ngas > 0;
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->retry_count, 0, 2 * sizeof(int32_t), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->inter_grav, 0, 2 * sizeof(unsigned long long), c->stream));
     const int dev_sms = c->sms;
     const int ngroups = c->ngroups;
@@ -1112,11 +1136,13 @@ int run_forces(Ctx *c)
     } else {
         // register budget variant (autotuned): 0 = compiler's choice, 1 = 80, 2 = 64
         const int v = c->walk_variant;
-#define W32(G, S)                                          \
-    do {                                                   \
-        if (v == 1) WALK((k_walk32<G, S, 6>));             \
-        else if (v == 2) WALK((k_walk32<G, S, 8>));        \
-        else WALK((k_walk32<G, S, 1>));                    \
+#define W32(G, S)                                                                 \
+    do {                                                                          \
+        if (v == 1) WALK((k_walk32<G, S, 6>));                                    \
+        else if (v == 2) WALK((k_walk32<G, S, 8>));                               \
+        else WALK((k_walk32<G, S, 1>));                                           \
+        /* groups whose stack outgrew the first pass (none in the usual case) */  \
+        AG2_LAUNCH(c, (k_walk32<G, S, 1, true>), dev_sms, kWalkBlock, 0, a);      \
     } while (0)
         if (general) {
             if (gas) W32(true, true); else W32(true, false);

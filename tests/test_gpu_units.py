@@ -92,3 +92,24 @@ def test_fp32_walk_far_from_origin_in_si():
     r64 = _run(d, G_SI, 0.02 * L, "fp64", offset=off)
     r32 = _run(d, G_SI, 0.02 * L, "fp32", offset=off)
     _check_contract(r32, r64, gas)
+
+
+def test_fp32_walk_deep_tree_matches_fp64():
+    """A tree whose walk stack outgrows the FP32 walk's first pass (clusters
+    nested down to 2^-40 of the box): the groups it cannot hold are walked
+    again with the full stack, so every particle still gets its force."""
+    rng = np.random.default_rng(3)
+    pts = []
+    for k in range(40):
+        s = 2.0 ** -k
+        c = np.array([s, 0.5 * s, 0.25 * s])
+        pts.append(c + rng.normal(0, 0.05 * s, (24, 3)))
+    pos = np.concatenate(pts + [rng.uniform(-1, 1, (4000, 3))])
+    n = len(pos)
+    d = {"pos": pos, "vel": np.zeros((n, 3)), "mass": np.full(n, 1.0 / n), "U": np.zeros(n),
+         "type": np.ones(n, np.uint8), "massInH": 0.0}
+    r64 = _run(d, 1.0, 1e-13, "fp64")
+    r32 = _run(d, 1.0, 1e-13, "fp32")
+    e = rel(r32["acc"], r64["acc"])
+    assert np.all(np.isfinite(r32["acc"])) and np.all(np.linalg.norm(r32["acc"], axis=1) > 0)
+    assert np.median(e) <= 1e-5 and np.quantile(e, 0.999) <= 1e-3, (np.median(e), e.max())
