@@ -171,7 +171,7 @@ void free_nodes(Nodes &d)
     void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs, d.childmask,
                   d.cx,    d.cy,    d.cz,    d.bkey,  d.mass,   d.comx,    d.comy, d.comz, d.gas,   d.mvx,
                   d.mvy,   d.mvz,   d.ngas,  d.tsum,
-                  d.wA,   d.wB,      d.wC,   d.wD,   d.flag, d.rho,
+                  d.wrec, d.flag, d.rho,
                   d.radius, d.inst, d.nlx, d.lint, d.lil};
     for (void *q : ps) cudaFree(q);
     d = Nodes{};
@@ -575,7 +575,7 @@ static unsigned long long fnv(unsigned long long h, const void *p, size_t n)
 static unsigned long long step_key(Ctx *c, double dt, double hubble, int with_visual, double Rv)
 {
     unsigned long long h = 1469598103934665603ull;
-    const void *ptrs[] = {c->nd.start, c->nd.bkey, c->nd.wA, c->nd.lint, c->hist, c->stream, c->gas_prefix,
+    const void *ptrs[] = {c->nd.start, c->nd.bkey, c->nd.wrec, c->nd.lint, c->hist, c->stream, c->gas_prefix,
                           c->groups, c->inst_first, c->leaves, c->pkey};
     h = fnv(h, ptrs, sizeof(ptrs));
     const int64_t sizes[] = {(int64_t)c->n, c->n_inst, (int64_t)c->node_cap, (int64_t)c->hist_cap, c->ngas,

@@ -857,7 +857,8 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     const double sx = scale2(cx, k), sy = scale2(cy, k), sz = scale2(cz, k);
     const float hx = (float)sx, hy = (float)sy, hz = (float)sz;
     const float lx = (float)(sx - (double)hx), ly = (float)(sy - (double)hy), lz = (float)(sz - (double)hz);
-    nd.wA[nid] = make_float4(hx, hy, hz, (float)scale2(mass, 2 * k));
+    WalkRec w;
+    w.A = make_float4(hx, hy, hz, (float)scale2(mass, 2 * k));
     float mac = -1.0f;
     if (!leaf) {
         // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2; FP32 is
@@ -865,12 +866,13 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
         const float q = (float)scale2(nd.radius[nid], k) / (float)ra.theta;
         mac = q * q;
     }
-    nd.wB[nid] = make_float4(lx, ly, lz, mac);
-    nd.wC[nid] = make_int4(nd.first[nid], nd.leafpos[nid], (int)cmask, 0);  // one load for the walk's child staging
+    w.B = make_float4(lx, ly, lz, mac);
+    w.C = make_int4(nd.first[nid], nd.leafpos[nid], (int)cmask, 0);
     if (leaf && lp >= 0)
-        nd.wD[nid] = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)scale2(gas, 2 * k));
+        w.D = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)scale2(gas, 2 * k));
     else
-        nd.wD[nid] = make_float4((float)mvx, (float)mvy, (float)mvz, (float)scale2(gas, 2 * k));
+        w.D = make_float4((float)mvx, (float)mvy, (float)mvz, (float)scale2(gas, 2 * k));
+    nd.wrec[nid] = w;
 }
 
 // Moments from the node's own mass set: the centre of mass and gas velocity as
@@ -1625,7 +1627,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
     G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
-    G(tsum) G(wA) G(wB) G(wC) G(wD) G(flag)
+    G(tsum) G(wrec) G(flag)
     G(rho) G(nlx) G(lint) G(lil)
 #undef G
     if ((rc = grow(c, d.bkey, 9 * old, 9 * nc)) != AG2_OK) return rc;

@@ -42,6 +42,18 @@ struct Particles {
     int32_t *id;
 };
 
+// A node's FP32 walk record, in the instance's scaled units: A = centre of mass
+// (hi floats) and mass * ls^2; B = centre of mass (lo floats) and the opening
+// threshold (radius * ls / theta)^2 (-1 for a leaf); C = first child (-1 leaf),
+// leaf particle slot (-1 none), child mask, 0; D = gas velocity (mVel, or the
+// leaf particle's velocity) and gasMass * ls^2.  One 64-byte record, so a staged
+// child is two sectors of one cache line.
+struct alignas(64) WalkRec {
+    float4 A, B;
+    int4 C;
+    float4 D;
+};
+
 // Sums of a node's whole routed range: mass, mass-weighted position, gas mass
 // and gas momentum, the mass of its lowest upload index, gas count and that
 // index.  80 bytes, written and read whole.
@@ -69,10 +81,7 @@ struct Nodes {
     // so a node's eight children are one contiguous read
     NodeSum *tsum;
     // walk records (FP32 view)
-    float4 *wA;  // com_hi.xyz, mass
-    float4 *wB;  // com_lo.xyz, mac radius^2 (leaf: -1)
-    float4 *wD;  // gas velocity (mVel or the leaf particle's velocity), gasMass
-    int4 *wC;    // first child (-1 leaf), leaf particle slot (-1 none), child mask, 0
+    WalkRec *wrec;  // FP32 walk record per node (64 B, one cache-line half)
     // SPH / visual density scratch
     uint8_t *flag;
     double *rho;

@@ -49,8 +49,7 @@ struct WalkArgs {
     const uint8_t *type;
     const int32_t *pnode;
     double *ax, *ay, *az, *dUdt;
-    const float4 *wA, *wB, *wD;
-    const int4 *wC;
+    const WalkRec *wrec;
     const int32_t *first, *leafpos;
     const uint8_t *childmask;
     const int8_t *level;
@@ -650,13 +649,14 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             // stage: lane j loads batch slot j (one round trip for the batch)
             if (lane < nc) {
                 const int c = W.bchild[lane];
-                const float4 A = a.wA[c];
-                const float4 B = a.wB[c];
-                const int4 C4 = a.wC[c];
+                const WalkRec *R = a.wrec + c;
+                const float4 A = R->A;
+                const float4 B = R->B;
+                const int4 C4 = R->C;
                 const int f = C4.x;
                 const unsigned char ccm = (unsigned char)C4.z;
                 float4 D;
-                if (kGas) D = a.wD[c];
+                if (kGas) D = R->D;
                 const float cx = (A.x - ghx) + (B.x - glx), cy = (A.y - ghy) + (B.y - gly),
                             cz = (A.z - ghz) + (B.z - glz);
                 W.cpos[lane] = make_float4(cx, cy, cz, G * A.w);
@@ -1037,13 +1037,13 @@ __global__ void __launch_bounds__(256) k_energy_sums(int n, const double *m, con
 }
 
 __global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double *radius, const int32_t *inst,
-                             const double *inst_R, float4 *wB, double theta)
+                             const double *inst_R, WalkRec *wrec, double theta)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     if (first[j] < 0) return;
     const float q = (float)scale2(radius[j], walk_scale_exp(inst_R[inst[j]])) / (float)theta;
-    wB[j].w = q * q;
+    wrec[j].B.w = q * q;
 }
 
 }  // namespace
@@ -1059,7 +1059,7 @@ static WalkArgs walk_args(Ctx *c)
     a.type = S.type;
     a.pnode = c->pnode;
     a.ax = S.ax; a.ay = S.ay; a.az = S.az; a.dUdt = S.dUdt;
-    a.wA = c->nd.wA; a.wB = c->nd.wB; a.wD = c->nd.wD; a.wC = c->nd.wC;
+    a.wrec = c->nd.wrec;
     a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.childmask = c->nd.childmask; a.level = c->nd.level;
     a.mass = c->nd.mass; a.comx = c->nd.comx; a.comy = c->nd.comy; a.comz = c->nd.comz;
     a.gas = c->nd.gas; a.mvx = c->nd.mvx; a.mvy = c->nd.mvy; a.mvz = c->nd.mvz;
@@ -1111,7 +1111,7 @@ int run_forces(Ctx *c)
     if (c->n == 0) return AG2_OK;
     if (c->prm.theta != c->tree_theta) {
         AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.radius,
-                   c->nd.inst, c->inst_R, c->nd.wB, c->prm.theta);
+                   c->nd.inst, c->inst_R, c->nd.wrec, c->prm.theta);
         c->tree_theta = c->prm.theta;
     }
     WalkArgs a = walk_args(c);
