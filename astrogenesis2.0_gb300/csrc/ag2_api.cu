@@ -169,8 +169,7 @@ void free_particles(Particles &p)
 void free_nodes(Nodes &d)
 {
     void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs, d.childmask,
-                  d.cx,    d.cy,    d.cz,    d.bkey,  d.mass,   d.comx,    d.comy, d.comz, d.gas,   d.mvx,
-                  d.mvy,   d.mvz,   d.ngas,  d.tsum,
+                  d.cx,    d.cy,    d.cz,    d.bkey,  d.mom,   d.tsum,
                   d.wrec, d.flag, d.rho,
                   d.radius, d.inst, d.nlx, d.lint, d.lil};
     for (void *q : ps) cudaFree(q);
@@ -916,14 +915,19 @@ int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle
     AG2_CUDA(c, cp(leafpos.data(), d.leafpos, nn * 4));
     AG2_CUDA(c, cp(level.data(), d.level, nn));
     AG2_CUDA(c, cp(mode.data(), d.mode, nn));
-    AG2_CUDA(c, cp(m.data(), d.mass, nn * 8));
-    AG2_CUDA(c, cp(cx.data(), d.comx, nn * 8));
-    AG2_CUDA(c, cp(cy.data(), d.comy, nn * 8));
-    AG2_CUDA(c, cp(cz.data(), d.comz, nn * 8));
-    AG2_CUDA(c, cp(g.data(), d.gas, nn * 8));
-    AG2_CUDA(c, cp(vx.data(), d.mvx, nn * 8));
-    AG2_CUDA(c, cp(vy.data(), d.mvy, nn * 8));
-    AG2_CUDA(c, cp(vz.data(), d.mvz, nn * 8));
+    // one field of every NodeMom record: a strided copy
+    auto cpm = [&](double *dst, size_t field) {
+        return cudaMemcpy2DAsync(dst, sizeof(double), reinterpret_cast<const char *>(d.mom) + field * sizeof(double),
+                                 sizeof(NodeMom), sizeof(double), nn, cudaMemcpyDeviceToHost, c->stream);
+    };
+    AG2_CUDA(c, cpm(m.data(), 0));
+    AG2_CUDA(c, cpm(cx.data(), 1));
+    AG2_CUDA(c, cpm(cy.data(), 2));
+    AG2_CUDA(c, cpm(cz.data(), 3));
+    AG2_CUDA(c, cpm(g.data(), 4));
+    AG2_CUDA(c, cpm(vx.data(), 5));
+    AG2_CUDA(c, cpm(vy.data(), 6));
+    AG2_CUDA(c, cpm(vz.data(), 7));
     AG2_CUDA(c, cp(ccx.data(), d.cx, nn * 8));
     AG2_CUDA(c, cp(ccy.data(), d.cy, nn * 8));
     AG2_CUDA(c, cp(ccz.data(), d.cz, nn * 8));

@@ -840,15 +840,16 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     ts.first_id = tot.first_id;
     nd.tsum[nid] = ts;
     nd.childmask[nid] = cmask;
-    nd.mass[nid] = mass;
-    nd.comx[nid] = cx;
-    nd.comy[nid] = cy;
-    nd.comz[nid] = cz;
-    nd.gas[nid] = gas;
-    nd.mvx[nid] = mvx;
-    nd.mvy[nid] = mvy;
-    nd.mvz[nid] = mvz;
-    nd.ngas[nid] = ng;
+    NodeMom mm;
+    mm.mass = mass;
+    mm.cx = cx;
+    mm.cy = cy;
+    mm.cz = cz;
+    mm.gas = gas;
+    mm.mvx = mvx;
+    mm.mvy = mvy;
+    mm.mvz = mvz;
+    nd.mom[nid] = mm;
     // FP32 walk record, lengths in the instance's scaled units (walk_scale):
     // COM split into hi + lo floats, mass * ls^2 (the walk's accelerations come
     // out in the caller's units), (radius/theta)^2, gasMass * ls^2 (the FP32
@@ -1032,7 +1033,7 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
         const int64_t c = first + o;
         if (nd.count[c] == 0) continue;
         own.add_node(nd, c);
-        if ((dbits(nd.mass[c]) << 1) != 0) cmask |= (uint8_t)(1u << o);  // mass != 0, on the bits
+        if ((dbits(nd.mom[c].mass) << 1) != 0) cmask |= (uint8_t)(1u << o);  // mass != 0, on the bits
     }
     tot = own;
     for (int32_t k = cnt - ndrop; k < cnt; k++) tot.add_particle(P, idx(k));
@@ -1626,7 +1627,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
 #define G(x) \
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
     G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
-    G(cx) G(cy) G(cz) G(radius) G(inst) G(mass) G(comx) G(comy) G(comz) G(gas) G(mvx) G(mvy) G(mvz) G(ngas)
+    G(cx) G(cy) G(cz) G(radius) G(inst) G(mom)
     G(tsum) G(wrec) G(flag)
     G(rho) G(nlx) G(lint) G(lil)
 #undef G

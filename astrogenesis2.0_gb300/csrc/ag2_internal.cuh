@@ -42,6 +42,12 @@ struct Particles {
     int32_t *id;
 };
 
+// A node's moments as the reference keeps them (Node.h): mass, centre of mass,
+// gasMass and the gas velocity mVel.  One 64-byte record per node.
+struct alignas(64) NodeMom {
+    double mass, cx, cy, cz, gas, mvx, mvy, mvz;
+};
+
 // A node's FP32 walk record, in the instance's scaled units: A = centre of mass
 // (hi floats) and mass * ls^2; B = centre of mass (lo floats) and the opening
 // threshold (radius * ls / theta)^2 (-1 for a leaf); C = first child (-1 leaf),
@@ -74,9 +80,8 @@ struct Nodes {
     double *radius;      // half-width (the root's R halved per level, exactly as Node.cpp:440)
     int32_t *inst;       // simulation instance the node belongs to
     int64_t *bkey;       // 9 ordered-integer keys per node: lo xyz, hi xyz, centre xyz
-    // moments (reference semantics, FP64)
-    double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz;
-    int32_t *ngas;
+    // moments (reference semantics, FP64), one record per node
+    NodeMom *mom;
     // sums over the whole routed range (bottom-up helper), one record per node
     // so a node's eight children are one contiguous read
     NodeSum *tsum;

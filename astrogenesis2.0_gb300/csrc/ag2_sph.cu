@@ -34,7 +34,8 @@ struct TreeView {
     const int32_t *start, *count, *ndrop, *parent, *leafpos, *pnode, *refnode;
     const int8_t *level;
     const uint8_t *mode;
-    const double *mass, *comx, *comy, *comz, *gas, *radius;
+    const NodeMom *mom;
+    const double *radius;
     const int32_t *pinst;
 };
 
@@ -50,11 +51,7 @@ TreeView view(Ctx *c)
     t.refnode = c->refnode;
     t.level = c->nd.level;
     t.mode = c->nd.mode;
-    t.mass = c->nd.mass;
-    t.comx = c->nd.comx;
-    t.comy = c->nd.comy;
-    t.comz = c->nd.comz;
-    t.gas = c->nd.gas;
+    t.mom = c->nd.mom;
     t.radius = c->nd.radius;
     t.pinst = c->pinst;
     return t;
@@ -82,11 +79,11 @@ __global__ void k_climb(int n, TreeView t, const uint8_t *type, const double *in
     if (pn < 0) return;  // Particle::node is null
     int64_t nd = pn;
     for (;;) {
-        double g = t.gas[nd];
+        double g = t.mom[nd].gas;
         if (g == 0) return;
         int32_t par = t.parent[nd];
         if (par < 0) return;
-        double md = M - g, pmd = M - t.gas[par];
+        double md = M - g, pmd = M - t.mom[par].gas;
         if (g < M && fabs(md) > fabs(pmd)) {
             nd = par;
             continue;
@@ -141,7 +138,7 @@ __global__ void k_rho(TreeView t, const double *px, const double *py, const doub
     if (w >= ctl->list_count) return;
     int64_t nd = list[w];
     double h = t.radius[nd] * 2;  // h = radius * 2 (Node.cpp:765)
-    double cx = t.comx[nd], cy = t.comy[nd], cz = t.comz[nd];
+    double cx = t.mom[nd].cx, cy = t.mom[nd].cy, cz = t.mom[nd].cz;
     int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
     uint8_t md = t.mode[nd];
     double acc = 0.0;
@@ -199,7 +196,7 @@ __global__ void k_vclimb(int n, TreeView t, double Rv, uint8_t *flag)
             continue;
         }
         double vol = r * r * r;
-        double mass = t.mass[nd];
+        double mass = t.mom[nd].mass;
         if (vol == 0 || mass == 0) return;
         double dens = mass / vol;
         if (dens == 0 || isinf(dens)) return;
@@ -217,7 +214,7 @@ __global__ void k_vfinal(int n, TreeView t, const uint8_t *flag, double *vdens)
     while (nd >= 0) {
         if (flag[nd] && cp_member(t, nd, i)) {
             double r = t.radius[nd];
-            v = t.mass[nd] / (r * r * r);
+            v = t.mom[nd].mass / (r * r * r);
         }
         nd = t.parent[nd];
     }

@@ -53,7 +53,8 @@ struct WalkArgs {
     const int32_t *first, *leafpos;
     const uint8_t *childmask;
     const int8_t *level;
-    const double *mass, *comx, *comy, *comz, *gas, *mvx, *mvy, *mvz, *radius;
+    const NodeMom *mom;
+    const double *radius;
     const int4 *groups;  // (first slot, lanes, instance = root node, 0)
     int ngroups;
     const uint8_t *active;  // per slot: walk it (block time steps); null = every particle
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
         const unsigned all = __ballot_sync(0xffffffffu, valid);
         int sp = 0;
         bool overflow = false;
-        if (all && a.mass[root] != 0.0) {
+        if (all && a.mom[root].mass != 0.0) {
             stk[0] = make_int2(root, (int)all);  // evaluate the root itself
             sp = 1;
         }
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
             const int32_t fc = a.first[c];
             const bool leaf = fc < 0;
             if (in && !(leaf && c == myleaf)) {
-                double dx = a.comx[c] - xi, dy = a.comy[c] - yi, dz = a.comz[c] - zi;
+                double dx = a.mom[c].cx - xi, dy = a.mom[c].cy - yi, dz = a.mom[c].cz - zi;
                 double r = sqrt(dx * dx + dy * dy + dz * dz);
                 if (r != 0.0) {
                     bool interact = leaf;
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
                         bool ok = true;
                         if (kGeneral) ok = general_eps2(r, a.e0, &e2);
                         if (ok) {
-                            double s = a.G * a.mass[c] / (r * r + e2);
+                            double s = a.G * a.mom[c].mass / (r * r + e2);
                             double gx = (dx / r) * s, gy = (dy / r) * s, gz = (dz / r) * s;
                             if (!(isnan(gx) || isnan(gy) || isnan(gz))) {
                                 acc.x += gx;
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
                                 acc.z += gz;
                                 cnt_g++;
                                 if (kGas && gas_i && r < hi_ * 2) {
-                                    double gm = a.gas[c];
+                                    double gm = a.mom[c].gas;
                                     if (gm > 0) {
                                         double vjx, vjy, vjz;
                                         if (leaf) {
@@ -286,9 +287,9 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
                                             vjy = a.vy[lp];
                                             vjz = a.vz[lp];
                                         } else {
-                                            vjx = a.mvx[c];
-                                            vjy = a.mvy[c];
-                                            vjz = a.mvz[c];
+                                            vjx = a.mom[c].mvx;
+                                            vjy = a.mom[c].mvy;
+                                            vjz = a.mom[c].mvz;
                                         }
                                         sph_pair<double>(gm, -dx, -dy, -dz, r, vxi - vjx, vyi - vjy, vzi - vjz, hi_,
                                                          pr, cs, acc, du);
@@ -470,14 +471,14 @@ __device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, co
                                          bool tiny, Vec3<float> &bs, unsigned long long &cnt_g)
 {
     const double xi = xd[0][lane], yi = xd[1][lane], zi = xd[2][lane];
-    double ddx = a.comx[c] - xi, ddy = a.comy[c] - yi, ddz = a.comz[c] - zi;
+    double ddx = a.mom[c].cx - xi, ddy = a.mom[c].cy - yi, ddz = a.mom[c].cz - zi;
     double r = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
     if (r == 0.0) return 0;
     int decision = (leaf || a.radius[c] / r < a.theta) ? 1 : 2;
     if (decision == 1 && tiny) {
         double e2 = a.e0 * a.e0;
         if (!kGeneral || general_eps2(r, a.e0, &e2)) {
-            double sc = a.G * a.mass[c] / (r * r + e2);
+            double sc = a.G * a.mom[c].mass / (r * r + e2);
             bs.x += (float)((ddx / r) * sc);
             bs.y += (float)((ddy / r) * sc);
             bs.z += (float)((ddz / r) * sc);
@@ -602,7 +603,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
         int sp = 0, nl = 0;
         bool overflow = false;
         // the root is the only child of a virtual parent (decided like any child)
-        if (all && a.mass[root] != 0.0) {
+        if (all && a.mom[root].mass != 0.0) {
             if (lane == 0) {
                 W.stk[0] = make_int2(root, (int)all);
                 W.stkcm[0] = 1;
@@ -960,7 +961,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_potential(WalkArgs a, double *ph
         const unsigned all = __ballot_sync(0xffffffffu, valid);
         int sp = 0;
         bool overflow = false;
-        if (all && a.mass[gd.z] != 0.0) {
+        if (all && a.mom[gd.z].mass != 0.0) {
             stk[0] = make_int2(gd.z, (int)all);
             sp = 1;
         }
@@ -975,11 +976,11 @@ __global__ void __launch_bounds__(kWalkBlock) k_potential(WalkArgs a, double *ph
             const int32_t fc = a.first[c];
             const bool leaf = fc < 0;
             if (in && !(leaf && c == myleaf)) {
-                const double dx = a.comx[c] - xi, dy = a.comy[c] - yi, dz = a.comz[c] - zi;
+                const double dx = a.mom[c].cx - xi, dy = a.mom[c].cy - yi, dz = a.mom[c].cz - zi;
                 const double r = sqrt(dx * dx + dy * dy + dz * dz);
                 if (r != 0.0) {
                     if (leaf || a.radius[c] / r < a.theta) {
-                        const double t = -(a.G * a.mass[c] / e0) * atan(e0 / r);
+                        const double t = -(a.G * a.mom[c].mass / e0) * atan(e0 / r);
                         if (!isnan(t)) p += t;
                     } else {
                         open = true;
@@ -1061,8 +1062,7 @@ static WalkArgs walk_args(Ctx *c)
     a.ax = S.ax; a.ay = S.ay; a.az = S.az; a.dUdt = S.dUdt;
     a.wrec = c->nd.wrec;
     a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.childmask = c->nd.childmask; a.level = c->nd.level;
-    a.mass = c->nd.mass; a.comx = c->nd.comx; a.comy = c->nd.comy; a.comz = c->nd.comz;
-    a.gas = c->nd.gas; a.mvx = c->nd.mvx; a.mvy = c->nd.mvy; a.mvz = c->nd.mvz;
+    a.mom = c->nd.mom;
     a.radius = c->nd.radius;
     a.groups = c->groups;
     a.active = c->walk_active;
