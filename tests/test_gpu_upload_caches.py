@@ -1,0 +1,69 @@
+"""Uploads keep the gasMass tables and the instance tables when nothing they
+depend on changed (the end-to-end step loop uploads the same particles every
+step).  These tests change exactly what the tables depend on between uploads
+and check every result against a fresh context, bit for bit."""
+import numpy as np
+import pytest
+
+import ics
+
+pytestmark = pytest.mark.gpu
+
+
+def _step_once(c, d):
+    c.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    if "first" in d:
+        c.set_instances(d["first"], d.get("mih"))
+    c.build_tree()
+    c.sph_density()
+    c.forces()
+    return {k: c.download(k) for k in ("h", "rho", "acc", "dUdt")}
+
+
+def _fresh(d, **kw):
+    import ag2
+
+    c = ag2.Context(len(d["mass"]), **kw)
+    r = _step_once(c, d)
+    c.close()
+    return r
+
+
+def _same(a, b):
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_gas_mass_change_rebuilds_table():
+    import ag2
+
+    d = ics.small_gas_cloud(3000, seed=9)
+    kw = dict(e0=0.02, theta=0.5, massInH=d["massInH"])
+    c = ag2.Context(3000, **kw)
+    _same(_step_once(c, d), _fresh(d, **kw))
+    d2 = dict(d)
+    d2["mass"] = d["mass"] * np.where(d["type"] == 2, 1.5, 1.0)  # gas particles heavier
+    _same(_step_once(c, d2), _fresh(d2, **kw))
+    d3 = dict(d2)
+    t = d2["type"].copy()
+    t[np.flatnonzero(t == 2)[:100]] = 1  # fewer gas particles
+    d3["type"] = t
+    _same(_step_once(c, d3), _fresh(d3, **kw))
+    _same(_step_once(c, d3), _fresh(d3, **kw))  # unchanged: the kept tables
+
+
+def test_instance_layout_change_with_same_count():
+    import ag2
+
+    parts = [ics.small_gas_cloud(n, seed=20 + k) for k, n in enumerate((700, 1300, 1000))]
+    d = {k: np.concatenate([p[k] for p in parts]) for k in ("pos", "vel", "mass", "type", "U")}
+    d["first"] = np.array([0, 700, 2000, 3000])
+    d["mih"] = np.array([p["massInH"] for p in parts])
+    kw = dict(e0=0.02, theta=0.5)
+    c = ag2.Context(3000, **kw)
+    _same(_step_once(c, d), _fresh(d, **kw))
+    d2 = dict(d)
+    d2["first"] = np.array([0, 2000, 3000])  # same particles, two simulations now
+    d2["mih"] = np.array([parts[0]["massInH"], parts[2]["massInH"]])
+    _same(_step_once(c, d2), _fresh(d2, **kw))
+    _same(_step_once(c, d), _fresh(d, **kw))
