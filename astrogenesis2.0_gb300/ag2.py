@@ -31,7 +31,7 @@ EXPORTS = [
     "ag2_last_error_string", "ag2_upload", "ag2_upload_device", "ag2_set_field", "ag2_download", "ag2_count",
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
-    "ag2_topology", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
+    "ag2_topology", "ag2_walk_records", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
     "ag2_diagnostics", "ag2_fp32_peak_probe", "ag2_autotune", "ag2_root_radius_noalloc", "ag2_phase_timing",
     "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy", "ag2_step_graphs",
     "ag2_block_init", "ag2_block_step", "ag2_set_tags", "ag2_get_tags", "ag2_snapshot_size",
@@ -95,6 +95,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
                                  ctypes.POINTER(ctypes.c_int32)]
     L.ag2_topology.argtypes = [P] * 12
     L.ag2_particle_node.argtypes = [P, P]
+    L.ag2_walk_records.argtypes = [P, P]
     L.ag2_interactions.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.ag2_direct_sum.argtypes = [P, ctypes.c_size_t, P, P]
     L.ag2_diagnostics.argtypes = [P, P]
@@ -401,6 +402,13 @@ class Context:
                  "radius"]
         self._check(self.L.ag2_topology(self.h, *[_ptr(t[k]) for k in order]))
         return t
+
+    def walk_records(self) -> np.ndarray:
+        """The FP32 walk's node records, (nodes, 16) float32 in topology() order."""
+        nn, _, _ = self.node_count()
+        out = np.empty((nn, 16), np.float32)
+        self._check(self.L.ag2_walk_records(self.h, _ptr(out)))
+        return out
 
 
 def ic_count(path: str, fmt: str) -> int:

@@ -890,6 +890,34 @@ int ag2_particle_node(ag2_ctx *c, int64_t *out)
     return AG2_OK;
 }
 
+int ag2_walk_records(ag2_ctx *c, float *out16)
+{
+    if (!c || !out16) return AG2_E_INVALID;
+    if (!c->have_tree) return set_err(c, AG2_E_INVALID, "no tree");
+    const int64_t nn = c->nnodes;
+    std::vector<int32_t> first(nn), count(nn);
+    std::vector<WalkRec> rec(nn);
+    AG2_CUDA(c, cudaMemcpyAsync(first.data(), c->nd.first, nn * 4, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(count.data(), c->nd.count, nn * 4, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(rec.data(), c->nd.wrec, nn * sizeof(WalkRec), cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<int64_t> stack;
+    for (int r = c->n_inst - 1; r >= 0; r--) stack.push_back(r);
+    int64_t k = 0;
+    while (!stack.empty()) {
+        const int64_t v = stack.back();
+        stack.pop_back();
+        float *o = out16 + 16 * k++;
+        if (count[v] > 0)
+            std::memcpy(o, &rec[v], sizeof(WalkRec));
+        else
+            std::memset(o, 0, sizeof(WalkRec));
+        if (first[v] >= 0)
+            for (int q = 7; q >= 0; q--) stack.push_back(first[v] + q);
+    }
+    return AG2_OK;
+}
+
 int ag2_topology(ag2_ctx *c, int32_t *depth, int32_t *is_leaf, int32_t *particle, int64_t *cp_count,
                  uint64_t *cp_hash, double *mass, double *com3, double *gas_mass, double *mvel3, double *center3,
                  double *radius)

@@ -818,7 +818,7 @@ __device__ __forceinline__ double div_back(double x, double m, double q)
 // node record shared by leaves and internal nodes: moments, FP32 walk records
 // what the FP32 walk records need beyond a node's moments
 struct RecArgs {
-    double theta;
+    float theta;           // (float)theta, rounded once on the host
     const double *inst_R;  // root half-width per instance (walk_scale)
 };
 
@@ -864,7 +864,7 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     if (!leaf) {
         // accept when radius/r < theta  <=>  r^2 > (radius/theta)^2; FP32 is
         // enough for the threshold the FP32 walk tests with its guard band
-        const float q = (float)scale2(nd.radius[nid], k) / (float)ra.theta;
+        const float q = (float)scale2(nd.radius[nid], k) / ra.theta;
         mac = q * q;
     }
     w.B = make_float4(lx, ly, lz, mac);
@@ -2025,7 +2025,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     // deepest first (the internal-node list bucketed by level)
     const unsigned gl = capture ? fixed_grid : std::max(1u, grid_for(c->nleaves, kBlock));
     AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, c->ctl, c->leaves, c->nd, c->S(), c->gas_prefix, c->gas_off,
-               c->gas_uni, RecArgs{c->prm.theta, c->inst_R});
+               c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
     const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
     AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint);
     if (capture) {
@@ -2038,7 +2038,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil);
         rc = capture_while(c, h, [&]() -> int {
             AG2_LAUNCH(c, k_moments_int<true>, fixed_grid, kBlock, 0, 0, c->nd.lil, c->ctl, c->nd, c->S(),
-                       c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{c->prm.theta, c->inst_R});
+                       c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
             AG2_LAUNCH(c, k_mlev_next, 1, 32, 0, c->ctl, h, 1);
             return AG2_OK;
         });
@@ -2054,7 +2054,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             const int32_t cnt = c->lvl_cnt_h[L];
             if (!cnt) continue;
             AG2_LAUNCH(c, k_moments_int<false>, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.lil + c->lvl_start_h[L],
-                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{c->prm.theta, c->inst_R});
+                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
         }
     }
     phase_mark(c, "build: moments");

@@ -190,6 +190,15 @@ int ag2_node_count(ag2_ctx *ctx, int64_t *nodes, int64_t *internal, int32_t *max
 int ag2_topology(ag2_ctx *ctx, int32_t *depth, int32_t *is_leaf, int32_t *particle, int64_t *cp_count,
                  uint64_t *cp_hash, double *mass, double *com3, double *gas_mass, double *mvel3,
                  double *center3, double *radius);
+/* The FP32 walk's node records in ag2_topology's numbering, 16 floats per node
+ * (zeros for an empty node): centre of mass as hi floats and mass * ls^2; the
+ * lo floats of the centre of mass and (radius * ls / theta)^2 (-1 for a leaf);
+ * first child, leaf particle slot, child mask and 0 as int32 bits; gas velocity
+ * and gasMass * ls^2.  ls = 2^k with k = 1022 - (the biased exponent of the
+ * instance's root half-width), so scaled lengths are below 1.  A diagnostic of
+ * the records the reference's calculateGravityForce reads as doubles
+ * (Node.cpp:285-305); the reference has no such view. */
+int ag2_walk_records(ag2_ctx *ctx, float *out16);
 /* For each particle (original upload order): the preorder index, in the
  * ag2_topology numbering, of the node the reference's Particle::node points at
  * after the build (its leaf; see Node.cpp:412-413, 621-625), or -1 for null. */
