@@ -63,27 +63,64 @@ namespace {
 
 constexpr int kBlock = 256;
 
+// Caller's arrays (upload order) into the state.  With `prev`, slot t takes
+// upload index prev[t], the particle it held before: the same particle set
+// uploaded again keeps the last build's spatial order, so the next build moves
+// neighbours together instead of starting from the caller's order.  (A gather:
+// scattered reads of the caller's records, whole-sector writes of the state.)
 __global__ void k_unpack(int n, const double *pos, const double *vel, const double *mass, const double *U,
-                         const uint8_t *type, Particles s, Ctx::Ctl *ctl)
+                         const uint8_t *type, const int32_t *prev, Particles s, Ctx::Ctl *ctl)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = prev ? prev[t] : t;
+    double x = pos[3 * (size_t)i], y = pos[3 * (size_t)i + 1], z = pos[3 * (size_t)i + 2];
     if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicExch(&ctl->err_code, (int)AG2_E_NAN);
-    s.px[i] = x;
-    s.py[i] = y;
-    s.pz[i] = z;
-    s.vx[i] = vel ? vel[3 * i] : 0.0;
-    s.vy[i] = vel ? vel[3 * i + 1] : 0.0;
-    s.vz[i] = vel ? vel[3 * i + 2] : 0.0;
-    s.ax[i] = s.ay[i] = s.az[i] = 0.0;
-    s.m[i] = mass[i];
-    s.U[i] = U ? U[i] : 0.0;
-    s.dUdt[i] = 0.0;
-    s.h[i] = s.rho[i] = s.P[i] = s.T[i] = s.vdens[i] = 0.0;
-    s.tstep[i] = s.tnext[i] = 0.0;
-    s.type[i] = type[i];
-    s.id[i] = i;
+    s.px[t] = x;
+    s.py[t] = y;
+    s.pz[t] = z;
+    s.vx[t] = vel ? vel[3 * (size_t)i] : 0.0;
+    s.vy[t] = vel ? vel[3 * (size_t)i + 1] : 0.0;
+    s.vz[t] = vel ? vel[3 * (size_t)i + 2] : 0.0;
+    s.ax[t] = s.ay[t] = s.az[t] = 0.0;
+    s.m[t] = mass[i];
+    s.U[t] = U ? U[i] : 0.0;
+    s.dUdt[t] = 0.0;
+    s.h[t] = s.rho[t] = s.P[t] = s.T[t] = s.vdens[t] = 0.0;
+    s.tstep[t] = s.tnext[t] = 0.0;
+    s.type[t] = type[i];
+    s.id[t] = i;
+}
+
+// The state back into upload order (slot i holds upload index i): a scatter by
+// each slot's upload index, for an instance layout the current permutation
+// does not keep apart.
+__global__ void k_to_upload_order(int n, Particles s, Particles d)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = s.id[t];
+    d.px[i] = s.px[t];
+    d.py[i] = s.py[t];
+    d.pz[i] = s.pz[t];
+    d.vx[i] = s.vx[t];
+    d.vy[i] = s.vy[t];
+    d.vz[i] = s.vz[t];
+    d.ax[i] = s.ax[t];
+    d.ay[i] = s.ay[t];
+    d.az[i] = s.az[t];
+    d.m[i] = s.m[t];
+    d.U[i] = s.U[t];
+    d.dUdt[i] = s.dUdt[t];
+    d.h[i] = s.h[t];
+    d.rho[i] = s.rho[t];
+    d.P[i] = s.P[t];
+    d.T[i] = s.T[t];
+    d.vdens[i] = s.vdens[t];
+    d.tstep[i] = s.tstep[t];
+    d.tnext[i] = s.tnext[t];
+    d.type[i] = s.type[t];
+    d.id[i] = i;
 }
 
 __device__ double *field1(Particles &s, int f)
@@ -202,8 +239,12 @@ int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const 
                   const uint8_t *type)
 {
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    // the same count again: keep the slots of the last build (each slot reads
+    // and rewrites only its own id, so the current buffer may be the target)
+    const int32_t *prev = (c->n == n && !c->upload_order) ? c->S().id : nullptr;
     c->cur = 0;
-    AG2_LAUNCH(c, k_unpack, grid_for(n, kBlock), kBlock, 0, (int)n, pos, vel, mass, U, type, c->S(), c->ctl);
+    AG2_LAUNCH(c, k_unpack, grid_for(n, kBlock), kBlock, 0, (int)n, pos, vel, mass, U, type, prev, c->S(), c->ctl);
+    if (!prev) c->upload_order = true;
     c->n = n;
     c->have_tree = false;
     c->gas_stats_dirty = true;
@@ -222,6 +263,13 @@ int ensure_instance_tables(Ctx *c)
 {
     if (!c->inst_dirty) return AG2_OK;
     const int K = c->n_inst;
+    if (!c->upload_order && K > 1 && c->inst_first_h != c->perm_first) {
+        // the slots hold a permutation made under another layout: instance k
+        // must own slots [first[k], first[k+1]) again
+        AG2_LAUNCH(c, k_to_upload_order, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), c->st[c->cur ^ 1]);
+        c->cur ^= 1;
+        c->upload_order = true;
+    }
     if ((size_t)K > c->inst_cap) {
         bool ok = realloc_dev(c->inst_first, K + 1) && realloc_dev(c->inst_R, K) && realloc_dev(c->inst_massInH, K) &&
                   realloc_dev(c->gas_off, K) && realloc_dev(c->gas_uni, K) && realloc_dev(c->gas_cnt, K) &&

@@ -2018,6 +2018,8 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     Particles &dst = c->st[c->cur ^ 1];
     AG2_LAUNCH(c, k_reorder, grid_for(n, kBlock), kBlock, 0, n, c->perm_final, src, dst);
     c->cur ^= 1;
+    c->upload_order = false;  // tree order, within each instance's slot range
+    c->perm_first = c->inst_first_h;
     AG2_LAUNCH(c, k_refnode, grid_for(n, kBlock), kBlock, 0, n, c->nd, c->pnode, c->S().id, c->refnode);
     phase_mark(c, "build: reorder");
 

@@ -229,6 +229,11 @@ struct Ctx {
     bool inst_dirty = true;         // instance tables need uploading
     bool inst_explicit = false;     // layout from ag2_set_instances (keeps its massInH)
     std::vector<int64_t> inst_tab_first;  // layout the device instance tables and walk groups describe
+    // Slot order of the state: upload order (slot i holds upload index i), or
+    // the permutation of the last build, which keeps every instance of layout
+    // perm_first inside its own slot range
+    bool upload_order = true;
+    std::vector<int64_t> perm_first;
     // gasMass tables: instance k's sequential partial sums start at gas_off[k]
     int32_t *gas_off = nullptr;     // device
     uint8_t *gas_uni = nullptr;     // device: instance's gas particles share one mass
