@@ -28,7 +28,8 @@ VECTOR_FIELDS = {"pos", "vel", "acc"}
 # every exported symbol of include/ag2.h
 EXPORTS = [
     "ag2_default_params", "ag2_create", "ag2_destroy", "ag2_set_params", "ag2_get_params", "ag2_set_stream",
-    "ag2_last_error_string", "ag2_upload", "ag2_upload_device", "ag2_set_field", "ag2_download", "ag2_count",
+    "ag2_last_error_string", "ag2_upload", "ag2_upload_device", "ag2_set_field", "ag2_download",
+    "ag2_download_fields", "ag2_count",
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_walk_records", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
@@ -82,6 +83,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_upload_device.argtypes = [P, ctypes.c_size_t, P, P, P, P, P]
     L.ag2_set_field.argtypes = [P, I, P, I]
     L.ag2_download.argtypes = [P, I, P, I]
+    L.ag2_download_fields.argtypes = [P, I, P, P]
     L.ag2_count.argtypes = [P]
     L.ag2_count.restype = ctypes.c_size_t
     for f in ("ag2_build_tree", "ag2_sph_density", "ag2_forces"):
@@ -203,6 +205,19 @@ class Context:
             raise ValueError("out must be a C-contiguous float64 array of shape %s" % (shape,))
         self._check(self.L.ag2_download(self.h, f, _ptr(out), 0))
         return out
+
+    def download_fields(self, outs: dict) -> dict:
+        """Several fields into preallocated host arrays in one call ({field: out})."""
+        names = list(outs)
+        for f in names:
+            shape = (self.n, 3) if f in VECTOR_FIELDS else (self.n,)
+            o = outs[f]
+            if o.shape != shape or o.dtype != np.float64 or not o.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float64 array of shape %s" % (shape,))
+        codes = (ctypes.c_int * len(names))(*[FIELDS[f] for f in names])
+        ptrs = (ctypes.c_void_p * len(names))(*[outs[f].ctypes.data for f in names])
+        self._check(self.L.ag2_download_fields(self.h, len(names), codes, ptrs))
+        return outs
 
     def download_device(self, field: str, dst_ptr: int):
         self._check(self.L.ag2_download(self.h, FIELDS[field], ctypes.c_void_p(dst_ptr), 1))

@@ -454,6 +454,11 @@ int ag2_destroy(ag2_ctx *c)
     for (auto &x : c->step_exec)
         if (x) cudaGraphExecDestroy(x);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    for (int b = 0; b < 2; b++) {
+        if (c->dl_gathered[b]) cudaEventDestroy(c->dl_gathered[b]);
+        if (c->dl_copied[b]) cudaEventDestroy(c->dl_copied[b]);
+    }
     if (c->blk_key) cudaFree(c->blk_key);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -557,6 +562,36 @@ int ag2_download(ag2_ctx *c, int f, double *dst, int dst_is_device)
         AG2_CUDA(c, cudaMemcpyAsync(dst, c->staging, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         AG2_CUDA(c, cudaStreamSynchronize(c->stream));
     }
+    return AG2_OK;
+}
+
+int ag2_download_fields(ag2_ctx *c, int nf, const int *fields, double *const *dst)
+{
+    if (!c || nf < 0 || (nf && (!fields || !dst))) return AG2_E_INVALID;
+    for (int k = 0; k < nf; k++)
+        if (!dst[k] || fields[k] < AG2_POS || fields[k] > AG2_TNEXT) return set_err(c, AG2_E_INVALID, "bad field");
+    if (!c->n || !nf) return AG2_OK;
+    if (!c->copy_stream) {
+        AG2_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; b++) {
+            AG2_CUDA(c, cudaEventCreateWithFlags(&c->dl_gathered[b], cudaEventDisableTiming));
+            AG2_CUDA(c, cudaEventCreateWithFlags(&c->dl_copied[b], cudaEventDisableTiming));
+        }
+    }
+    // field k: gathered into upload order in staging half k % 2 on the context's
+    // stream, copied out on the copy stream while the next field is gathered
+    double *half[2] = {c->staging, c->staging + 3 * c->n};
+    for (int k = 0; k < nf; k++) {
+        const int b = k & 1;
+        const size_t cnt = (fields[k] <= AG2_ACC ? 3 : 1) * c->n;
+        if (k >= 2) AG2_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_copied[b], 0));  // the half is free again
+        AG2_LAUNCH(c, k_gather_out, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), fields[k], half[b]);
+        AG2_CUDA(c, cudaEventRecord(c->dl_gathered[b], c->stream));
+        AG2_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->dl_gathered[b], 0));
+        AG2_CUDA(c, cudaMemcpyAsync(dst[k], half[b], cnt * sizeof(double), cudaMemcpyDeviceToHost, c->copy_stream));
+        AG2_CUDA(c, cudaEventRecord(c->dl_copied[b], c->copy_stream));
+    }
+    AG2_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     return AG2_OK;
 }
 

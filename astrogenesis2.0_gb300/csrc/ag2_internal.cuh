@@ -234,6 +234,10 @@ struct Ctx {
     // perm_first inside its own slot range
     bool upload_order = true;
     std::vector<int64_t> perm_first;
+    // ag2_download_fields: device-to-host copies on their own stream, behind
+    // the gathers of the context's stream (two staging halves)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t dl_gathered[2] = {}, dl_copied[2] = {};
     // gasMass tables: instance k's sequential partial sums start at gas_off[k]
     int32_t *gas_off = nullptr;     // device
     uint8_t *gas_uni = nullptr;     // device: instance's gas particles share one mass

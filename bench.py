@@ -522,10 +522,7 @@ def our_arm(args, wl, d):
                 ctx.set_instances(d["first"])
             ctx.set_field("acc", hacc)
             ctx.step(dt)
-            ctx.download("pos", out=hpos)
-            ctx.download("vel", out=hvel)
-            ctx.download("acc", out=hacc)
-            ctx.download("U", out=hU)
+            ctx.download_fields({"pos": hpos, "vel": hvel, "acc": hacc, "U": hU})
         te = time.perf_counter() - t0
         te = max_over_ranks(te, D)
         e2e = {"value": n * args.e2e_steps * D.world / te, "unit": UNIT,

@@ -114,6 +114,10 @@ int ag2_upload_device(ag2_ctx *ctx, size_t n, const double *pos, const double *v
 int ag2_set_field(ag2_ctx *ctx, int field, const double *src, int src_is_device);
 /* Read one field back in the original particle order (host or device buffer). */
 int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
+/* Several fields to host buffers in one call, as ag2_download each: the
+ * gather of one field into upload order runs while the previous one crosses
+ * to the host, and the call returns once every copy has landed. */
+int ag2_download_fields(ag2_ctx *ctx, int nfields, const int *fields, double *const *dst);
 size_t ag2_count(const ag2_ctx *ctx);
 
 /* Independent simulations in one context (the batched ensemble and the

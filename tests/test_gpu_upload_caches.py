@@ -67,3 +67,37 @@ def test_instance_layout_change_with_same_count():
     d2["mih"] = np.array([parts[0]["massInH"], parts[2]["massInH"]])
     _same(_step_once(c, d2), _fresh(d2, **kw))
     _same(_step_once(c, d), _fresh(d, **kw))
+
+
+def test_reupload_keeps_slots_and_download_order():
+    """A second upload of the same count takes the last build's slot order;
+    downloads still return the caller's order, bit for bit."""
+    import ag2
+
+    d = ics.small_gas_cloud(5000, seed=31)
+    c = ag2.Context(5000, e0=0.02, theta=0.5, massInH=d["massInH"])
+    _step_once(c, d)
+    rng = np.random.default_rng(2)
+    pos2 = d["pos"] + rng.normal(0, 1e-3, d["pos"].shape)
+    vel2 = rng.normal(0, 1, d["vel"].shape)
+    c.upload(pos2, d["mass"], d["type"], vel=vel2, U=d["U"] * 2)
+    np.testing.assert_array_equal(c.download("pos"), pos2)
+    np.testing.assert_array_equal(c.download("vel"), vel2)
+    np.testing.assert_array_equal(c.download("U"), d["U"] * 2)
+    np.testing.assert_array_equal(c.download("mass"), d["mass"])
+
+
+def test_download_fields_equals_download():
+    import ag2
+
+    d = ics.small_gas_cloud(4000, seed=32)
+    c = ag2.Context(4000, e0=0.02, theta=0.5, massInH=d["massInH"])
+    _step_once(c, d)
+    c.step(1e-3)
+    names = ["pos", "vel", "acc", "U", "h", "rho", "dUdt"]  # more fields than staging halves
+    outs = {f: np.empty((4000, 3) if f in ("pos", "vel", "acc") else 4000) for f in names}
+    c.download_fields(outs)
+    for f in names:
+        np.testing.assert_array_equal(outs[f], c.download(f), err_msg=f)
+    with pytest.raises(ValueError):
+        c.download_fields({"pos": np.empty(4000)})
