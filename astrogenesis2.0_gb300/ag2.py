@@ -29,7 +29,7 @@ VECTOR_FIELDS = {"pos", "vel", "acc"}
 EXPORTS = [
     "ag2_default_params", "ag2_create", "ag2_destroy", "ag2_set_params", "ag2_get_params", "ag2_set_stream",
     "ag2_last_error_string", "ag2_upload", "ag2_upload_device", "ag2_set_field", "ag2_download",
-    "ag2_download_fields", "ag2_count",
+    "ag2_download_fields", "ag2_step_host", "ag2_count",
     "ag2_build_tree", "ag2_visual_density", "ag2_sph_density", "ag2_forces", "ag2_kick", "ag2_drift",
     "ag2_kick_drift", "ag2_ueuler", "ag2_scale_positions", "ag2_step", "ag2_root_radius", "ag2_node_count",
     "ag2_topology", "ag2_walk_records", "ag2_particle_node", "ag2_interactions", "ag2_launch_count", "ag2_direct_sum",
@@ -92,6 +92,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
               "ag2_scale_positions"):
         getattr(L, f).argtypes = [P, D]
     L.ag2_step.argtypes = [P, D, D, I, D]
+    L.ag2_step_host.argtypes = [P, ctypes.c_size_t, D, D, I, D, P]
     L.ag2_root_radius.argtypes = [P, dp]
     L.ag2_node_count.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                  ctypes.POINTER(ctypes.c_int32)]
@@ -129,6 +130,12 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _HostIO(ctypes.Structure):
+    """ag2_host_io (include/ag2.h)."""
+    _fields_ = [(k, ctypes.c_void_p) for k in
+                ("pos", "vel", "mass", "U", "acc", "type", "pos_out", "vel_out", "acc_out", "U_out")]
 
 
 class Context:
@@ -260,6 +267,34 @@ class Context:
 
     def step(self, dt, hubble_factor=1.0, visual_density=False, visual_radius=0.0):
         self._check(self.L.ag2_step(self.h, dt, hubble_factor, 1 if visual_density else 0, visual_radius))
+
+    def step_host(self, dt, pos, mass, type_, vel=None, U=None, acc=None, out=None, hubble_factor=1.0,
+                  visual_density=False, visual_radius=0.0):
+        """One step with host arrays in and out (ag2_step_host): upload, step,
+        and pos/vel/acc/U read back into out = {field: array} (arrays may be the
+        inputs).  Inputs must be C-contiguous float64 (uint8 type)."""
+        n = len(mass)
+        arrs = {"pos": pos, "vel": vel, "mass": mass, "U": U, "acc": acc}
+        def bad(k, a):
+            size = n * (3 if k in VECTOR_FIELDS else 1)
+            return a.dtype != np.float64 or not a.flags.c_contiguous or a.size != size
+
+        for k, a in arrs.items():
+            if a is not None and bad(k, a):
+                raise ValueError(k + " must be a C-contiguous float64 array of n" + (" x 3" if k in VECTOR_FIELDS else ""))
+        if type_.dtype != np.uint8 or not type_.flags.c_contiguous or type_.size != n:
+            raise ValueError("type must be a C-contiguous uint8 array of n")
+        out = out or {}
+        for k, a in out.items():
+            if k not in ("pos", "vel", "acc", "U") or bad(k, a):
+                raise ValueError("bad output array for " + k)
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        io = _HostIO(ptr(pos), ptr(vel), ptr(mass), ptr(U), ptr(acc), ptr(type_), ptr(out.get("pos")),
+                     ptr(out.get("vel")), ptr(out.get("acc")), ptr(out.get("U")))
+        self._check(self.L.ag2_step_host(self.h, n, dt, hubble_factor, 1 if visual_density else 0, visual_radius,
+                                         ctypes.byref(io)))
+        self.n = n
+        return out
 
     # -- introspection --------------------------------------------------------
     def root_radius(self) -> float:

@@ -565,34 +565,50 @@ int ag2_download(ag2_ctx *c, int f, double *dst, int dst_is_device)
     return AG2_OK;
 }
 
+// Read-back pipeline of ag2_download_fields and ag2_step_host: field k is
+// gathered into upload order in staging half k % 2 on the context's stream and
+// copied to the host on the copy stream, so the next gather (or other device
+// work) overlaps the copy; dl_end waits for every copy.
+static int dl_begin(Ctx *c)
+{
+    if (c->copy_stream) return AG2_OK;
+    AG2_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+        AG2_CUDA(c, cudaEventCreateWithFlags(&c->dl_gathered[b], cudaEventDisableTiming));
+        AG2_CUDA(c, cudaEventCreateWithFlags(&c->dl_copied[b], cudaEventDisableTiming));
+    }
+    return AG2_OK;
+}
+static int dl_field(Ctx *c, int k, int field, double *dst)
+{
+    const int b = k & 1;
+    double *half = c->staging + (size_t)b * 3 * c->n;
+    const size_t cnt = (field <= AG2_ACC ? 3 : 1) * c->n;
+    if (k >= 2) AG2_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_copied[b], 0));  // the half is free again
+    AG2_LAUNCH(c, k_gather_out, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), field, half);
+    AG2_CUDA(c, cudaEventRecord(c->dl_gathered[b], c->stream));
+    AG2_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->dl_gathered[b], 0));
+    AG2_CUDA(c, cudaMemcpyAsync(dst, half, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->copy_stream));
+    AG2_CUDA(c, cudaEventRecord(c->dl_copied[b], c->copy_stream));
+    return AG2_OK;
+}
+static int dl_end(Ctx *c)
+{
+    AG2_CUDA(c, cudaStreamSynchronize(c->copy_stream));
+    return AG2_OK;
+}
+
 int ag2_download_fields(ag2_ctx *c, int nf, const int *fields, double *const *dst)
 {
     if (!c || nf < 0 || (nf && (!fields || !dst))) return AG2_E_INVALID;
     for (int k = 0; k < nf; k++)
         if (!dst[k] || fields[k] < AG2_POS || fields[k] > AG2_TNEXT) return set_err(c, AG2_E_INVALID, "bad field");
     if (!c->n || !nf) return AG2_OK;
-    if (!c->copy_stream) {
-        AG2_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        for (int b = 0; b < 2; b++) {
-            AG2_CUDA(c, cudaEventCreateWithFlags(&c->dl_gathered[b], cudaEventDisableTiming));
-            AG2_CUDA(c, cudaEventCreateWithFlags(&c->dl_copied[b], cudaEventDisableTiming));
-        }
-    }
-    // field k: gathered into upload order in staging half k % 2 on the context's
-    // stream, copied out on the copy stream while the next field is gathered
-    double *half[2] = {c->staging, c->staging + 3 * c->n};
-    for (int k = 0; k < nf; k++) {
-        const int b = k & 1;
-        const size_t cnt = (fields[k] <= AG2_ACC ? 3 : 1) * c->n;
-        if (k >= 2) AG2_CUDA(c, cudaStreamWaitEvent(c->stream, c->dl_copied[b], 0));  // the half is free again
-        AG2_LAUNCH(c, k_gather_out, grid_for(c->n, kBlock), kBlock, 0, (int)c->n, c->S(), fields[k], half[b]);
-        AG2_CUDA(c, cudaEventRecord(c->dl_gathered[b], c->stream));
-        AG2_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->dl_gathered[b], 0));
-        AG2_CUDA(c, cudaMemcpyAsync(dst[k], half[b], cnt * sizeof(double), cudaMemcpyDeviceToHost, c->copy_stream));
-        AG2_CUDA(c, cudaEventRecord(c->dl_copied[b], c->copy_stream));
-    }
-    AG2_CUDA(c, cudaStreamSynchronize(c->copy_stream));
-    return AG2_OK;
+    int rc;
+    if ((rc = dl_begin(c))) return rc;
+    for (int k = 0; k < nf; k++)
+        if ((rc = dl_field(c, k, fields[k], dst[k]))) return rc;
+    return dl_end(c);
 }
 
 size_t ag2_count(const ag2_ctx *c) { return c ? c->n : 0; }
@@ -826,6 +842,48 @@ int ag2_step(ag2_ctx *c, double dt, double hubble_factor, int with_visual, doubl
     if ((rc = run_close_step(c, dt, hubble_factor))) return rc;
     phase_mark(c, "second kick");
     rc = check_walk(c);
+    phase_finish(c);
+    return rc;
+}
+
+int ag2_step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int with_visual, double Rv,
+                  const ag2_host_io *io)
+{
+    if (!c || !io) return AG2_E_INVALID;
+    if (n == 0) return set_err(c, AG2_E_INVALID, "no particles");
+    int rc;
+    if ((rc = ag2_upload(c, n, io->pos, io->vel, io->mass, io->U, io->type))) return rc;
+    if (io->acc && (rc = ag2_set_field(c, AG2_ACC, io->acc, 0))) return rc;
+    if ((rc = dl_begin(c))) return rc;
+    phase_reset(c);
+    if ((rc = run_kick_drift(c, dt))) return rc;
+    phase_mark(c, "first kick");
+    const bool t = c->timing;
+    c->timing = false;
+    rc = build_tree(c);
+    c->timing = t;
+    if (rc) return rc;
+    phase_mark(c, "build tree");
+    if (with_visual && (rc = run_visual_density(c, Rv))) return rc;
+    phase_mark(c, "Visual Density");
+    if ((rc = run_sph_density(c))) return rc;
+    phase_mark(c, "SPH density and update");
+    // positions are final since the drift: their read-back crosses to the host
+    // during the walk, which reads nothing back until it ends (the build reads
+    // its control block every level, and those small copies would queue behind
+    // this one on the device-to-host copy engine)
+    int k = 0;
+    if (io->pos_out && (rc = dl_field(c, k++, AG2_POS, io->pos_out))) return rc;
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    if ((rc = run_forces(c))) return rc;
+    phase_mark(c, "Force Calculation");
+    if ((rc = run_close_step(c, dt, hubble_factor))) return rc;
+    phase_mark(c, "second kick");
+    if ((rc = check_walk(c))) return rc;
+    if (io->vel_out && (rc = dl_field(c, k++, AG2_VEL, io->vel_out))) return rc;
+    if (io->acc_out && (rc = dl_field(c, k++, AG2_ACC, io->acc_out))) return rc;
+    if (io->U_out && (rc = dl_field(c, k++, AG2_U, io->U_out))) return rc;
+    rc = dl_end(c);
     phase_finish(c);
     return rc;
 }

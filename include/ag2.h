@@ -114,6 +114,20 @@ int ag2_upload_device(ag2_ctx *ctx, size_t n, const double *pos, const double *v
 int ag2_set_field(ag2_ctx *ctx, int field, const double *src, int src_is_device);
 /* Read one field back in the original particle order (host or device buffer). */
 int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
+/* One step of the reference's loop with the caller's particle arrays as its
+ * source and destination (upload order, host memory): ag2_upload(pos, vel,
+ * mass, U, type) and ag2_set_field(ACC, acc), ag2_step(dt, hubble_factor,
+ * with_visual_density, visualDensityRadius), then pos/vel/acc/U read back into
+ * the *_out arrays (a NULL input is not uploaded, a NULL output not read).
+ * The positions' read-back overlaps the walk (they are final after the
+ * drift).  The out arrays may be the input arrays. */
+typedef struct ag2_host_io {
+    const double *pos, *vel, *mass, *U, *acc;
+    const uint8_t *type;
+    double *pos_out, *vel_out, *acc_out, *U_out;
+} ag2_host_io;
+int ag2_step_host(ag2_ctx *ctx, size_t n, double dt, double hubble_factor, int with_visual_density,
+                  double visualDensityRadius, const ag2_host_io *io);
 /* Several fields to host buffers in one call, as ag2_download each: the
  * gather of one field into upload order runs while the previous one crosses
  * to the host, and the call returns once every copy has landed. */

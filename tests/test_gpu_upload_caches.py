@@ -101,3 +101,26 @@ def test_download_fields_equals_download():
         np.testing.assert_array_equal(outs[f], c.download(f), err_msg=f)
     with pytest.raises(ValueError):
         c.download_fields({"pos": np.empty(4000)})
+
+
+def test_step_host_equals_separate_calls():
+    """ag2_step_host gives the same state as upload + set_field + step +
+    downloads, bit for bit, with the outputs written over the inputs."""
+    import ag2
+
+    d = ics.small_gas_cloud(6000, seed=33)
+    kw = dict(e0=0.02, theta=0.5, massInH=d["massInH"])
+    a, b = ag2.Context(6000, **kw), ag2.Context(6000, **kw)
+    pos, vel, U = d["pos"].copy(), d["vel"].copy(), d["U"].copy()
+    acc = np.zeros_like(pos)
+    mass, typ = np.ascontiguousarray(d["mass"]), np.ascontiguousarray(d["type"], np.uint8)
+    ref = {"pos": pos.copy(), "vel": vel.copy(), "acc": acc.copy(), "U": U.copy()}
+    for _ in range(3):
+        a.step_host(1e-3, pos, mass, typ, vel=vel, U=U, acc=acc, out={"pos": pos, "vel": vel, "acc": acc, "U": U})
+        b.upload(ref["pos"], mass, typ, vel=ref["vel"], U=ref["U"])
+        b.set_field("acc", ref["acc"])
+        b.step(1e-3)
+        ref = {f: b.download(f) for f in ("pos", "vel", "acc", "U")}
+        for f, got in (("pos", pos), ("vel", vel), ("acc", acc), ("U", U)):
+            np.testing.assert_array_equal(got, ref[f], err_msg=f)
+    assert np.abs(acc).max() > 0
