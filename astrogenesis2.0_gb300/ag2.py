@@ -135,7 +135,8 @@ def _ptr(a):
 class _HostIO(ctypes.Structure):
     """ag2_host_io (include/ag2.h)."""
     _fields_ = [(k, ctypes.c_void_p) for k in
-                ("pos", "vel", "mass", "U", "acc", "type", "pos_out", "vel_out", "acc_out", "U_out")]
+                ("pos", "vel", "mass", "U", "acc", "type", "pos_out", "vel_out", "acc_out", "U_out")] + \
+               [("n_inst", ctypes.c_int32), ("first", ctypes.c_void_p), ("massInH", ctypes.c_void_p)]
 
 
 class Context:
@@ -269,10 +270,12 @@ class Context:
         self._check(self.L.ag2_step(self.h, dt, hubble_factor, 1 if visual_density else 0, visual_radius))
 
     def step_host(self, dt, pos, mass, type_, vel=None, U=None, acc=None, out=None, hubble_factor=1.0,
-                  visual_density=False, visual_radius=0.0):
+                  visual_density=False, visual_radius=0.0, first=None, massInH=None):
         """One step with host arrays in and out (ag2_step_host): upload, step,
         and pos/vel/acc/U read back into out = {field: array} (arrays may be the
-        inputs).  Inputs must be C-contiguous float64 (uint8 type)."""
+        inputs).  Inputs must be C-contiguous float64 (uint8 type).  `first`
+        (and `massInH`) split the particles into simulations, as
+        set_instances."""
         n = len(mass)
         arrs = {"pos": pos, "vel": vel, "mass": mass, "U": U, "acc": acc}
         def bad(k, a):
@@ -291,6 +294,12 @@ class Context:
         ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
         io = _HostIO(ptr(pos), ptr(vel), ptr(mass), ptr(U), ptr(acc), ptr(type_), ptr(out.get("pos")),
                      ptr(out.get("vel")), ptr(out.get("acc")), ptr(out.get("U")))
+        if first is not None:
+            first = np.ascontiguousarray(first, np.int64)
+            io.n_inst, io.first = len(first) - 1, first.ctypes.data
+            if massInH is not None:
+                massInH = np.ascontiguousarray(massInH, np.float64)
+                io.massInH = massInH.ctypes.data
         self._check(self.L.ag2_step_host(self.h, n, dt, hubble_factor, 1 if visual_density else 0, visual_radius,
                                          ctypes.byref(io)))
         self.n = n

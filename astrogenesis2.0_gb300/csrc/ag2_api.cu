@@ -853,6 +853,7 @@ int ag2_step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int wit
     if (n == 0) return set_err(c, AG2_E_INVALID, "no particles");
     int rc;
     if ((rc = ag2_upload(c, n, io->pos, io->vel, io->mass, io->U, io->type))) return rc;
+    if (io->first && (rc = ag2_set_instances(c, io->n_inst, io->first, io->massInH))) return rc;
     if (io->acc && (rc = ag2_set_field(c, AG2_ACC, io->acc, 0))) return rc;
     if ((rc = dl_begin(c))) return rc;
     phase_reset(c);

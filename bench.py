@@ -517,15 +517,8 @@ def our_arm(args, wl, d):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         outs = {"pos": hpos, "vel": hvel, "acc": hacc, "U": hU}
-        for _ in range(args.e2e_steps):
-            if "first" in d:  # the instance layout goes with the upload: separate calls
-                ctx.upload(hpos, hmass, htype, vel=hvel, U=hU)
-                ctx.set_instances(d["first"])
-                ctx.set_field("acc", hacc)
-                ctx.step(dt)
-                ctx.download_fields(outs)
-            else:  # one call: upload, step, read-back (positions overlapping the step)
-                ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs)
+        for _ in range(args.e2e_steps):  # one call: upload, step, read-back (positions during the walk)
+            ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs, first=d.get("first"))
         te = time.perf_counter() - t0
         te = max_over_ranks(te, D)
         e2e = {"value": n * args.e2e_steps * D.world / te, "unit": UNIT,

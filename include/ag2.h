@@ -120,11 +120,16 @@ int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
  * with_visual_density, visualDensityRadius), then pos/vel/acc/U read back into
  * the *_out arrays (a NULL input is not uploaded, a NULL output not read).
  * The positions' read-back overlaps the walk (they are final after the
- * drift).  The out arrays may be the input arrays. */
+ * drift).  The out arrays may be the input arrays.  With first != NULL the
+ * particles are n_inst simulations, as ag2_set_instances(n_inst, first,
+ * massInH) after the upload. */
 typedef struct ag2_host_io {
     const double *pos, *vel, *mass, *U, *acc;
     const uint8_t *type;
     double *pos_out, *vel_out, *acc_out, *U_out;
+    int32_t n_inst;
+    const int64_t *first;
+    const double *massInH;
 } ag2_host_io;
 int ag2_step_host(ag2_ctx *ctx, size_t n, double dt, double hubble_factor, int with_visual_density,
                   double visualDensityRadius, const ag2_host_io *io);

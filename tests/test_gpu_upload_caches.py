@@ -124,3 +124,26 @@ def test_step_host_equals_separate_calls():
         for f, got in (("pos", pos), ("vel", vel), ("acc", acc), ("U", U)):
             np.testing.assert_array_equal(got, ref[f], err_msg=f)
     assert np.abs(acc).max() > 0
+
+
+def test_step_host_with_instances():
+    import ag2
+
+    parts = [ics.small_gas_cloud(n, seed=40 + k) for k, n in enumerate((900, 2100, 1500))]
+    d = {k: np.concatenate([p[k] for p in parts]) for k in ("pos", "vel", "mass", "type", "U")}
+    first = np.array([0, 900, 3000, 4500])
+    mih = np.array([p["massInH"] for p in parts])
+    a, b = ag2.Context(4500, e0=0.02, theta=0.5), ag2.Context(4500, e0=0.02, theta=0.5)
+    typ = np.ascontiguousarray(d["type"], np.uint8)
+    pos, vel, U, acc = d["pos"].copy(), d["vel"].copy(), d["U"].copy(), np.zeros_like(d["pos"])
+    ref = {"pos": pos.copy(), "vel": vel.copy(), "acc": acc.copy(), "U": U.copy()}
+    for _ in range(2):
+        a.step_host(1e-3, pos, d["mass"], typ, vel=vel, U=U, acc=acc,
+                    out={"pos": pos, "vel": vel, "acc": acc, "U": U}, first=first, massInH=mih)
+        b.upload(ref["pos"], d["mass"], typ, vel=ref["vel"], U=ref["U"])
+        b.set_instances(first, mih)
+        b.set_field("acc", ref["acc"])
+        b.step(1e-3)
+        ref = {f: b.download(f) for f in ("pos", "vel", "acc", "U")}
+        for f, got in (("pos", pos), ("vel", vel), ("acc", acc), ("U", U)):
+            np.testing.assert_array_equal(got, ref[f], err_msg=f)
