@@ -450,6 +450,9 @@ int ag2_destroy(ag2_ctx *c)
                   c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    if (c->ctl_snap) cudaFreeHost(c->ctl_snap);
+    for (auto &e : c->snap_ev)
+        if (e) cudaEventDestroy(e);
     if (c->inst_R_pin) cudaFreeHost(c->inst_R_pin);
     for (auto &x : c->step_exec)
         if (x) cudaGraphExecDestroy(x);

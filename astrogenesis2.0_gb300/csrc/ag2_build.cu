@@ -612,6 +612,9 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
 __global__ void k_level_next(Ctx::Ctl *ctl, int inc, int max_depth, cudaGraphConditionalHandle h, int use_h)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    // a level queued past the last one (the launched loop runs one level ahead
+    // of the host) had no split nodes: it leaves the control block as it was
+    if (inc && ctl->cur_nnl == 0) return;
     ctl->level += inc;
     ctl->cur_nnl = ctl->next_needs;
     ctl->cur_nap = ctl->next_active;
@@ -1950,23 +1953,54 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
                                     c->stream));
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
         c->root_radius = c->inst_R_h[0];
-        int nnl = c->ctl_host->cur_nnl, nap = c->ctl_host->cur_nap;
-        while (nnl > 0) {
-            if ((rc = ensure_node_capacity(c, (size_t)(c->level_base.back() + 8 * (int64_t)nnl))) != AG2_OK) return rc;
+        // The levels run one ahead of the host: level k + 1 is queued before
+        // the host waits for level k's counts (a snapshot of the control block
+        // copied behind it), so the device does not idle between levels.  The
+        // level queued after the last one finds no split node and changes
+        // nothing.  Kernels take their counts from the control block (grid-
+        // stride launches of a fixed grid, as in a captured build).
+        if (!c->ctl_snap) {
+            AG2_CUDA(c, cudaMallocHost(&c->ctl_snap, 2 * sizeof(Ctx::Ctl)));
+            for (auto &e : c->snap_ev) AG2_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        int64_t known_nodes = c->ctl_host->node_count;  // nodes after the last level read back
+        int64_t nnl = c->ctl_host->cur_nnl;             // split nodes of the level after it
+        int queued = 0, seen = 0;
+        bool more = nnl > 0;
+        while (more) {
+            // pool room for the levels in flight: the one read back next
+            // allocates 8 * nnl children, the one queued now at most 8 times that
+            if ((rc = ensure_node_capacity(c, (size_t)(known_nodes + 72 * nnl + 8))) != AG2_OK) return rc;
             lpair.b[0] = level_bufs(c, 0);
             lpair.b[1] = level_bufs(c, 1);
             lpair.b[0].local_ok = lpair.b[1].local_ok = local_ok;
-            AG2_LAUNCH(c, k_nodes, grid_for((size_t)nnl * 8, kBlock), kBlock, 0, lpair, thresh, (int64_t)c->node_cap,
-                       c->nd, c->ctl, (int)AG2_MAX_DEPTH);
-            AG2_LAUNCH(c, k_scatter, grid_for(nap, kBlock), kBlock, 0, lpair, c->nd, c->ctl);
+            AG2_LAUNCH(c, k_nodes, fixed_grid, kBlock, 0, lpair, thresh, (int64_t)c->node_cap, c->nd, c->ctl,
+                       (int)AG2_MAX_DEPTH);
+            AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
             AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 1, (int)AG2_MAX_DEPTH, none, 0);
-            if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-            const Ctx::Ctl &h = *c->ctl_host;
-            if (h.err_code) return build_error(c, h.err_code);
+            const int slot = queued & 1;
+            AG2_CUDA(c, cudaMemcpyAsync(c->ctl_snap + slot, c->ctl, sizeof(Ctx::Ctl), cudaMemcpyDeviceToHost,
+                                        c->stream));
+            AG2_CUDA(c, cudaEventRecord(c->snap_ev[slot], c->stream));
+            queued++;
+            if (queued - seen < 2) continue;  // keep one level queued ahead
+            AG2_CUDA(c, cudaEventSynchronize(c->snap_ev[seen & 1]));
+            const Ctx::Ctl &h = c->ctl_snap[seen & 1];
+            seen++;
+            if (h.err_code) {
+                if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+                if (c->ctl_host->err_code == AG2_E_NOMEM) local_nomem = true;  // grow the pool and build again
+                return build_error(c, c->ctl_host->err_code);
+            }
             c->level_base.push_back(h.node_count);
+            known_nodes = h.node_count;
             nnl = h.cur_nnl;
-            nap = h.cur_nap;
+            more = nnl > 0;
         }
+        // the host mirror after the loop (the serial subtrees' launch reads its
+        // counts): the level queued past the last one left the block unchanged
+        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        if (c->ctl_host->err_code) return build_error(c, c->ctl_host->err_code);
         AG2_LAUNCH(c, k_mark_loop_nodes, 1, 32, 0, c->ctl);
     }
     phase_mark(c, "build: levels");

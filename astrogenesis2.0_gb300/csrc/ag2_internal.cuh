@@ -280,6 +280,10 @@ struct Ctx {
     };
     Ctl *ctl = nullptr;      // device
     Ctl *ctl_host = nullptr; // pinned mirror
+    // the launched level loop's control-block snapshots (pinned, two levels in
+    // flight) and the events that mark them copied
+    Ctl *ctl_snap = nullptr;
+    cudaEvent_t snap_ev[2] = {};
 
     Nodes nd = {};
 
