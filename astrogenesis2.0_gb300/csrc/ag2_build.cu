@@ -1157,7 +1157,8 @@ __global__ void k_bucket(Ctx::Ctl *ctl, const int2 *__restrict__ lint, int32_t *
 // touch a node's own fields).
 
 constexpr int kLocalCapMax = 1024;  // largest serial subtree (particles) built by one warp
-constexpr int kLocalWarps = 8;      // warps per thread block of k_local (fewer for large subtrees)
+constexpr int kLocalWarps = 7;      // warps per thread block of k_local (fewer for large subtrees)
+constexpr int kLocalBlocks = 4;     // resident blocks per SM the registers are budgeted for
 constexpr int kPoolChunk = 512;     // nodes per warp-private pool chunk
 constexpr int kLeafChunk = 256;     // leaf-list entries per warp-private stretch
 constexpr int kIntChunk = 128;      // internal-node-list entries per warp-private stretch
@@ -1170,7 +1171,7 @@ constexpr int kCoop = 16;           // frontier nodes of more particles are done
 // digit starts 9 x 2 B, parent of a next-frontier node 4 B.
 __host__ __device__ constexpr size_t local_smem_bytes(int cap) { return (size_t)cap * 76; }
 
-__global__ void __launch_bounds__(kLocalWarps * 32) k_local(const int32_t *__restrict__ roots, int cap,
+__global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const int32_t *__restrict__ roots, int cap,
                                                             Nodes nd, Ctx::Ctl *ctl, const int64_t *__restrict__ pkey,
                                                             int64_t keycap, int32_t *perm_final, int32_t *pnode,
                                                             const int32_t *__restrict__ sid, int32_t *leaves,
@@ -1752,7 +1753,9 @@ struct LocalConfig {
 static int local_config(Ctx *c, int thresh, LocalConfig &lc)
 {
     lc.lcap = std::max(8, ((thresh - 1) + 7) & ~7);
-    lc.wpb = (int)std::max<size_t>(1, std::min<size_t>(kLocalWarps, (150u << 10) / local_smem_bytes(lc.lcap)));
+    // kLocalBlocks blocks per SM when the subtrees are small enough (224 KB of
+    // shared memory per SM), else fewer, larger ones
+    lc.wpb = (int)std::max<size_t>(1, std::min<size_t>(kLocalWarps, (56u << 10) / local_smem_bytes(lc.lcap)));
     lc.smem = (size_t)lc.wpb * local_smem_bytes(lc.lcap);
     AG2_CUDA(c, cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lc.smem));
     int per_sm = 0;
