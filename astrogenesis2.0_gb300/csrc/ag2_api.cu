@@ -301,7 +301,7 @@ int ensure_instance_tables(Ctx *c)
         std::vector<std::pair<int32_t, int32_t>> cur(K);  // per instance: (first pair, count) of its current level
         for (int k = 0; k < K; k++) {
             const int64_t b = c->inst_first_h[k], n = c->inst_first_h[k + 1] - b;
-            const int64_t run = n <= 4096 ? std::max<int64_t>(n, 1) : 64;
+            const int64_t run = n <= kSeqWidthMax ? std::max<int64_t>(n, 1) : 64;
             const int32_t cnt = (int32_t)((n + run - 1) / run);
             cur[k] = {nbuf, std::max(cnt, 1)};
             for (int64_t j = 0; j < std::max<int64_t>(n, 1); j += run)
@@ -404,7 +404,6 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
         return rc;
     }
     c->stream = c->own_stream;
-    c->leaves_cap = cap + kLeafListSpare;
     bool ok = alloc_particles(c, c->st[0], cap) == AG2_OK && alloc_particles(c, c->st[1], cap) == AG2_OK;
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
@@ -416,7 +415,6 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
          cudaMalloc(&c->perm_final, cap * 4) == cudaSuccess && cudaMalloc(&c->ap[0], cap * 4) == cudaSuccess &&
          cudaMalloc(&c->ap[1], cap * 4) == cudaSuccess && cudaMalloc(&c->nl[0], cap * 4) == cudaSuccess &&
          cudaMalloc(&c->nl[1], cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->leaves, (cap + kLeafListSpare) * 4) == cudaSuccess &&
          cudaMalloc(&c->lroots, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->pkey, 6 * cap * sizeof(int64_t)) == cudaSuccess &&
          cudaMalloc(&c->tag_id, cap * 4) == cudaSuccess && cudaMalloc(&c->tag_gp, cap) == cudaSuccess &&
@@ -447,7 +445,7 @@ int ag2_destroy(ag2_ctx *c)
                   c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
                   c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->retry_groups, c->inst_first, c->inst_R,
                   c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax,
-                  c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->leaves, c->pkey, c->lroots};
+                  c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     if (c->ctl_snap) cudaFreeHost(c->ctl_snap);
@@ -677,7 +675,7 @@ static unsigned long long step_key(Ctx *c, double dt, double hubble, int with_vi
 {
     unsigned long long h = 1469598103934665603ull;
     const void *ptrs[] = {c->nd.start, c->nd.bkey, c->nd.wrec, c->nd.lint, c->hist, c->stream, c->gas_prefix,
-                          c->groups, c->inst_first, c->leaves, c->pkey};
+                          c->groups, c->inst_first, c->pkey};
     h = fnv(h, ptrs, sizeof(ptrs));
     const int64_t sizes[] = {(int64_t)c->n, c->n_inst, (int64_t)c->node_cap, (int64_t)c->hist_cap, c->ngas,
                              c->walk_variant, c->ngroups, with_visual, c->graph_epoch};

@@ -32,8 +32,6 @@ namespace ag2 {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kWidthBlocks = 608;  // 4 x 152 SMs
-constexpr int kSeqWidthMax = 4096;
 constexpr int kMaxDropNodes = 1 << 16;  // nodes with out-of-bounds tails tracked for the ordering pass
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
@@ -212,7 +210,7 @@ __device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
 // root of instance k is node k (Tree.cpp:28-33: centre at the origin, half-width
 // from calcTreeWidth, depth 0)
 __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *first, const double *R, int thresh,
-                            int32_t *nl0, int32_t *leaves, bool local_ok, int32_t *lroots)
+                            int32_t *nl0, bool local_ok, int32_t *lroots)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_inst) return;
@@ -235,7 +233,6 @@ __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *
     const uint8_t needs = mode == MODE_PAR ? 1 : mode == MODE_SER_ENTRY ? (local_ok ? 2 : 1) : 0;
     nd.needs[k] = needs;
     nd.leafpos[k] = (mode == MODE_VEC1) ? start : -1;
-    if (mode == MODE_VEC1) leaves[atomicAdd(&ctl->nleaf, 1)] = k;
     if (needs == 2) atomicAdd(&ctl->nlocal_part, n);
     if (needs) set_bounds(nd, k, R[k]);
     if (needs == 1) {
@@ -256,7 +253,6 @@ __global__ void k_ctl_reset(Ctx::Ctl *ctl, int n_inst)
     ctl->any_drop = 0;
     ctl->ndrop_nodes = 0;
     ctl->next_active = 0;
-    ctl->nleaf = 0;
 }
 
 // Block-wide reservation in a compact list: every thread of the block calls
@@ -302,7 +298,6 @@ struct LevelBufs {
     int32_t *hist, *cursor;  // 9 per split-list entry
     const int32_t *nl;       // this level's split list (node ids)
     int32_t *nl_next;
-    int32_t *leaves;         // every non-empty leaf
     int32_t *drop_list;      // nodes with out-of-bounds tails of two or more
     int32_t *lroots;         // roots of serial subtrees for k_local
     bool local_ok;           // serial subtrees go to k_local (else they stay in the level loop)
@@ -516,12 +511,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes(LevelPair lpair, int thresh, i
         b.nl_next[q] = (int32_t)c;
         nd.nlx[c] = q;
     }
-    // leaves: one-particle children of a parallel node, and nodes of this list
-    // that stay leaves; internal nodes with their level
-    const bool leaf_self = exists && o == 0 && !internal;
-    const bool lflag = (split && cm == MODE_VEC1) || leaf_self;
-    const int32_t ql = block_reserve<int32_t>(lflag, &ctl->nleaf, 1, sh, &sbase);
-    if (lflag) b.leaves[ql] = (int32_t)(leaf_self ? nid : c);
+    // internal nodes with their level
     const bool iflag = split && o == 0;
     const int32_t qi = block_reserve<int32_t>(iflag, &ctl->nlint, 1, sh, &sbase);
     if (iflag) nd.lint[qi] = make_int2((int)nid, level);
@@ -1046,18 +1036,20 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
     store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, ra);
 }
 
-// Leaves (every level at once), on the state in tree order.  -1 entries pad
-// the list's per-warp stretches.
-__global__ void __launch_bounds__(kBlock) k_moments_leaf(const Ctx::Ctl *ctl, const int32_t *__restrict__ list,
-                                                         Nodes nd, Particles P, const double *gas_prefix,
+// Leaves (every level at once), on the state in tree order, one thread per
+// slot: the thread of a leaf's first slot computes it.  pnode[s] is the node a
+// slot settled in (its leaf, or the node whose out-of-bounds tail holds it),
+// and a leaf's in-bounds particle sits at its first slot, so these are exactly
+// the non-empty leaves, met in tree order: neighbouring threads read
+// neighbouring particles.
+__global__ void __launch_bounds__(kBlock) k_moments_leaf(int n, const int32_t *__restrict__ pnode, Nodes nd,
+                                                         Particles P, const double *gas_prefix,
                                                          const int32_t *gas_off, const uint8_t *gas_uni, RecArgs ra)
 {
-    const int nleaf = ctl->nleaf;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nleaf; t += gridDim.x * blockDim.x) {
-        const int64_t nid = list[t];
-        if (nid < 0) continue;
-        const int32_t start = nd.start[nid];
-        moments_leaf(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, ra);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const int32_t v = pnode[s];
+        if (v < 0 || nd.first[v] >= 0 || nd.start[v] != s) continue;
+        moments_leaf(nd, v, P, [=](int32_t k) { return s + k; }, gas_prefix, gas_off, gas_uni, ra);
     }
 }
 
@@ -1148,8 +1140,7 @@ __global__ void k_bucket(Ctx::Ctl *ctl, const int2 *__restrict__ lint, int32_t *
 // never holds more than split_threshold - 1 particles, so one warp builds it in
 // shared memory, level by level, with the level loop's rules: the same rounded
 // bounds, digits, modes, drop tails in upload order, child centres and
-// half-widths.  Its leaves and internal nodes join the lists the moments
-// passes read.
+// half-widths.  Its internal nodes join the list the internal moments read.
 //
 // Nodes come from a warp-private pool of kPoolChunk nodes (one global atomic
 // per chunk); a chunk's unused tail stays a hole in the pool, which no kernel
@@ -1160,7 +1151,6 @@ constexpr int kLocalCapMax = 1024;  // largest serial subtree (particles) built 
 constexpr int kLocalWarps = 7;      // warps per thread block of k_local (fewer for large subtrees)
 constexpr int kLocalBlocks = 4;     // resident blocks per SM the registers are budgeted for
 constexpr int kPoolChunk = 512;     // nodes per warp-private pool chunk
-constexpr int kLeafChunk = 256;     // leaf-list entries per warp-private stretch
 constexpr int kIntChunk = 128;      // internal-node-list entries per warp-private stretch
 constexpr int kCoop = 16;           // frontier nodes of more particles are done by the whole warp
 
@@ -1174,8 +1164,8 @@ __host__ __device__ constexpr size_t local_smem_bytes(int cap) { return (size_t)
 __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const int32_t *__restrict__ roots, int cap,
                                                             Nodes nd, Ctx::Ctl *ctl, const int64_t *__restrict__ pkey,
                                                             int64_t keycap, int32_t *perm_final, int32_t *pnode,
-                                                            const int32_t *__restrict__ sid, int32_t *leaves,
-                                                            int64_t leaf_cap, int max_depth, int64_t node_cap)
+                                                            const int32_t *__restrict__ sid, int max_depth,
+                                                            int64_t node_cap)
 {
     extern __shared__ __align__(16) unsigned char lsm[];
     const unsigned full = 0xffffffffu;
@@ -1198,8 +1188,7 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
 
     const int nroots = ctl->nlocal;
     unsigned long long pool = 0, pool_end = 0;  // warp-private node pool [pool, pool_end)
-    int lpool = 0, lpool_end = 0;                // warp-private stretch of the leaf list
-    int ipool = 0, ipool_end = 0;                // ... and of the internal-node list
+    int ipool = 0, ipool_end = 0;                // warp-private stretch of the internal-node list
     long long splits = 0;
     int deepest = 0;
     for (int r = blockIdx.x * (blockDim.x >> 5) + wib; r < nroots; r += nwarps) {
@@ -1350,43 +1339,6 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
                         nd.leafpos[fnc[f]] = -1;
                     }
                     run += __popc(bb);
-                }
-            }
-            // the leaves of this level join the leaf list
-            {
-                int nl = 0;
-                for (int f = lane; f < nf; f += 32) nl += FF[f] == -1 ? 1 : 0;
-                nl = (int)__reduce_add_sync(full, (unsigned)nl);
-                if (nl) {
-                    const int rem = lpool_end - lpool;
-                    int nb = 0;
-                    if (nl > rem) {  // the rest goes to a fresh stretch
-                        const int grab = max(nl - rem, kLeafChunk);
-                        if (lane == 0) nb = atomicAdd(&ctl->nleaf, grab);
-                        nb = __shfl_sync(full, nb, 0);
-                        if ((int64_t)nb + grab > leaf_cap) {
-                            if (lane == 0) atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
-                            return;
-                        }
-                    }
-                    int run = 0;
-                    for (int f0 = 0; f0 < nf; f0 += 32) {
-                        const int f = f0 + lane;
-                        const bool isl = f < nf && FF[f] == -1;
-                        const unsigned bl = __ballot_sync(full, isl);
-                        if (isl) {
-                            const int k = run + __popc(bl & lt);
-                            leaves[k < rem ? lpool + k : nb + (k - rem)] = fnc[f];
-                        }
-                        run += __popc(bl);
-                    }
-                    if (nl > rem) {
-                        const int grab = max(nl - rem, kLeafChunk);
-                        lpool = nb + (nl - rem);
-                        lpool_end = nb + grab;
-                    } else {
-                        lpool += nl;
-                    }
                 }
             }
             // this level's internal nodes join the internal-node list with their level
@@ -1546,7 +1498,6 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
             level++;
         }
     }
-    for (int k = lpool + lane; k < lpool_end; k += 32) leaves[k] = -1;  // the stretches' unused tails
     for (int k = ipool + lane; k < ipool_end; k += 32) nd.lint[k] = make_int2(-1, 0);
     if (lane == 0) {
         if (splits) atomicAdd((unsigned long long *)&ctl->local_splits, (unsigned long long)splits);
@@ -1737,7 +1688,6 @@ static LevelBufs level_bufs(Ctx *c, int w)
     b.cursor = c->cursor;
     b.nl = c->nl[w];
     b.nl_next = c->nl[w ^ 1];
-    b.leaves = c->leaves;
     b.drop_list = c->drop_list;
     b.lroots = c->lroots;
     b.local_ok = false;
@@ -1843,7 +1793,6 @@ void build_tree_finish_captured(Ctx *c)
     c->nnodes = h.node_count;
     c->nnodes_true = h.loop_nodes + 8 * (int64_t)h.local_splits;
     c->ninternal = (c->nnodes_true - c->n_inst) / 8;
-    c->nleaves = h.nleaf;
     c->root_radius = c->inst_R_pin ? c->inst_R_pin[0] : 0.0;
     c->inst_R_h.assign(c->inst_R_pin, c->inst_R_pin + c->n_inst);
     c->have_tree = true;
@@ -1922,7 +1871,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     // serial subtrees (fewer than split_threshold particles) are built one warp each when they fit
     const bool local_ok = thresh - 1 <= kLocalCapMax;
     AG2_LAUNCH(c, k_root_init, grid_for(K, kBlock), kBlock, 0, K, c->nd, c->ctl, c->inst_first, c->inst_R, thresh,
-               c->nl[0], c->leaves, local_ok, c->lroots);
+               c->nl[0], local_ok, c->lroots);
     AG2_LAUNCH(c, k_level0, grid_for(n, kBlock), kBlock, 0, n, c->pinst, c->nd, S.px, S.py, S.pz, level_bufs(c, 0),
                c->ctl);
     LevelPair lpair;
@@ -2016,7 +1965,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         lc.blocks = c->loc_blocks;
         lc.smem = c->loc_smem;
         AG2_LAUNCH(c, k_local, lc.blocks, lc.wpb * 32, lc.smem, c->lroots, lc.lcap, c->nd, c->ctl, c->pkey,
-                   (int64_t)c->cap, c->perm_final, c->pnode, S.id, c->leaves, (int64_t)c->leaves_cap,
+                   (int64_t)c->cap, c->perm_final, c->pnode, S.id,
                    (int)AG2_MAX_DEPTH, (int64_t)c->node_cap);
         AG2_LAUNCH(c, k_sort_drops, fixed_grid, kBlock, 0, c->ctl, c->drop_list, c->nd, c->perm_final, S.id, c->perm2);
     } else {
@@ -2029,7 +1978,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
                                 (size_t)blocks * lc.wpb * kPoolChunk + 1024;
             if ((rc = ensure_node_capacity(c, need)) != AG2_OK) return rc;
             AG2_LAUNCH(c, k_local, blocks, lc.wpb * 32, lc.smem, c->lroots, lc.lcap, c->nd, c->ctl, c->pkey,
-                       (int64_t)c->cap, c->perm_final, c->pnode, S.id, c->leaves, (int64_t)c->leaves_cap,
+                       (int64_t)c->cap, c->perm_final, c->pnode, S.id,
                        (int)AG2_MAX_DEPTH, (int64_t)c->node_cap);
             if ((rc = sync_ctl(c)) != AG2_OK) return rc;
             const Ctx::Ctl &h = *c->ctl_host;
@@ -2043,7 +1992,6 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         c->nnodes = c->ctl_host->node_count;
         c->nnodes_true = loop_nodes + 8 * (int64_t)c->ctl_host->local_splits;
         c->ninternal = (c->nnodes_true - K) / 8;
-        c->nleaves = c->ctl_host->nleaf;
         if (c->ctl_host->ndrop_nodes > kMaxDropNodes) return build_error(c, AG2_E_CAPACITY);
         if (c->ctl_host->ndrop_nodes > 0)
             AG2_LAUNCH(c, k_sort_drops, (unsigned)c->ctl_host->ndrop_nodes, kBlock, 0, c->ctl, c->drop_list, c->nd,
@@ -2062,8 +2010,8 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
 
     // moments: every leaf at once, then the internal nodes level by level,
     // deepest first (the internal-node list bucketed by level)
-    const unsigned gl = capture ? fixed_grid : std::max(1u, grid_for(c->nleaves, kBlock));
-    AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, c->ctl, c->leaves, c->nd, c->S(), c->gas_prefix, c->gas_off,
+    const unsigned gl = capture ? fixed_grid : std::max(1u, grid_for(n, kBlock));
+    AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, n, c->pnode, c->nd, c->S(), c->gas_prefix, c->gas_off,
                c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
     const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
     AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint);

@@ -168,13 +168,10 @@ struct Ctx {
     int32_t *perm_final = nullptr;
     int32_t *ap[2] = {};          // active slots of a level (compact list)
     int32_t *nl[2] = {};          // split list of a level (node ids)
-    int32_t *leaves = nullptr;    // every non-empty leaf (-1 entries are padding)
-    size_t leaves_cap = 0;
     int32_t *lroots = nullptr;    // roots of serial subtrees built by one warp each
     int64_t *pkey = nullptr;      // 2 buffers x 3 coordinates x cap ordered keys
     int64_t nnodes_true = 0;      // nodes of the tree (nnodes also counts unused pool tails)
     std::vector<int32_t> lvl_cnt_h, lvl_start_h;  // internal nodes per level and their list segments
-    int32_t nleaves = 0;
     int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
     int32_t *refnode = nullptr;   // the reference's Particle::node per slot (-1 = null)
     int32_t *slot_of = nullptr;   // tree-order slot of each upload index
@@ -262,7 +259,6 @@ struct Ctx {
         int32_t retry_claim;    // ... and claimed by it
         int32_t ndrop_nodes;
         int32_t next_active;    // active slots at the next level
-        int32_t nleaf;          // entries of the leaf list
         int32_t nlocal;         // serial subtree roots for k_local
         int32_t nlint;          // entries of the internal-node list
         int32_t level;          // level loop: the level being split
@@ -365,9 +361,10 @@ __host__ __device__ inline double scale2(double x, int k)
     return x * ldexp(1.0, k);  // zero, subnormal, inf, NaN, or a result outside the normal range
 }
 
-// entries of the leaf list beyond one per particle: the unused tails of the
-// build's per-warp stretches
-constexpr size_t kLeafListSpare = size_t(1) << 22;
+
+// the root half-width's sums are sequential (the reference's, bit for bit) up to
+// this many particles per instance, a 64-ary tree of sequential runs above
+constexpr int kSeqWidthMax = 4096;
 
 // status helpers
 int set_err(Ctx *c, int code, const std::string &msg);
