@@ -879,11 +879,13 @@ int ag2_step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int wit
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
     if ((rc = run_forces(c))) return rc;
     phase_mark(c, "Force Calculation");
+    // accelerations are final after the walk: their copy runs during the
+    // closing kick and the internal-energy update
+    if (io->acc_out && (rc = dl_field(c, k++, AG2_ACC, io->acc_out))) return rc;
     if ((rc = run_close_step(c, dt, hubble_factor))) return rc;
     phase_mark(c, "second kick");
     if ((rc = check_walk(c))) return rc;
     if (io->vel_out && (rc = dl_field(c, k++, AG2_VEL, io->vel_out))) return rc;
-    if (io->acc_out && (rc = dl_field(c, k++, AG2_ACC, io->acc_out))) return rc;
     if (io->U_out && (rc = dl_field(c, k++, AG2_U, io->U_out))) return rc;
     rc = dl_end(c);
     phase_finish(c);
