@@ -542,16 +542,18 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
     if (t < nap) {
         i = b.ap[t];
         const int j = b.posnode[i];
-        const int32_t nid = b.nl[j];
         const int32_t p = b.perm[i];
         const int d = b.digit[i];
+        // the keys are loaded with the slot's other fields, off the chain
+        // through the node, the cursor atomic and the child
+        const int64_t kx = b.kx[i], ky = b.ky[i], kz = b.kz[i];
+        const int32_t nid = b.nl[j];
         const int np = agg_inc(b.cursor, 9 * j + d);
         const int32_t first = nd.first[nid];
         if (first >= 0 && d < 8) {
             const int32_t child = first + d;
             const uint8_t cn = nd.needs[child];
             if (cn) {  // split again: by the next level (1) or by k_local (2), which reads the keys there
-                const int64_t kx = b.kx[i], ky = b.ky[i], kz = b.kz[i];
                 b.kx_next[np] = kx;
                 b.ky_next[np] = ky;
                 b.kz_next[np] = kz;
