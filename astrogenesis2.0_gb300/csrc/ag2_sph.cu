@@ -117,45 +117,67 @@ __global__ void k_final(int n, TreeView t, const uint8_t *type, uint8_t *flag, i
     }
 }
 
-__device__ __forceinline__ double cubic_spline(double r, double h)
+// The node's gas particles are gathered 32 at a time into a per-warp queue
+// (ballot over its range), so every FP64 square root and division runs on 32
+// gas lanes rather than on the one or two gas lanes of a mixed stretch (FP64
+// issues at 1/64 of the FP32 rate, whatever the active lanes).  alpha =
+// 1 / (pi h^3) is the same for every particle of the node (kernel.cpp:4-16
+// computes it per call from the same h).
+__global__ void __launch_bounds__(kBlock) k_rho(TreeView t, const double *px, const double *py, const double *pz,
+                                                const double *m, const uint8_t *type, const int32_t *list,
+                                                const Ctx::Ctl *ctl, double *rho_node)
 {
-    // kernel::cubicSplineKernel (kernel.cpp:4-16)
-    double alpha = 1.0 / (kPi * h * h * h);
-    double q = r / h;
-    if (q < 1.0) return alpha * (1 - 1.5 * q * q + 0.75 * q * q * q);
-    if (q < 2.0) {
-        double t = 2 - q;
-        return alpha * 0.25 * (t * t * t);
-    }
-    return 0.0;
-}
-
-__global__ void k_rho(TreeView t, const double *px, const double *py, const double *pz, const double *m,
-                      const uint8_t *type, const int32_t *list, const Ctx::Ctl *ctl, double *rho_node)
-{
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
+    __shared__ int32_t queue[kBlock / 32][64];
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (w >= ctl->list_count) return;
-    int64_t nd = list[w];
-    double h = t.radius[nd] * 2;  // h = radius * 2 (Node.cpp:765)
-    double cx = t.mom[nd].cx, cy = t.mom[nd].cy, cz = t.mom[nd].cz;
-    int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
-    uint8_t md = t.mode[nd];
+    int32_t *q = queue[threadIdx.x >> 5];
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t nd = list[w];
+    const double h = t.radius[nd] * 2;  // h = radius * 2 (Node.cpp:765)
+    const double alpha = 1.0 / (kPi * h * h * h);
+    const double cx = t.mom[nd].cx, cy = t.mom[nd].cy, cz = t.mom[nd].cz;
+    const int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
+    const uint8_t md = t.mode[nd];
+    // the childParticles multiplicity of slot j: the parent's list plus serial
+    // insertion for a serial entry node (Node.cpp:518, 615), in-bounds only below it
+    auto mult = [&](int32_t j) -> int {
+        if (md == MODE_SER_ENTRY) return j < reached_end ? 2 : 1;
+        if (md == MODE_SER) return j < reached_end ? 1 : 0;
+        return 1;
+    };
     double acc = 0.0;
-    for (int32_t j = s + lane; j < e; j += 32) {
-        if (type[j] != 2) continue;
-        int mult;
-        if (md == MODE_SER_ENTRY)
-            mult = j < reached_end ? 2 : 1;  // list from the parent plus serial insertion (Node.cpp:518, 615)
-        else if (md == MODE_SER)
-            mult = j < reached_end ? 1 : 0;
-        else
-            mult = 1;
-        if (!mult) continue;
-        double dx = px[j] - cx, dy = py[j] - cy, dz = pz[j] - cz;
-        double r = sqrt(dx * dx + dy * dy + dz * dz);
-        acc += mult * (m[j] * cubic_spline(r, h));
+    auto add = [&](int32_t j) {
+        const double dx = px[j] - cx, dy = py[j] - cy, dz = pz[j] - cz;
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double qh = r / h;  // kernel::cubicSplineKernel (kernel.cpp:4-16)
+        double W = 0.0;
+        if (qh < 1.0) {
+            W = alpha * (1 - 1.5 * qh * qh + 0.75 * qh * qh * qh);
+        } else if (qh < 2.0) {
+            const double u = 2 - qh;
+            W = alpha * 0.25 * (u * u * u);
+        }
+        acc += mult(j) * (m[j] * W);
+    };
+    int qn = 0;
+    for (int32_t j0 = s; j0 < e; j0 += 32) {
+        const int32_t j = j0 + lane;
+        const bool g = j < e && type[j] == 2 && mult(j) != 0;
+        const unsigned bm = __ballot_sync(0xffffffffu, g);
+        if (g) q[qn + __popc(bm & lt)] = j;
+        qn += __popc(bm);
+        __syncwarp();
+        if (qn >= 32) {
+            const int32_t jj = q[lane];
+            __syncwarp();
+            if (lane < qn - 32) q[lane] = q[32 + lane];
+            qn -= 32;
+            __syncwarp();
+            add(jj);
+        }
     }
+    if (lane < qn) add(q[lane]);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) rho_node[nd] = acc;
 }
