@@ -21,13 +21,16 @@ __device__ __forceinline__ bool acc_nan(const Particles &s, int i)
     return isnan(s.ax[i]) || isnan(s.ay[i]) || isnan(s.az[i]);
 }
 
-// v = v + a*dt/2, skipped when acc has a NaN (TimeIntegration.cpp:12-18)
+// v = v + a*dt/2, skipped when acc has a NaN (TimeIntegration.cpp:12-18).
+// (a*dt)/2 is taken as (a*dt)*0.5: both are the correctly rounded value of the
+// same real number, and the multiply spares an FP64 division (about nine
+// multiplies' worth of the FP64 pipe on this part).
 __device__ __forceinline__ void kick1(Particles &s, int i, double dt)
 {
     if (acc_nan(s, i)) return;
-    s.vx[i] = __dadd_rn(s.vx[i], __ddiv_rn(__dmul_rn(s.ax[i], dt), 2.0));
-    s.vy[i] = __dadd_rn(s.vy[i], __ddiv_rn(__dmul_rn(s.ay[i], dt), 2.0));
-    s.vz[i] = __dadd_rn(s.vz[i], __ddiv_rn(__dmul_rn(s.az[i], dt), 2.0));
+    s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dmul_rn(s.ax[i], dt), 0.5));
+    s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dmul_rn(s.ay[i], dt), 0.5));
+    s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dmul_rn(s.az[i], dt), 0.5));
 }
 
 // x = x + v*dt (TimeIntegration.cpp:21-25)
@@ -89,9 +92,11 @@ __global__ void k_close_step(int n, Particles s, double dt, double f)
         if (!isnan(du)) s.U[i] = __dadd_rn(s.U[i], __dmul_rn(du, dt));
         s.dUdt[i] = 0.0;
     }
-    s.px[i] = __dmul_rn(s.px[i], f);
-    s.py[i] = __dmul_rn(s.py[i], f);
-    s.pz[i] = __dmul_rn(s.pz[i], f);
+    if (f != 1.0) {  // x * 1 is x: without expansion the positions are not touched
+        s.px[i] = __dmul_rn(s.px[i], f);
+        s.py[i] = __dmul_rn(s.py[i], f);
+        s.pz[i] = __dmul_rn(s.pz[i], f);
+    }
     kick1(s, i, dt);
 }
 
