@@ -21,16 +21,24 @@ __device__ __forceinline__ bool acc_nan(const Particles &s, int i)
     return isnan(s.ax[i]) || isnan(s.ay[i]) || isnan(s.az[i]);
 }
 
-// v = v + a*dt/2, skipped when acc has a NaN (TimeIntegration.cpp:12-18).
-// (a*dt)/2 is taken as (a*dt)*0.5: both are the correctly rounded value of the
-// same real number, and the multiply spares an FP64 division (about nine
-// multiplies' worth of the FP64 pipe on this part).
+// x / 2, exactly: the exponent field less one where x and the result are
+// normal, else the multiply by 0.5 (zero, subnormal, infinity, NaN).  Both are
+// the correctly rounded value of the same real number; the integer path keeps
+// the FP64 pipe (1/64 of the FP32 rate on this part) for the other arithmetic.
+__device__ __forceinline__ double half_of(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const int ef = (int)((b >> 52) & 0x7ff);
+    return (ef > 1 && ef < 0x7ff) ? __longlong_as_double(b - (1LL << 52)) : __dmul_rn(x, 0.5);
+}
+
+// v = v + a*dt/2, skipped when acc has a NaN (TimeIntegration.cpp:12-18)
 __device__ __forceinline__ void kick1(Particles &s, int i, double dt)
 {
     if (acc_nan(s, i)) return;
-    s.vx[i] = __dadd_rn(s.vx[i], __dmul_rn(__dmul_rn(s.ax[i], dt), 0.5));
-    s.vy[i] = __dadd_rn(s.vy[i], __dmul_rn(__dmul_rn(s.ay[i], dt), 0.5));
-    s.vz[i] = __dadd_rn(s.vz[i], __dmul_rn(__dmul_rn(s.az[i], dt), 0.5));
+    s.vx[i] = __dadd_rn(s.vx[i], half_of(__dmul_rn(s.ax[i], dt)));
+    s.vy[i] = __dadd_rn(s.vy[i], half_of(__dmul_rn(s.ay[i], dt)));
+    s.vz[i] = __dadd_rn(s.vz[i], half_of(__dmul_rn(s.az[i], dt)));
 }
 
 // x = x + v*dt (TimeIntegration.cpp:21-25)
