@@ -1919,12 +1919,17 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         }
         int64_t known_nodes = c->ctl_host->node_count;  // nodes after the last level read back
         int64_t nnl = c->ctl_host->cur_nnl;             // split nodes of the level after it
+        int64_t nap = c->ctl_host->cur_nap;             // and its active slots
         int queued = 0, seen = 0;
         bool more = nnl > 0;
         while (more) {
             // pool room for the levels in flight: the one read back next
-            // allocates 8 * nnl children, the one queued now at most 8 times that
-            if ((rc = ensure_node_capacity(c, (size_t)(known_nodes + 72 * nnl + 8))) != AG2_OK) return rc;
+            // allocates 8 * nnl children; of those, the ones the level queued
+            // now splits are at most 8 * nnl, and each holds two or more of
+            // the nap active particles
+            const int64_t next_split = std::min<int64_t>(8 * nnl, nap / 2);
+            if ((rc = ensure_node_capacity(c, (size_t)(known_nodes + 8 * nnl + 8 * next_split + 8))) != AG2_OK)
+                return rc;
             lpair.b[0] = level_bufs(c, 0);
             lpair.b[1] = level_bufs(c, 1);
             lpair.b[0].local_ok = lpair.b[1].local_ok = local_ok;
@@ -1949,6 +1954,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             c->level_base.push_back(h.node_count);
             known_nodes = h.node_count;
             nnl = h.cur_nnl;
+            nap = h.cur_nap;
             more = nnl > 0;
         }
         // the host mirror after the loop (the serial subtrees' launch reads its

@@ -130,13 +130,18 @@ def port_world(d, threads=1, massInH=0.0, e0=0.01, theta=0.5):
     return w
 
 
-@pytest.mark.parametrize("name", ["plummer16k", "disk65k", "general4k", "plummer16k_t8"])
+@pytest.mark.parametrize("name", ["plummer16k", "disk65k", "general4k", "plummer16k_t8", "disk65k_t16"])
 def test_against_port_medium(name):
+    """disk65k_t16: 16 threads put the parallel threshold at 1600, above what one
+    warp builds in shared memory, so the level loop builds the serial levels too."""
     threads, e0, massInH = 1, 0.01, 0.0
     if name == "plummer16k":
         d = ics.plummer(16384, seed=1)
     elif name == "plummer16k_t8":
         d, threads = ics.plummer(16384, seed=1), 8
+    elif name == "disk65k_t16":
+        d, threads = ics.disk_galaxy(49152, 12288, 4096, seed=7), 16
+        e0, massInH = 0.02, d["massInH"]
     elif name == "disk65k":
         d = ics.disk_galaxy(49152, 12288, 4096, seed=7)
         e0, massInH = 0.02, d["massInH"]
