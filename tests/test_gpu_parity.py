@@ -280,6 +280,19 @@ def test_edge_cases():
     with pytest.raises(ag2.AG2Error) as ei:
         c.build_tree()
     assert ei.value.code == ag2.E_COINCIDENT
+    # the same in the level loop: 150 coincident particles keep a parallel node
+    # (threshold 100) splitting until the depth limit; the loop, one level ahead
+    # of the host, reports the error from the control block it reads back
+    pos = np.concatenate([[[0.0, 0.0, 0.0]] * 150, ics.plummer(400, seed=2)["pos"]])
+    d = {"pos": pos, "mass": np.ones(len(pos)), "type": np.ones(len(pos), np.uint8)}
+    c = ctx_for(d)
+    with pytest.raises(ag2.AG2Error) as ei:
+        c.build_tree()
+    assert ei.value.code == ag2.E_COINCIDENT
+    c.close()
+    c = ctx_for(ics.plummer(550, seed=3))  # a context after the failed one builds normally
+    c.build_tree()
+    assert c.node_count()[0] > 1
     # non-finite position
     d = {"pos": np.array([[0.1, np.nan, 0.3], [0.0, 0.0, 0.0]]), "mass": np.ones(2), "type": np.ones(2, np.uint8)}
     c = ag2.Context(2)
