@@ -6,8 +6,8 @@
 //
 // The reference decides octants by FP64 comparisons against node centres that
 // are accumulated as c + r*(+-0.5) from the root, with inclusive bounds tests
-// at every node.  This build is a most-significant-digit radix sort of the
-// particles by those decisions, one tree level per pass: each node that is
+// at every node.  The tree is built as a most-significant-digit radix sort of
+// the particles by those decisions, one tree level per pass: each node that is
 // split at level L gets one pass in which every particle of its range computes
 // its 4-bit digit (octant 0..7, or 8 = outside this node's bounds) against the
 // node's precomputed bounds, and the range is partitioned by digit.  The digit
