@@ -37,6 +37,7 @@ EXPORTS = [
     "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy", "ag2_step_graphs",
     "ag2_block_init", "ag2_block_step", "ag2_set_tags", "ag2_get_tags", "ag2_snapshot_size",
     "ag2_snapshot_encode", "ag2_snapshot_write", "ag2_snapshot_wait", "ag2_ic_count", "ag2_load_ics",
+    "ag2_inject_fault",
 ]
 
 # file formats of ag2_snapshot_* / ag2_load_ics (the reference's format names)
@@ -124,6 +125,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_snapshot_wait.argtypes = [P]
     L.ag2_ic_count.argtypes = [ctypes.c_char_p, I, ctypes.POINTER(ctypes.c_int64)]
     L.ag2_load_ics.argtypes = [P, ctypes.c_char_p, I, P]
+    L.ag2_inject_fault.argtypes = [P, I, I]
     _lib = L
     return L
 
@@ -304,6 +306,11 @@ class Context:
                                          ctypes.byref(io)))
         self.n = n
         return out
+
+    def inject_fault(self, site: int, code: int):
+        """ag2_inject_fault: site 1 makes the next step_host fail with `code`
+        right after the walk (host side only; for tests of the error path)."""
+        self._check(self.L.ag2_inject_fault(self.h, site, code))
 
     # -- introspection --------------------------------------------------------
     def root_radius(self) -> float:

@@ -22,7 +22,6 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libag2.so")
 INCLUDE = os.path.join(REPO, "include")
 ORACLE = os.path.join(REPO, "oracle")
-REF_SRC = "/root/reference/simulation/src"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
@@ -84,8 +83,12 @@ def build_checkers(verbose: bool = False) -> None:
     r = subprocess.run(["make", "-s", "-C", ORACLE, "liboracle.so"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    if os.path.isdir(REF_SRC):
-        r = subprocess.run(["make", "-s", "-C", ORACLE, "ref", f"REF={REF_SRC}"], capture_output=True, text=True)
+    # the reference harness, where a reference checkout exists (oracle/Makefile
+    # locates it: $AG2_REF or its default)
+    r = subprocess.run(["make", "-s", "-C", ORACLE, "print-ref"], capture_output=True, text=True)
+    ref_src = os.path.join(r.stdout.strip(), "simulation", "src") if r.returncode == 0 else ""
+    if ref_src and os.path.isdir(ref_src):
+        r = subprocess.run(["make", "-s", "-C", ORACLE, "ref"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference harness build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:

@@ -598,6 +598,16 @@ static int dl_end(Ctx *c)
     AG2_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     return AG2_OK;
 }
+// Error exit of a call that may have queued read-backs: wait for every copy
+// already on the copy stream, so that none still writes into the caller's
+// buffers or reads the staging area after the call returns (the next upload
+// or download reuses staging on the context's stream).  The first error is
+// the one reported.
+static int dl_abort(Ctx *c, int rc)
+{
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    return rc;
+}
 
 int ag2_download_fields(ag2_ctx *c, int nf, const int *fields, double *const *dst)
 {
@@ -608,8 +618,16 @@ int ag2_download_fields(ag2_ctx *c, int nf, const int *fields, double *const *ds
     int rc;
     if ((rc = dl_begin(c))) return rc;
     for (int k = 0; k < nf; k++)
-        if ((rc = dl_field(c, k, fields[k], dst[k]))) return rc;
+        if ((rc = dl_field(c, k, fields[k], dst[k]))) return dl_abort(c, rc);
     return dl_end(c);
+}
+
+int ag2_inject_fault(ag2_ctx *c, int site, int code)
+{
+    if (!c || site < 0 || site > 1 || code > 0) return AG2_E_INVALID;
+    c->inject_site = site;
+    c->inject_code = code;
+    return AG2_OK;
 }
 
 size_t ag2_count(const ag2_ctx *c) { return c ? c->n : 0; }
@@ -847,11 +865,11 @@ int ag2_step(ag2_ctx *c, double dt, double hubble_factor, int with_visual, doubl
     return rc;
 }
 
-int ag2_step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int with_visual, double Rv,
-                  const ag2_host_io *io)
+// The step itself; ag2_step_host routes every failure through dl_abort, since
+// the position and acceleration read-backs start before the step ends.
+static int step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int with_visual, double Rv,
+                     const ag2_host_io *io)
 {
-    if (!c || !io) return AG2_E_INVALID;
-    if (n == 0) return set_err(c, AG2_E_INVALID, "no particles");
     int rc;
     if ((rc = ag2_upload(c, n, io->pos, io->vel, io->mass, io->U, io->type))) return rc;
     if (io->first && (rc = ag2_set_instances(c, io->n_inst, io->first, io->massInH))) return rc;
@@ -885,11 +903,24 @@ int ag2_step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int wit
     if ((rc = run_close_step(c, dt, hubble_factor))) return rc;
     phase_mark(c, "second kick");
     if ((rc = check_walk(c))) return rc;
+    if (c->inject_site == 1) {  // a failure of the walk's check, as the host sees one (ag2_inject_fault)
+        c->inject_site = 0;
+        return set_err(c, c->inject_code, "injected failure after the walk");
+    }
     if (io->vel_out && (rc = dl_field(c, k++, AG2_VEL, io->vel_out))) return rc;
     if (io->U_out && (rc = dl_field(c, k++, AG2_U, io->U_out))) return rc;
     rc = dl_end(c);
     phase_finish(c);
     return rc;
+}
+
+int ag2_step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int with_visual, double Rv,
+                  const ag2_host_io *io)
+{
+    if (!c || !io) return AG2_E_INVALID;
+    if (n == 0) return set_err(c, AG2_E_INVALID, "no particles");
+    const int rc = step_host(c, n, dt, hubble_factor, with_visual, Rv, io);
+    return rc ? dl_abort(c, rc) : rc;
 }
 
 int ag2_phase_timing(ag2_ctx *c, int enable)

@@ -155,6 +155,7 @@ struct Ctx {
     int64_t launches = 0;
     bool debug_sync = false;  // AG2_DEBUG_SYNC=1: synchronise and check after every launch
     int64_t inter_grav = 0, inter_sph = 0;
+    int32_t inject_site = 0, inject_code = 0;  // ag2_inject_fault: one host-side failure, then cleared
     std::string err;
 
     Particles st[2] = {};

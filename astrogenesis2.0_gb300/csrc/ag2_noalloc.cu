@@ -20,6 +20,7 @@
 // different streams, or from different host threads) race; serialise them.
 #include <cstdint>
 #include <mutex>
+#include <tuple>
 
 #include "ag2_internal.cuh"
 
@@ -156,6 +157,21 @@ __global__ void k_na_out(const NoAllocScratch *s, double *radius)
     if (threadIdx.x == 0) radius[0] = __longlong_as_double((long long)s->R_bits);
 }
 
+// One launch through cudaLaunchKernel, which returns that launch's status.
+// The arguments are converted to the kernel's parameter types first, and the
+// launch reads them through pointers before it returns.
+template <class... P, class... A>
+cudaError_t na_launch(void (*kernel)(P...), int grid, int block, cudaStream_t st, A... args)
+{
+    std::tuple<P...> t(args...);
+    void *pa[sizeof...(P)];
+    std::apply([&pa](auto &...x) {
+        int i = 0;
+        ((pa[i++] = (void *)&x), ...);
+    }, t);
+    return cudaLaunchKernel((const void *)kernel, dim3(grid), dim3(block), pa, 0, st);
+}
+
 // Device address of the scratch array on the current device, looked up once
 // per device.
 int scratch_for_current_device(NoAllocScratch **out)
@@ -187,16 +203,27 @@ extern "C" int ag2_root_radius_noalloc(const double *pos, int64_t n, double *rad
     if (rc != AG2_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const int ni = (int)n;
-    k_na_clear<<<1, 32, 0, st>>>(s);
+    // Each launch's own status comes back from cudaLaunchKernel, so an error
+    // that the caller's earlier work left pending is neither consumed nor
+    // blamed on this call.  A failed launch of this call stops it, and its
+    // error is cleared so that the caller's next cudaGetLastError does not
+    // report it a second time.
+    auto failed = [](cudaError_t e) {
+        if (e == cudaSuccess) return false;
+        cudaGetLastError();
+        return true;
+    };
+    if (failed(na_launch(k_na_clear, 1, 32, st, s))) return AG2_E_CUDA;
     if (ni <= kNaSeqMax) {
-        k_na_seq<<<1, 1, 0, st>>>(pos, ni, s);
+        if (failed(na_launch(k_na_seq, 1, 1, st, pos, ni, s))) return AG2_E_CUDA;
     } else {
         const int nent = (ni + 4095) / 4096;
-        k_na_level2<<<(nent + kNaBlock - 1) / kNaBlock, kNaBlock, 0, st>>>(pos, ni, nent, s);
-        k_na_final<<<1, 32, 0, st>>>(nent, s);
+        if (failed(na_launch(k_na_level2, (nent + kNaBlock - 1) / kNaBlock, kNaBlock, st, pos, ni, nent, s)))
+            return AG2_E_CUDA;
+        if (failed(na_launch(k_na_final, 1, 32, st, nent, s))) return AG2_E_CUDA;
     }
-    k_na_thr<<<1, 32, 0, st>>>(ni, s);
-    k_na_max<<<kNaBlocks, kNaBlock, 0, st>>>(pos, ni, s);
-    k_na_out<<<1, 32, 0, st>>>(s, radius);
-    return cudaGetLastError() == cudaSuccess ? AG2_OK : AG2_E_CUDA;
+    if (failed(na_launch(k_na_thr, 1, 32, st, ni, s))) return AG2_E_CUDA;
+    if (failed(na_launch(k_na_max, kNaBlocks, kNaBlock, st, pos, ni, s))) return AG2_E_CUDA;
+    if (failed(na_launch(k_na_out, 1, 32, st, (const NoAllocScratch *)s, radius))) return AG2_E_CUDA;
+    return AG2_OK;
 }

@@ -122,7 +122,13 @@ int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
  * The positions' read-back overlaps the walk (they are final after the
  * drift).  The out arrays may be the input arrays.  With first != NULL the
  * particles are n_inst simulations, as ag2_set_instances(n_inst, first,
- * massInH) after the upload. */
+ * massInH) after the upload.
+ * Host memory: the read-backs are asynchronous copies into the *_out arrays
+ * while later stages run.  They overlap the device work only when the arrays
+ * are page-locked (cudaHostAlloc / cudaHostRegister); with pageable memory each
+ * copy blocks until it has landed and the stages after it queue behind it.
+ * The arrays are written until the call returns, on success and on failure
+ * alike (a failing call waits for the copies it started before returning). */
 typedef struct ag2_host_io {
     const double *pos, *vel, *mass, *U, *acc;
     const uint8_t *type;
@@ -135,8 +141,16 @@ int ag2_step_host(ag2_ctx *ctx, size_t n, double dt, double hubble_factor, int w
                   double visualDensityRadius, const ag2_host_io *io);
 /* Several fields to host buffers in one call, as ag2_download each: the
  * gather of one field into upload order runs while the previous one crosses
- * to the host, and the call returns once every copy has landed. */
+ * to the host, and the call returns once every copy has landed (also when it
+ * fails).  The overlap needs page-locked destination buffers; pageable ones
+ * are filled one copy after another. */
 int ag2_download_fields(ag2_ctx *ctx, int nfields, const int *fields, double *const *dst);
+/* Host-side fault injection for tests of the error paths: with site 1 the
+ * next ag2_step_host fails with `code` (an AG2_E_* value) right after the walk
+ * and its check, as it would when the walk reports AG2_E_STACK, with the
+ * position and acceleration read-backs already queued.  Site 0 clears it.
+ * Nothing on the device is made to fail.  No counterpart in the reference. */
+int ag2_inject_fault(ag2_ctx *ctx, int site, int code);
 size_t ag2_count(const ag2_ctx *ctx);
 
 /* Independent simulations in one context (the batched ensemble and the

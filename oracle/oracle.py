@@ -23,6 +23,25 @@ FIELDS = {"pos": 0, "vel": 1, "acc": 2, "mass": 3, "h": 4, "rho": 5, "P": 6, "T"
 VECTOR_FIELDS = {"pos", "vel", "acc"}
 
 _libs: dict[str, ctypes.CDLL] = {}
+_ref_root: list = []
+
+
+def reference_checkout():
+    """Root of the reference checkout (the directory holding simulation/ and
+    input_data/), or None where there is none.  The location is the AG2_REF
+    environment variable when set, else the one oracle/Makefile names."""
+    if not _ref_root:
+        root = os.environ.get("AG2_REF")
+        if not root:
+            import subprocess
+
+            try:
+                r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True, timeout=30)
+                root = r.stdout.strip() if r.returncode == 0 else None
+            except (OSError, subprocess.SubprocessError):
+                root = None
+        _ref_root.append(root if root and os.path.isdir(os.path.join(root, "simulation", "src")) else None)
+    return _ref_root[0]
 
 
 def available(kind: str) -> bool:

@@ -8,7 +8,8 @@ oracle/_ref/libag2ref.so by oracle/Makefile) on
   * oracle.snapio.random_particles(1000, seed=3), written with saveData in
     each snapshot format for count 1000 and 777: sha256 of the file bytes
     (the ag/agc/age header's 4 uninitialised padding bytes zeroed).
-Usage: python tests/golden/make_ic_golden.py [reference checkout]
+Usage: python tests/golden/make_ic_golden.py [reference checkout]  (default: $AG2_REF, else the
+location oracle/Makefile names)
 """
 import hashlib
 import json
@@ -17,6 +18,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import oracle  # noqa: E402
 import snapio as S  # noqa: E402
 
 EXAMPLES = [("gassphere_littleendian.dat", "gadget"), ("galaxy_littleendian.dat", "gadget"),
@@ -24,7 +26,8 @@ EXAMPLES = [("gassphere_littleendian.dat", "gadget"), ("galaxy_littleendian.dat"
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else oracle.reference_checkout()
+    assert ref, "no reference checkout: set AG2_REF or pass its path"
     assert S.ref_lib() is not None, "build oracle/_ref first (make -C oracle ref)"
     out = {"examples": {}, "snapshots": {}}
     for name, fmt in EXAMPLES:

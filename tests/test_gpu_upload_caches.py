@@ -147,3 +147,54 @@ def test_step_host_with_instances():
         ref = {f: b.download(f) for f in ("pos", "vel", "acc", "U")}
         for f, got in (("pos", pos), ("vel", vel), ("acc", acc), ("U", U)):
             np.testing.assert_array_equal(got, ref[f], err_msg=f)
+
+
+def test_step_host_failure_after_readbacks_started():
+    """A step_host that fails after its position and acceleration read-backs
+    were queued (here a host-injected AG2_E_STACK right after the walk, the
+    point where the walk's own stack check would report one) returns only once
+    those copies have landed: the position buffer holds the drifted positions,
+    and the next upload and step through the same staging area give the same
+    bits as a fresh context."""
+    import torch
+
+    import ag2
+
+    d = ics.small_gas_cloud(20000, seed=41)
+    n = len(d["mass"])
+    kw = dict(e0=0.02, theta=0.5, massInH=d["massInH"])
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    c = ag2.Context(n, **kw)
+    c.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    c.build_tree()
+    c.sph_density()
+    c.forces()
+    acc0 = c.download("acc")
+    hpos, hvel, hmass, hU, htype, hacc = (pin(d["pos"]), pin(d["vel"]), pin(d["mass"]), pin(d["U"]), pin(d["type"]),
+                                          pin(acc0))
+    out = {"pos": pin(np.zeros_like(d["pos"])), "acc": pin(np.zeros_like(acc0)), "vel": pin(np.zeros_like(d["vel"])),
+           "U": pin(np.zeros_like(d["U"]))}
+    c.inject_fault(1, ag2.E_STACK)
+    with pytest.raises(ag2.AG2Error) as ei:
+        c.step_host(1e-3, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=out)
+    assert ei.value.code == ag2.E_STACK
+    # the positions after the kick and drift, as a separate context computes them
+    r = ag2.Context(n, **kw)
+    r.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    r.set_field("acc", acc0)
+    r.kick_drift(1e-3)
+    assert np.array_equal(out["pos"], r.download("pos"))
+    r.close()
+    # the same context, reused at once: a full step_host against a fresh context
+    d2 = ics.small_gas_cloud(20000, seed=42)
+    outs = {k: pin(np.zeros_like(v)) for k, v in out.items()}
+    c.step_host(1e-3, pin(d2["pos"]), pin(d2["mass"]), pin(d2["type"]), vel=pin(d2["vel"]), U=pin(d2["U"]),
+                acc=pin(acc0), out=outs)
+    f = ag2.Context(n, **kw)
+    ref = {k: pin(np.zeros_like(v)) for k, v in out.items()}
+    f.step_host(1e-3, pin(d2["pos"]), pin(d2["mass"]), pin(d2["type"]), vel=pin(d2["vel"]), U=pin(d2["U"]),
+                acc=pin(acc0), out=ref)
+    for k in outs:
+        assert np.array_equal(outs[k], ref[k]), k
+    c.close()
+    f.close()

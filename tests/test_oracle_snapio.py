@@ -16,7 +16,11 @@ sys.path.insert(0, os.path.join(HERE, "..", "oracle"))
 import snapio as S  # noqa: E402
 
 GOLDEN = json.load(open(os.path.join(HERE, "golden", "ic_examples.json")))
-EXAMPLES = "/root/reference/input_data/Example"
+sys.path.insert(0, os.path.join(HERE, "..", "oracle"))
+import oracle  # noqa: E402
+
+_REF = oracle.reference_checkout()
+EXAMPLES = os.path.join(_REF, "input_data", "Example") if _REF else ""
 FIELDS = ("pos", "vel", "mass", "T", "P", "vdens", "U", "sfr", "type", "gp", "id")
 need_ref = pytest.mark.skipif(S.ref_lib() is None, reason="oracle/_ref not built (no reference checkout)")
 
