@@ -146,14 +146,21 @@ def cpu_step_time(d: dict, wl: dict, walk_fraction: int, threads: int, world=Non
     if (d["type"] == 2).any():
         world.gas_density(d.get("massInH", 0.0))
     t2 = time.perf_counter()
-    world.forces_subset(wl["e0"], wl["theta"], idx, threads)
+    if walk_fraction == 1:
+        world.forces(wl["e0"], wl["theta"], threads)
+    else:
+        world.forces_subset(wl["e0"], wl["theta"], idx, threads)
     t3 = time.perf_counter()
     world.ueuler(dt)
     world.kick(dt)
     t4 = time.perf_counter()
     scaled = (t1 - t0) + (t2 - t1) + (t3 - t2) * (n / idx.size) + (t4 - t3)
-    sample = (f"full build + SPH density + kick/drift over all {n} particles, walk for every "
-              f"{walk_fraction}th particle ({idx.size}) scaled by {n / idx.size:.1f}")
+    if walk_fraction == 1:
+        sample = (f"a full step over all {n} particles, timed in full: kick+drift, build, SPH density, walk, "
+                  f"Ueuler, kick")
+    else:
+        sample = (f"full build + SPH density + kick/drift over all {n} particles, walk for every "
+                  f"{walk_fraction}th particle ({idx.size}) scaled by {n / idx.size:.1f}")
     return scaled, world, sample
 
 
@@ -209,7 +216,8 @@ def reference_arm(args, wl, d):
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_block(args, wl, d, walk="fp64 recursive walk on host cores", split_threshold=100 * threads),
+        "config": config_block(args, wl, d),
+        "method": reference_method(threads),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -235,7 +243,9 @@ def needs_flush(n: int) -> bool:
     return n * BYTES_PER_PARTICLE < 4 * L2_BYTES
 
 
-def config_block(args, wl, d, walk=None, split_threshold=100):
+def config_block(args, wl, d):
+    """The workload (the same block in both arms: the reference arm runs the
+    same particles, parameters and step)."""
     import numpy as np
 
     n = int(len(d["mass"]))
@@ -244,8 +254,27 @@ def config_block(args, wl, d, walk=None, split_threshold=100):
     extra = {"instances": int(len(d["first"]) - 1)} if "first" in d else {}
     return {"workload": f"{args.workload}: {wl['desc']}", "particles": n, **extra,
             "gas_particles": int(np.sum(d["type"] == 2)), "theta": wl["theta"], "eps": wl["e0"], "dt": wl["dt"],
-            "G": 1.0, "walk": walk or args.precision, "split_threshold": split_threshold, "parallelism": "replicas",
-            "l2": l2}
+            "G": 1.0, "step": "kick+drift, octree build, SPH density, walk with SPH force, Ueuler, kick; "
+                              "every particle active", "parallelism": "replicas", "l2": l2}
+
+
+TOPOLOGY_NOTE = ("Node::insert switches to serial insertion below threads*100 particles (Node.cpp:420). The octree "
+                 "does not depend on that threshold: node count, per-node membership and depth are the same at 100 "
+                 "and at 1600 (checked on the restatement at 1, 8 and 16 threads against the reference's own "
+                 "fixtures). Only the childParticles duplicates at the nodes where the build turns serial move, "
+                 "which changes rho of the gas whose density node is such a node.")
+
+
+def our_method(args):
+    return {"walk": "FP32-offset warp walk with compensated sums" if args.precision == "fp32" else "FP64 warp walk",
+            "split_threshold": 100, "threshold_rule": "the reference's deterministic one-thread setting (100)"}
+
+
+def reference_method(threads):
+    return {"walk": "FP64 recursive walk (Node::calculateGravityForce restated), one host thread per particle group",
+            "split_threshold": 100 * threads,
+            "threshold_rule": f"the reference's own rule on {threads} host threads (threads*100)",
+            "topology_note": TOPOLOGY_NOTE}
 
 
 # ---------------------------------------------------------------------------
@@ -508,6 +537,55 @@ def our_arm(args, wl, d):
                        "fp32_vs_fp64_walk_median": float(np.median(ep)),
                        "fp32_vs_fp64_walk_p999": float(np.quantile(ep, 0.999))}
 
+    # the opening-angle sweep of the precision form: force errors of both walks
+    # at the state above (the same tree and direct sum), then each angle timed
+    theta_sweep = None
+    thetas = [float(t) for t in args.thetas.split(",") if t] if args.thetas else []
+    if thetas and force_error is not None:
+        theta_sweep = []
+        for th in thetas:
+            row = {"theta": th}
+            ctx.set(theta=th, precision="fp32")
+            ctx.forces()
+            s32 = ctx.download("acc")
+            g32, sph32 = ctx.interactions()
+            ctx.set(precision="fp64")
+            ctx.forces()
+            s64 = ctx.download("acc")
+            nrm = np.maximum(np.linalg.norm(direct, axis=1), 1e-300)
+            e32 = np.linalg.norm(s32[ids] - direct, axis=1) / nrm
+            e64 = np.linalg.norm(s64[ids] - direct, axis=1) / nrm
+            ep = np.linalg.norm(s32 - s64, axis=1) / np.maximum(np.linalg.norm(s64, axis=1), 1e-300)
+            row["force_error"] = {"samples": int(ids.size), "median": float(np.median(e32)),
+                                  "p99": float(np.quantile(e32, 0.99)), "fp64_walk_median": float(np.median(e64)),
+                                  "fp64_walk_p99": float(np.quantile(e64, 0.99)),
+                                  "fp32_vs_fp64_walk_median": float(np.median(ep)),
+                                  "fp32_vs_fp64_walk_p999": float(np.quantile(ep, 0.999))}
+            row["interactions_per_step"] = {"gravity": g32, "sph": sph32}
+            theta_sweep.append(row)
+        for row in theta_sweep:
+            th = row["theta"]
+            ctx.set(theta=th, precision=args.precision)
+            for _ in range(2):
+                step()
+            q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            q0.record(stream)
+            for _ in range(args.sweep_steps):
+                step()
+            q1.record(stream)
+            torch.cuda.synchronize()
+            t32 = q0.elapsed_time(q1) / 1e3 / args.sweep_steps
+            ctx.set(precision="fp64")
+            q0.record(stream)
+            for _ in range(args.plain_steps):
+                step()
+            q1.record(stream)
+            torch.cuda.synchronize()
+            t64 = q0.elapsed_time(q1) / 1e3 / max(1, args.plain_steps)
+            row.update({"value": n / t32, "ms_per_step": t32 * 1e3, "steps": args.sweep_steps,
+                        "plain_fp64": n / t64, "plain_ms_per_step": t64 * 1e3, "speedup_vs_plain": t64 / t32})
+        ctx.set(theta=wl["theta"], precision=args.precision)
+
     # end to end through the C-ABI with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
@@ -557,8 +635,8 @@ def our_arm(args, wl, d):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": D.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tmax / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
-            "data": "synthetic", "config": config_block(args, wl, d), "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks,
+            "data": "synthetic", "config": config_block(args, wl, d), "method": our_method(args), "e2e": e2e,
+            "gpu_launches": launches, "clocks": clocks,
             "walk_variant": variant,
             "roofline": {"bound": "fp32", "kernel": "k_walk32" if args.precision == "fp32" else "k_walk64",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
@@ -576,6 +654,8 @@ def our_arm(args, wl, d):
             "plain_fp64": {"value": plain, "unit": UNIT, "steps": args.plain_steps} if plain else None,
             "speedup_vs_plain": value / plain if plain else None,
             "force_error": force_error,
+            "accuracy_bar": ACCURACY_NOTE,
+            "theta_sweep": theta_sweep,
             "energy_drift": drift,
             "step_graph": graph,
             "io": io,
@@ -583,10 +663,16 @@ def our_arm(args, wl, d):
         if per_launch:
             out["one_sim_per_launch"] = per_launch
             out["speedup_vs_plain_per_launch"] = value / per_launch["fp64"]["value"]
-        print(json.dumps(out), flush=True)
+    else:
+        out = None
     ctx.close()
-    finalize(D)
+    return out, D
 
+
+ACCURACY_NOTE = ("The <= 1e-4 median force-error bar applies to the FP32-offset walk against the FP64 walk at the same "
+                 "opening angle (force_error.fp32_vs_fp64_walk_median). Against FP64 direct summation both walks "
+                 "carry the reference's monopole-tree error at that angle (force_error.median / fp64_walk_median; "
+                 "per angle in theta_sweep).")
 
 SERVE_BUDGET_BYTES = 150e9
 SERVE_BYTES_PER_PARTICLE = 2 * BYTES_PER_PARTICLE  # the step context and the initial-force context
@@ -611,18 +697,35 @@ def _fcfs(arrivals, service):
     return lat, end
 
 
-def serving_arm(args, wl):
-    """Continuous batching of a Poisson request stream (one line; value = the
-    aggregate particle-steps/s at the highest arrival rate)."""
+def _serve_rate(eng, specs, rate, seed):
+    """One real-time pass of the request trace at `rate` requests/s."""
+    import numpy as np
+
+    import serving
+
+    arr = ics.poisson_arrivals(len(specs), rate, seed=seed)
+    trace = _serve_trace(specs, arr)
+    ps0, st0 = eng.particle_steps, eng.steps_done
+    t0 = time.perf_counter()
+    res = serving.serve(eng, trace, realtime=True)
+    span = time.perf_counter() - t0
+    lat = np.array([r.completed - r.arrival for r in res])
+    wait = np.array([r.admitted - r.arrival for r in res])
+    return {"rate_per_s": rate, "requests": len(res), "p50_latency_s": float(np.quantile(lat, 0.5)),
+            "p99_latency_s": float(np.quantile(lat, 0.99)), "max_latency_s": float(lat.max()),
+            "p99_admission_wait_s": float(np.quantile(wait, 0.99)), "makespan_s": span,
+            "particle_steps_per_s": (eng.particle_steps - ps0) / span, "engine_steps": eng.steps_done - st0}
+
+
+def serving_leg(args, wl):
+    """Continuous batching of a Poisson request stream (config: serving), and
+    the same requests served one at a time on the plain FP64 path."""
     import numpy as np
     import torch
 
     import ag2
     import serving
-    from dist import finalize, init
 
-    D = init()
-    torch.cuda.set_device(D.local_rank)
     specs = ics.serving_requests(args.serve_requests)
     sizes = np.array([len(q["mass"]) for q in specs])
     steps = np.array([q["steps"] for q in specs])
@@ -630,60 +733,55 @@ def serving_arm(args, wl):
     cap = int(min(budget_particles, sizes.sum()))
     stream = torch.cuda.Stream()
     eng = serving.Engine(cap, e0=wl["e0"], theta=wl["theta"], dt=wl["dt"], stream=stream)
-    # warm-up: two short simulations through the whole loop
-    warm = _serve_trace(specs[:2], [0.0, 0.0])
+    warm = _serve_trace(specs[:2], [0.0, 0.0])  # warm-up: two short simulations through the whole loop
     for q in warm:
         q.steps = 3
     serving.serve(eng, warm, realtime=False)
-    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
-    clk = ClockSampler(int(vis) if vis.isdigit() else D.local_rank)
-    time.sleep(0.5)
     l0 = eng.ctx.launches() + eng.init_ctx.launches()
     rates = [float(r) for r in args.serve_rates.split(",")]
-    per_rate = []
-    clk.mark_start()
-    for rate in rates:
-        arr = ics.poisson_arrivals(len(specs), rate, seed=8 + int(rate))
-        trace = _serve_trace(specs, arr)
-        ps0, st0 = eng.particle_steps, eng.steps_done
-        t0 = time.perf_counter()
-        res = serving.serve(eng, trace, realtime=True)
-        span = time.perf_counter() - t0
-        lat = np.array([r.completed - r.arrival for r in res])
-        per_rate.append({"rate_per_s": rate, "requests": len(res), "p50_latency_s": float(np.quantile(lat, 0.5)),
-                         "p99_latency_s": float(np.quantile(lat, 0.99)), "makespan_s": span,
-                         "particle_steps_per_s": (eng.particle_steps - ps0) / span,
-                         "engine_steps": eng.steps_done - st0})
-    clk.mark_stop()
-    clocks = clk.stop()
+    per_rate = [_serve_rate(eng, specs, rate, 8 + int(rate)) for rate in rates]
     launches = eng.ctx.launches() + eng.init_ctx.launches() - l0
     eng.close()
 
-    # each request alone on the plain FP64 path: per-step time measured on every
-    # 4th request (3 timed steps after its initial forces), fitted as a + b*N,
-    # then a first-come-first-served single server over the same arrivals
-    sample = list(range(0, len(specs), 4))
-    ms = []
-    for k in sample:
-        q = specs[k]
+    # the same trace at the highest rate under a budget that binds: requests
+    # wait for resident ones to finish before they are admitted
+    bound = None
+    if args.serve_small_budget_gb > 0:
+        small = int(max(args.serve_small_budget_gb * 1e9 // SERVE_BYTES_PER_PARTICLE, sizes.max()))
+        eng = serving.Engine(small, e0=wl["e0"], theta=wl["theta"], dt=wl["dt"], stream=stream)
+        serving.serve(eng, _serve_trace(specs[:1], [0.0]), realtime=False)
+        bound = _serve_rate(eng, specs, max(rates), 8 + int(max(rates)))
+        bound.update({"budget_gb": args.serve_small_budget_gb, "capacity_particles": small,
+                      "offered_particles": int(sizes.sum())})
+        eng.close()
+
+    # each request alone on the plain FP64 path, measured request by request:
+    # its initial forces (wall clock) and 2 steps after a warm-up step (CUDA
+    # events); its service time is the initial forces plus its step count
+    # times the measured step
+    service, per_step = [], []
+    for q in specs:
         c = ag2.Context(len(q["mass"]), e0=wl["e0"], theta=wl["theta"], massInH=q["massInH"], precision="fp64")
         c.set_stream(stream.cuda_stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         c.upload(q["pos"], q["mass"], q["type"], vel=q["vel"], U=q["U"])
         c.build_tree()
         c.sph_density()
         c.forces()
+        torch.cuda.synchronize()
+        t_init = time.perf_counter() - t0
         c.step(wl["dt"])
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(3):
+        for _ in range(2):
             c.step(wl["dt"])
         e1.record(stream)
         torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1) / 3)
+        per = e0.elapsed_time(e1) / 2 / 1e3
+        per_step.append(per)
+        service.append(t_init + q["steps"] * per)
         c.close()
-    A = np.stack([np.ones(len(sample)), sizes[sample]], axis=1)
-    coef, *_ = np.linalg.lstsq(A, np.array(ms) / 1e3, rcond=None)
-    service = steps * (coef[0] + coef[1] * sizes)
     plain = []
     for rate in rates:
         arr = ics.poisson_arrivals(len(specs), rate, seed=8 + int(rate))
@@ -692,31 +790,146 @@ def serving_arm(args, wl):
                       "p99_latency_s": float(np.quantile(lat, 0.99)),
                       "particle_steps_per_s": float((sizes * steps).sum() / end)})
     top = per_rate[-1]
-    n_h2d = int(sum(len(q["mass"]) * (24 + 24 + 8 + 8 + 1) for q in specs))
-    n_d2h = int(sum(len(q["mass"]) * (24 + 24 + 24 + 8 + 8) for q in specs))
+    return {
+        "workload": f"serving: {wl['desc']}", "requests": len(specs), "particles": int(sizes.sum()),
+        "particle_steps": int((sizes * steps).sum()),
+        "gas_requests": int(sum((q["type"] == 2).any() for q in specs)), "theta": wl["theta"], "eps": wl["e0"],
+        "dt": wl["dt"], "capacity_particles": cap, "budget_particles": budget_particles,
+        "rates": per_rate, "budget_bound": bound, "gpu_launches": launches,
+        "plain_alone": {"how": "each request alone in its own context on the FP64 path, one at a time in arrival "
+                               "order: initial forces and 2 steps measured per request, service time = initial + "
+                               "steps x measured step", "requests_measured": len(specs),
+                        "median_step_ms": float(np.median(per_step) * 1e3), "rates": plain},
+        "speedup_vs_plain_alone": top["particle_steps_per_s"] / plain[-1]["particle_steps_per_s"],
+        "p99_speedup_vs_plain_alone": plain[-1]["p99_latency_s"] / top["p99_latency_s"],
+    }
+
+
+def serving_arm(args, wl):
+    """--workload serving: the serving leg as its own line (value = the
+    aggregate particle-steps/s at the highest arrival rate)."""
+    import torch
+
+    from dist import finalize, init
+
+    D = init()
+    torch.cuda.set_device(D.local_rank)
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+    clk = ClockSampler(int(vis) if vis.isdigit() else D.local_rank)
+    time.sleep(0.5)
+    clk.mark_start()
+    sv = serving_leg(args, wl)
+    clk.mark_stop()
+    clocks = clk.stop()
+    top = sv["rates"][-1]
+    specs_bytes = sv["particles"]
     if D.rank == 0:
         out = {
             "metric": METRIC, "value": top["particle_steps_per_s"], "unit": UNIT, "n_gpus": D.world,
-            "steps": int(top["engine_steps"]), "warmup": 1, "ms_per_step": top["makespan_s"] / top["engine_steps"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"serving: {wl['desc']}", "requests": len(specs), "particles": int(sizes.sum()),
-                       "gas_requests": int(sum((q["type"] == 2).any() for q in specs)), "theta": wl["theta"],
-                       "eps": wl["e0"], "dt": wl["dt"], "capacity_particles": cap,
-                       "budget_particles": budget_particles, "parallelism": "replicas",
+            "steps": int(top["engine_steps"]), "warmup": 1,
+            "ms_per_step": top["makespan_s"] / top["engine_steps"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": sv["workload"], "requests": sv["requests"], "particles": sv["particles"],
+                       "theta": wl["theta"], "eps": wl["e0"], "dt": wl["dt"], "parallelism": "replicas",
                        "l2": "resident state far above the 129 MB L2 at the higher rates; no flush"},
             "e2e": {"value": top["particle_steps_per_s"], "unit": UNIT,
-                    "h2d_bytes_per_step": n_h2d / max(1, sum(r["engine_steps"] for r in per_rate)) * len(rates),
-                    "d2h_bytes_per_step": n_d2h / max(1, sum(r["engine_steps"] for r in per_rate)) * len(rates),
+                    "h2d_bytes_per_step": specs_bytes * 65 / max(1, top["engine_steps"]),
+                    "d2h_bytes_per_step": specs_bytes * 88 / max(1, top["engine_steps"]),
                     "note": "requests arrive as host arrays and results return to the host; latencies are wall clock"},
-            "gpu_launches": launches, "clocks": clocks, "roofline": None,
-            "serving": per_rate,
-            "plain_alone": {"model": f"FP64 path, one request at a time in arrival order; per-step time "
-                                     f"{coef[0] * 1e3:.3f} ms + {coef[1] * 1e9:.3f} ns x N fitted on {len(sample)} "
-                                     f"requests", "rates": plain},
-            "speedup_vs_plain_alone": top["particle_steps_per_s"] / plain[-1]["particle_steps_per_s"],
+            "gpu_launches": sv["gpu_launches"], "clocks": clocks, "roofline": None, "serving": sv,
         }
         print(json.dumps(out), flush=True)
     finalize(D)
+
+
+def ensemble_leg(args):
+    """The batched form: 512 independent Plummer spheres in one context (one
+    build and one walk launch per step over all of them), against the same
+    simulations stepped one per launch with the plain FP64 walk and the FP32
+    walk."""
+    import numpy as np
+    import torch
+
+    import ag2
+
+    wl = WORKLOADS["ensemble512"]
+    d = wl["make"]()
+    n = len(d["mass"])
+    dt = wl["dt"]
+    stream = torch.cuda.Stream()
+    ctx = ag2.Context(n, e0=wl["e0"], theta=wl["theta"], precision="fp32")
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    ctx.set_instances(d["first"])
+    ctx.build_tree()
+    ctx.forces()
+    tune = ctx.autotune()
+    for _ in range(3):
+        ctx.step(dt)
+    torch.cuda.synchronize()
+    l0 = ctx.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.ens_steps):
+        ctx.step(dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / args.ens_steps
+    launches = (ctx.launches() - l0) / args.ens_steps
+    ctx.step_graphs(True)
+    for _ in range(3):
+        ctx.step(dt)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.ens_steps):
+        ctx.step(dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    tg = e0.elapsed_time(e1) / 1e3 / args.ens_steps
+    ctx.step_graphs(False)
+    # accuracy of both walks against FP64 direct summation, same state
+    rng = np.random.default_rng(4096)
+    ids = np.sort(rng.choice(n, size=min(4096, n), replace=False))
+    ctx.build_tree()
+    ctx.forces()
+    a32 = ctx.download("acc")
+    direct = ctx.direct_sum(ids)
+    ctx.set(precision="fp64")
+    ctx.forces()
+    a64 = ctx.download("acc")
+    ctx.set(precision="fp32")
+    nrm = np.maximum(np.linalg.norm(direct, axis=1), 1e-300)
+    e32 = np.linalg.norm(a32[ids] - direct, axis=1) / nrm
+    e64 = np.linalg.norm(a64[ids] - direct, axis=1) / nrm
+    ep = np.linalg.norm(a32 - a64, axis=1) / np.maximum(np.linalg.norm(a64, axis=1), 1e-300)
+    # end to end through the C-ABI with pinned host buffers and the instance layout
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    hpos, hvel, hmass, hU, htype, hacc = (pin(ctx.download("pos")), pin(ctx.download("vel")), pin(d["mass"]),
+                                          pin(ctx.download("U")), pin(d["type"]), pin(a32))
+    outs = {"pos": hpos, "vel": hvel, "acc": hacc, "U": hU}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs, first=d["first"])
+    te = (time.perf_counter() - t0) / 3
+    ctx.close()
+    per_launch = one_sim_per_launch(d, wl, args.plain_steps, stream)
+    value = n / t
+    return {
+        "workload": f"ensemble512: {wl['desc']}", "particles": n, "instances": int(len(d["first"]) - 1),
+        "theta": wl["theta"], "eps": wl["e0"], "dt": dt, "value": value, "unit": UNIT, "ms_per_step": t * 1e3,
+        "steps": args.ens_steps, "gpu_launches_per_step": launches, "walk_tuning": tune,
+        "step_graph": {"value": n / tg, "ms_per_step": tg * 1e3},
+        "e2e": {"value": n / te, "unit": UNIT, "h2d_bytes_per_step": int(n * 89), "d2h_bytes_per_step": int(n * 80)},
+        "one_sim_per_launch": per_launch,
+        "speedup_vs_plain_per_launch": value / per_launch["fp64"]["value"],
+        "speedup_vs_fp32_per_launch": value / per_launch["fp32"]["value"],
+        "force_error": {"against": "FP64 direct summation within each simulation", "samples": int(ids.size),
+                        "median": float(np.median(e32)), "p99": float(np.quantile(e32, 0.99)),
+                        "fp64_walk_median": float(np.median(e64)),
+                        "fp32_vs_fp64_walk_median": float(np.median(ep)),
+                        "fp32_vs_fp64_walk_p999": float(np.quantile(ep, 0.999))},
+    }
 
 
 def serving_reference_arm(args, wl):
@@ -810,14 +1023,21 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--error-samples", type=int, default=65536)
-    ap.add_argument("--cpu-walk-fraction", type=int, default=8)
-    ap.add_argument("--ref-walk-fraction", type=int, default=32)
+    ap.add_argument("--cpu-walk-fraction", type=int, default=1)
+    ap.add_argument("--ref-walk-fraction", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--graph-steps", type=int, default=10)
     ap.add_argument("--io-reps", type=int, default=3)
-    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rates", default="10,50,200")
+    ap.add_argument("--serve-small-budget-gb", type=float, default=8.0,
+                    help="budget of the extra serving pass at the highest rate where admission waits (0: skip)")
+    ap.add_argument("--thetas", default="0.4,0.5,0.7", help="opening angles of the precision-form sweep")
+    ap.add_argument("--sweep-steps", type=int, default=5)
+    ap.add_argument("--ens-steps", type=int, default=10)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="the merger line without the ensemble and serving summaries")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -831,8 +1051,18 @@ def main():
     d = wl["make"]()
     if args.impl == "reference":
         reference_arm(args, wl, d)
-    else:
-        our_arm(args, wl, d)
+        return
+    out, D = our_arm(args, wl, d)
+    del d
+    # the metric's other two parts, on one GPU: the batched ensemble and serving
+    if args.workload == "merger4m" and not args.no_extra and D.world == 1:
+        out["ensemble512"] = ensemble_leg(args)
+        out["serving"] = serving_leg(args, WORKLOADS["serving"])
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    from dist import finalize
+
+    finalize(D)
 
 
 if __name__ == "__main__":

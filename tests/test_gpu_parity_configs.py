@@ -1,0 +1,179 @@
+"""CUDA path against the C restatement of the reference (pinned bit-exactly to
+the reference's own outputs by tests/test_oracle_golden.py) at the sizes the
+benchmark runs, not only at fixture sizes:
+
+* the isolated disk galaxy of 1,048,576 particles (786,432 halo, 196,608
+  stars, 65,536 gas; e0 = 0.02, massInH = 64 m_gas, theta = 0.5), every
+  particle;
+* the galaxy merger scaled to 262,144 particles at theta = 0.4, 0.5 and 0.7
+  (Node.cpp:331-334: the opening test changes the walk, not the tree), every
+  particle;
+* the 4,194,304-particle merger itself at theta = 0.5: full topology, root
+  half-width, h and rho, and the walk on 65,536 seeded particles;
+* the 512-sphere ensemble: every 16th simulation against the restatement run
+  on that simulation alone.
+
+Tolerances (as tests/test_gpu_parity.py): node count, per-node depth / leaf
+flag / leaf particle / childParticles count and membership hash / centre /
+half-width, Particle::node, the root half-width and h bit-exact; rho relative
+1e-12; acc FP64 walk relative 1e-11 per particle (node moments are summed
+bottom-up, not as the reference's running mean: 1e-12 relative); FP32 walk
+median <= 1e-5 and 99.9th percentile <= 1e-3 relative (the accuracy
+contract).  The measured figures are printed (pytest -s).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import ics
+import oracle
+
+pytestmark = pytest.mark.gpu
+THREADS = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import build
+
+    build.build()
+    if not oracle.available("port"):
+        build.build_checkers()
+
+
+def rel_err(a, b):
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+def port_tree(d, massInH):
+    w = oracle.World(d["pos"], d["mass"], d["type"], d.get("vel"), d.get("U"), kind="port")
+    w.build(1)
+    if massInH:
+        w.gas_density(massInH)
+    return w
+
+
+def check_tree(c, w, massInH, label):
+    nn = c.node_count()[0]
+    assert nn == w.node_count(), (label, nn, w.node_count())
+    assert c.root_radius() == w.root_radius(), label
+    t, ref = c.topology(), w.topology()
+    for k in ("depth", "is_leaf", "particle", "cp_count", "cp_hash", "center", "radius"):
+        assert np.array_equal(t[k], ref[k]), (label, k)
+    np.testing.assert_array_equal(c.particle_node(), w.leaf_index())
+    del t, ref
+    if massInH:
+        c.sph_density()
+        np.testing.assert_array_equal(c.download("h"), w.get("h"))
+        np.testing.assert_allclose(c.download("rho"), w.get("rho"), rtol=1e-12, atol=0)
+    return nn
+
+
+def check_forces(c, ref_acc, idx, precision, label):
+    c.forces()
+    acc = c.download("acc")
+    e = rel_err(acc[idx], ref_acc[idx])
+    med, p999, mx = float(np.median(e)), float(np.quantile(e, 0.999)), float(e.max())
+    print(f"\n{label} {precision}: {idx.size} particles, rel err median {med:.2e} p99.9 {p999:.2e} max {mx:.2e}")
+    if precision == "fp64":
+        assert mx <= 1e-11, (label, mx)
+    else:
+        assert med <= 1e-5 and p999 <= 1e-3, (label, med, p999)
+
+
+def ctx_for(d, e0, theta, massInH, precision):
+    import ag2
+
+    c = ag2.Context(len(d["mass"]), e0=e0, theta=theta, massInH=massInH, split_threshold=100, precision=precision)
+    c.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    return c
+
+
+def test_disk1m_against_port():
+    """The plain-method configuration: a 1,048,576-particle disk galaxy."""
+    d = ics.disk_galaxy(seed=2)
+    e0, theta, mih = 0.02, 0.5, d["massInH"]
+    w = port_tree(d, mih)
+    w.forces(e0, theta, THREADS)
+    ref_acc = w.get("acc")
+    idx = np.arange(len(d["mass"]))
+    for precision in ("fp64", "fp32"):
+        c = ctx_for(d, e0, theta, mih, precision)
+        c.build_tree()
+        nn = check_tree(c, w, mih, "disk1m")
+        check_forces(c, ref_acc, idx, precision, f"disk1m ({nn} nodes)")
+        c.close()
+
+
+@pytest.mark.parametrize("theta", [0.4, 0.5, 0.7])
+def test_merger262k_theta_sweep_against_port(theta):
+    """The precision form's opening angles on the merger, scaled to 262,144."""
+    d = ics.merger(131072, seed=3)
+    e0, mih = 0.02, d["massInH"]
+    w = port_tree(d, mih)
+    w.forces(e0, theta, THREADS)
+    ref_acc = w.get("acc")
+    idx = np.arange(len(d["mass"]))
+    for precision in ("fp64", "fp32"):
+        c = ctx_for(d, e0, theta, mih, precision)
+        c.build_tree()
+        check_tree(c, w, mih, f"merger262k theta {theta}")
+        check_forces(c, ref_acc, idx, precision, f"merger262k theta {theta}")
+        c.close()
+
+
+def test_merger4m_against_port():
+    """The benchmark's own 4,194,304-particle merger at theta = 0.5: the whole
+    tree, h and rho bit for bit, and the walk on 65,536 seeded particles."""
+    d = ics.merger(2097152, seed=3)
+    e0, theta, mih = 0.02, 0.5, d["massInH"]
+    w = port_tree(d, mih)
+    rng = np.random.default_rng(65536)
+    idx = np.sort(rng.choice(len(d["mass"]), size=65536, replace=False)).astype(np.int32)
+    w.forces_subset(e0, theta, idx, THREADS)
+    ref_acc = w.get("acc")
+    for precision in ("fp64", "fp32"):
+        c = ctx_for(d, e0, theta, mih, precision)
+        c.build_tree()
+        if precision == "fp64":
+            check_tree(c, w, mih, "merger4m")
+        else:
+            c.sph_density()
+        check_forces(c, ref_acc, idx, precision, "merger4m")
+        c.close()
+
+
+def test_ensemble_instances_against_port():
+    """The 512-simulation ensemble in one context: every 16th simulation
+    against the restatement run on that simulation alone."""
+    import ag2
+
+    d = ics.ensemble(512)
+    first = d["first"]
+    e0, theta = 0.01, 0.5
+    c = ag2.Context(len(d["mass"]), e0=e0, theta=theta, split_threshold=100, precision="fp64")
+    c.upload(d["pos"], d["mass"], d["type"], vel=d["vel"], U=d["U"])
+    c.set_instances(first)
+    c.build_tree()
+    c.forces()
+    a64 = c.download("acc")
+    c.set(precision="fp32")
+    c.forces()
+    a32 = c.download("acc")
+    worst64, e32 = 0.0, []
+    for k in range(0, len(first) - 1, 16):
+        a, b = int(first[k]), int(first[k + 1])
+        w = oracle.World(d["pos"][a:b], d["mass"][a:b], d["type"][a:b], d["vel"][a:b], d["U"][a:b], kind="port")
+        w.build(1)
+        w.forces(e0, theta, THREADS)
+        r = rel_err(a64[a:b], w.get("acc"))
+        worst64 = max(worst64, float(r.max()))
+        assert r.max() <= 1e-11, (k, r.max())
+        e32.append(rel_err(a32[a:b], w.get("acc")))
+        assert c.instance_radius(k) == w.root_radius(), k
+    e = np.concatenate(e32)
+    print(f"\nensemble: 32 of 512 simulations ({e.size} particles), FP64 max {worst64:.2e}, "
+          f"FP32 median {np.median(e):.2e} p99.9 {np.quantile(e, 0.999):.2e}")
+    assert np.median(e) <= 1e-5 and np.quantile(e, 0.999) <= 1e-3
+    c.close()
