@@ -37,7 +37,7 @@ EXPORTS = [
     "ag2_phase_times", "ag2_set_instances", "ag2_instance_radius", "ag2_energy", "ag2_step_graphs",
     "ag2_block_init", "ag2_block_step", "ag2_set_tags", "ag2_get_tags", "ag2_snapshot_size",
     "ag2_snapshot_encode", "ag2_snapshot_write", "ag2_snapshot_wait", "ag2_ic_count", "ag2_load_ics",
-    "ag2_inject_fault",
+    "ag2_inject_fault", "ag2_autotune_walk", "ag2_set_walk_variant",
 ]
 
 # file formats of ag2_snapshot_* / ag2_load_ics (the reference's format names)
@@ -48,6 +48,12 @@ class Params(ctypes.Structure):
     _fields_ = [("G", ctypes.c_double), ("e0", ctypes.c_double), ("theta", ctypes.c_double),
                 ("massInH", ctypes.c_double), ("split_threshold", ctypes.c_int32),
                 ("precision", ctypes.c_int32), ("group_size", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class WalkConfig(ctypes.Structure):
+    """ag2_walk_config (include/ag2.h)."""
+    _fields_ = [("variant", ctypes.c_int32), ("regs", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("stack", ctypes.c_int32), ("group_size", ctypes.c_int32), ("ms", ctypes.c_float)]
 
 
 class AG2Error(RuntimeError):
@@ -126,6 +132,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.ag2_ic_count.argtypes = [ctypes.c_char_p, I, ctypes.POINTER(ctypes.c_int64)]
     L.ag2_load_ics.argtypes = [P, ctypes.c_char_p, I, P]
     L.ag2_inject_fault.argtypes = [P, I, I]
+    L.ag2_autotune_walk.argtypes = [P, I, P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.ag2_set_walk_variant.argtypes = [P, I]
     _lib = L
     return L
 
@@ -396,7 +404,28 @@ class Context:
     def autotune(self) -> int:
         v = ctypes.c_int()
         self._check(self.L.ag2_autotune(self.h, ctypes.byref(v)))
+        self.params.group_size = self._get_params().group_size
         return v.value
+
+    def autotune_walk(self) -> dict:
+        """ag2_autotune_walk: every candidate (variant, register budget, blocks
+        per SM, first-pass stack, group size) with its walk time on the current
+        tree, and the one kept."""
+        out = (WalkConfig * 16)()
+        cnt, chosen = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.ag2_autotune_walk(self.h, 16, out, ctypes.byref(cnt), ctypes.byref(chosen)))
+        self.params.group_size = self._get_params().group_size
+        cands = [{"variant": c.variant, "regs": c.regs, "blocks_per_sm": c.blocks_per_sm, "stack": c.stack,
+                  "group_size": c.group_size, "ms": c.ms} for c in out[:min(cnt.value, 16)]]
+        return {"candidates": cands, "chosen": cands[chosen.value] if 0 <= chosen.value < len(cands) else None}
+
+    def set_walk_variant(self, variant: int):
+        self._check(self.L.ag2_set_walk_variant(self.h, variant))
+
+    def _get_params(self) -> "Params":
+        p = Params()
+        self._check(self.L.ag2_get_params(self.h, ctypes.byref(p)))
+        return p
 
     def launches(self) -> int:
         return int(self.L.ag2_launch_count(self.h))

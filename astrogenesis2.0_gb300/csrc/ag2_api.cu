@@ -216,7 +216,7 @@ void free_nodes(Nodes &d)
 bool valid_params(const ag2_params *p)
 {
     return p && p->split_threshold >= 1 && (p->precision == AG2_PREC_FP64 || p->precision == AG2_PREC_FP32) &&
-           p->theta > 0.0;
+           p->theta > 0.0 && p->group_size >= 0 && p->group_size <= 32;
 }
 
 __global__ void k_pinst(const int64_t *first, int32_t *pinst)
@@ -234,6 +234,34 @@ bool realloc_dev(T *&p, size_t n)
 }
 
 }  // namespace
+
+// particles per walk group (0 reads as 32)
+int group_size_of(const ag2_params &p) { return p.group_size > 0 ? p.group_size : 32; }
+
+// Walk groups of the current instance layout: runs of group_size consecutive
+// slots that never straddle two instances.  They depend on the layout and the
+// group size only, so a new table is valid for the tree already built.
+int build_groups(Ctx *c)
+{
+    const int gs = group_size_of(c->prm);
+    std::vector<int4> g;
+    for (int k = 0; k < c->n_inst; k++) {
+        const int64_t b = c->inst_first_h[k], e = c->inst_first_h[k + 1];
+        for (int64_t s = b; s < e; s += gs) g.push_back(make_int4((int)s, (int)std::min<int64_t>(gs, e - s), k, 0));
+    }
+    if (g.size() > c->groups_cap) {
+        if (!realloc_dev(c->groups, g.size()) || !realloc_dev(c->retry_groups, g.size()))
+            return set_err(c, AG2_E_NOMEM, "group table allocation failed");
+        c->groups_cap = g.size();
+    }
+    if (!g.empty())
+        AG2_CUDA(c, cudaMemcpyAsync(c->groups, g.data(), g.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));  // g goes out of scope
+    c->ngroups = (int32_t)g.size();
+    c->groups_gs = gs;
+    return AG2_OK;
+}
+
 
 int upload_common(Ctx *c, size_t n, const double *pos, const double *vel, const double *mass, const double *U,
                   const uint8_t *type)
@@ -285,6 +313,10 @@ int ensure_instance_tables(Ctx *c)
     AG2_CUDA(c, cudaMemcpyAsync(c->inst_massInH, c->inst_massInH_h.data(), K * sizeof(double), cudaMemcpyHostToDevice,
                                 c->stream));
     if (c->inst_first_h == c->inst_tab_first) {  // same layout (an upload of the same particles): tables stand
+        if (c->groups_gs != group_size_of(c->prm)) {
+            int rc = build_groups(c);
+            if (rc) return rc;
+        }
         c->inst_dirty = false;
         c->gas_stats_dirty = true;
         return AG2_OK;
@@ -342,19 +374,10 @@ int ensure_instance_tables(Ctx *c)
                                     c->stream));
         AG2_CUDA(c, cudaStreamSynchronize(c->stream));
     }
-    std::vector<int4> g;
-    for (int k = 0; k < K; k++) {
-        const int64_t b = c->inst_first_h[k], e = c->inst_first_h[k + 1];
-        for (int64_t s = b; s < e; s += 32) g.push_back(make_int4((int)s, (int)std::min<int64_t>(32, e - s), k, 0));
+    {
+        int rc = build_groups(c);
+        if (rc) return rc;
     }
-    if (g.size() > c->groups_cap) {
-        if (!realloc_dev(c->groups, g.size()) || !realloc_dev(c->retry_groups, g.size()))
-            return set_err(c, AG2_E_NOMEM, "group table allocation failed");
-        c->groups_cap = g.size();
-    }
-    if (!g.empty())
-        AG2_CUDA(c, cudaMemcpyAsync(c->groups, g.data(), g.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
-    c->ngroups = (int32_t)g.size();
     if (c->n) AG2_LAUNCH(c, k_pinst, K, 256, 0, c->inst_first, c->pinst);
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));  // host vectors above go out of scope
     c->inst_tab_first = c->inst_first_h;
@@ -472,8 +495,17 @@ int ag2_set_params(ag2_ctx *c, const ag2_params *p)
 {
     if (!c || !valid_params(p)) return set_err(c, AG2_E_INVALID, "invalid parameters");
     bool retree = p->split_threshold != c->prm.split_threshold;
+    const bool regroup = group_size_of(*p) != group_size_of(c->prm);
     c->prm = *p;
     if (retree) c->have_tree = false;
+    if (regroup) {
+        // the groups depend on the layout and the group size only: a built
+        // layout gets its new table now (valid for the tree already built)
+        if (!c->inst_dirty && !c->inst_tab_first.empty()) {
+            int rc = build_groups(c);
+            if (rc) return rc;
+        }
+    }
     if (c->n_inst == 1 && !c->inst_explicit) c->inst_massInH_h = {p->massInH};
     c->graph_epoch++;
     return AG2_OK;
@@ -696,7 +728,7 @@ static unsigned long long step_key(Ctx *c, double dt, double hubble, int with_vi
                           c->groups, c->inst_first, c->pkey};
     h = fnv(h, ptrs, sizeof(ptrs));
     const int64_t sizes[] = {(int64_t)c->n, c->n_inst, (int64_t)c->node_cap, (int64_t)c->hist_cap, c->ngas,
-                             c->walk_variant, c->ngroups, with_visual, c->graph_epoch};
+                             c->walk_variant, c->ngroups, c->groups_gs, with_visual, c->graph_epoch};
     h = fnv(h, sizes, sizeof(sizes));
     h = fnv(h, &c->prm, sizeof(c->prm));
     const double d[] = {dt, hubble, Rv};
@@ -1010,6 +1042,28 @@ int ag2_autotune(ag2_ctx *c, int *variant)
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
     int rc = run_autotune(c, variant);
     if (rc) return rc;
+    return check_walk(c);
+}
+
+int ag2_set_walk_variant(ag2_ctx *c, int variant)
+{
+    if (!c || variant < 0 || variant >= kWalkVariantCount) return AG2_E_INVALID;
+    c->walk_variant = variant;
+    c->graph_epoch++;
+    return AG2_OK;
+}
+
+int ag2_autotune_walk(ag2_ctx *c, int max, ag2_walk_config *out, int *count, int *chosen)
+{
+    if (!c || !chosen || max < 0 || (max > 0 && !out)) return AG2_E_INVALID;
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->err_code, 0, sizeof(int32_t), c->stream));
+    int variant = 0, k = 0;
+    int rc = run_autotune(c, &variant, out, max, &k);
+    if (rc) return rc;
+    if (count) *count = k;
+    *chosen = -1;
+    for (int j = 0; j < std::min(k, max); j++)
+        if (out[j].variant == variant && out[j].group_size == c->prm.group_size) *chosen = j;
     return check_walk(c);
 }
 

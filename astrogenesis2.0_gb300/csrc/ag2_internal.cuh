@@ -223,6 +223,7 @@ struct Ctx {
     int4 *groups = nullptr;         // device walk groups: (first slot, lanes, instance, 0)
     int32_t *retry_groups = nullptr; // device, groups_cap: groups for the FP32 walk's retry pass
     int32_t ngroups = 0;
+    int32_t groups_gs = 0;           // group size the table was built for
     size_t groups_cap = 0;
     bool inst_dirty = true;         // instance tables need uploading
     bool inst_explicit = false;     // layout from ag2_set_instances (keeps its massInH)
@@ -396,6 +397,8 @@ inline bool launch_ok(const dim3 &g) { return g.x > 0 && g.y > 0 && g.z > 0; }
 // entry points implemented per translation unit
 int build_tree(Ctx *c);
 int ensure_instance_tables(Ctx *c);
+int build_groups(Ctx *c);
+int group_size_of(const ag2_params &p);
 int build_tree_captured(Ctx *c);
 void build_tree_finish_captured(Ctx *c);
 int prepare_captured_build(Ctx *c);
@@ -417,7 +420,8 @@ int run_block_step(Ctx *c, double H0, int with_visual, double Rv, double *t_out,
 int run_fma_probe(Ctx *c, double *gflops);
 int io_reset_tags(Ctx *c, size_t n);
 void io_release(Ctx *c);
-int run_autotune(Ctx *c, int *chosen);
+constexpr int kWalkVariantCount = 4;  // FP32 walk variants (ag2_walk.cu kVariants)
+int run_autotune(Ctx *c, int *chosen, ag2_walk_config *out = nullptr, int max_out = 0, int *count = nullptr);
 
 // physical constants of the reference (Constants.h:14-15, Particle.h:40)
 constexpr double kGamma = 5.0 / 3.0;

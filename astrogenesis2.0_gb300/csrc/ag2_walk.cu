@@ -41,7 +41,20 @@ constexpr int kStack = 512;      // stack entries per warp (FP64 walk, potential
 // retry list and is walked again by a second launch with the full stack.
 constexpr int kStackFast = 256;
 constexpr float kGuard = 1e-5f;
-constexpr int kWalkVariants = 3;
+// FP32 walk variants the autotuner chooses among: the register budget (through
+// the resident 4-warp blocks per SM it is built for; 1 = the compiler's
+// choice) and the first pass's stack depth, which sets the shared memory per
+// block.  Together they set how many warps an SM holds: 16 (compiler, ~120
+// registers), 24 (80 registers, 256 entries), 28 (72 registers, 128 entries),
+// 32 (64 registers, 64 entries; 8 blocks of ~27 KB).  A shallower stack sends
+// more groups to the retry pass; the deepest stack on the bench workloads is
+// under 50 entries.  Results do not depend on the variant.
+struct WalkVariant {
+    int min_blocks, stack, regs;
+};
+constexpr WalkVariant kVariants[] = {{1, 256, 0}, {6, 256, 80}, {7, 128, 72}, {8, 64, 64}};
+constexpr int kWalkVariants = kWalkVariantCount;
+static_assert(sizeof(kVariants) / sizeof(kVariants[0]) == kWalkVariants, "variant table");
 
 struct WalkArgs {
     int n;
@@ -378,10 +391,14 @@ struct alignas(16) WarpSmemT {
     unsigned cself[kBatch];     // lane whose own leaf this child is (bit), else 0
     unsigned bkeep[kBatch];     // lanes that evaluate batch slot j, less the one whose own leaf it is
     unsigned char mq[kBatch];   // batch slot of the q-th child the lanes decide one by one
-    float4 mpos[kBatch];        // ... its cpos, cthr and lane mask, in that order (no indirection in the loop)
-    float4 mthr[kBatch];
-    unsigned mkeep[kBatch];
-    float4 lpos[kList];      // accepted nodes: relative com, mass
+    // ... its centre and thresholds, two children per three float4 so that the
+    // decision loop reads packed pairs: (x0 x1 y0 y1) (z0 z1 acc0 acc1)
+    // (open-above0 open-above1 open-below0 open-below1), children 2p and 2p+1
+    float4 mpair[3 * kBatch / 2];
+    unsigned mkeep[kBatch];     // ... and the lanes that decide it
+    // accepted nodes, two entries per two float4: (x0 x1 y0 y1) (z0 z1 w0 w1)
+    // for entries 2p and 2p+1 (relative com, G m ls^2)
+    float4 lpair[kList];
     unsigned lmask[kList];   // lanes that accepted them
     double xd[3][32];        // FP64 positions of the group (read only by the exact re-check)
     int2 stk[kStk];          // (first child of a node to open, lane mask)
@@ -403,30 +420,57 @@ __device__ __forceinline__ unsigned transpose32(unsigned x, int lane)
     return x;
 }
 
+// Interaction-list entry q: its node's relative centre of mass and G m ls^2
+// into the pair layout, and the lanes that take it.
+template <class WS>
+__device__ __forceinline__ void put_entry(WS &W, int q, float4 P, unsigned lanes)
+{
+    float *L = reinterpret_cast<float *>(W.lpair) + 8 * (q >> 1) + (q & 1);
+    L[0] = P.x;
+    L[2] = P.y;
+    L[4] = P.z;
+    L[6] = P.w;
+    W.lmask[q] = lanes;
+}
+template <class WS>
+__device__ __forceinline__ float4 get_entry(const WS &W, int q)
+{
+    const float *L = reinterpret_cast<const float *>(W.lpair) + 8 * (q >> 1) + (q & 1);
+    return make_float4(L[0], L[2], L[4], L[6]);
+}
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
 // Force loop over the interaction list: every lane evaluates every entry and
-// keeps it when its bit is set (predicated, no branches), summing into a batch
-// that is added to the compensated accumulator once per flush.  With kOneRsq
-// the factor 1 / (r (r^2 + e^2)) is one reciprocal square root of
+// keeps it when its bit is set, summing into a batch that is added to the
+// compensated accumulator once per flush.  Entries go two at a time through
+// packed FP32 instructions (fma/add/mul.rn.f32x2, IEEE rounding per element):
+// entry 2p in the low and 2p+1 in the high half of every pair, so the low and
+// high halves of the batch sums hold the even and the odd entries, added
+// together at the end of the flush.  An entry a lane does not take gets the
+// factor 0 (a select), which leaves the sums unchanged.  With kOneRsq the
+// factor 1 / (r (r^2 + e^2)) is one reciprocal square root of
 // r^2 (r^2 + e^2)^2 instead of a reciprocal square root and a reciprocal; the
 // caller takes it when e0^2 (scaled) exceeds 3e-9, where every distance the
 // list holds (r^2 above 1e-12 e0^2, smaller ones go to the FP64 path) keeps
-// that product above 1e-12 e0^6 > 2.7e-37, inside FP32's normal range.
+// that product above 1e-12 e0^6 > 2.7e-37, inside FP32's normal range.  The
+// general softening law decides per lane in FP64 and keeps the scalar loop.
 template <bool kGeneral, bool kOneRsq = false, class WS>
-__device__ __forceinline__ void flush_list(const WS &W, int cnt, int lane, float ox, float oy, float oz,
+__device__ __forceinline__ void flush_list(WS &W, int cnt, int lane, float ox, float oy, float oz,
                                            float eps02, double e0, double ls, float &sx, float &sy, float &sz,
                                            float &kx, float &ky, float &kz, unsigned long long &cnt_g)
 {
     float bx = 0.f, by = 0.f, bz = 0.f;
-    int mine = 0;
-#pragma unroll 4
-    for (int j = 0; j < cnt; j++) {
-        const float4 P = W.lpos[j];
-        bool take = (W.lmask[j] >> lane) & 1u;
-        const float dx = P.x - ox, dy = P.y - oy, dz = P.z - oz;
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float ir = rsqrtf(r2);
-        float e2 = eps02;
-        if (kGeneral) {
+    if (kGeneral) {
+        int mine = 0;
+#pragma unroll 1
+        for (int j = 0; j < cnt; j++) {
+            const float4 P = get_entry(W, j);
+            bool take = (W.lmask[j] >> lane) & 1u;
+            const float dx = P.x - ox, dy = P.y - oy, dz = P.z - oz;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float ir = rsqrtf(r2);
+            float e2 = eps02;
             // the general law decides on the distance in the caller's units
             double de2 = 0.0;
             if (take) {
@@ -436,30 +480,53 @@ __device__ __forceinline__ void flush_list(const WS &W, int cnt, int lane, float
                     take = false;  // the reference returns without a force (Node.cpp:285-305)
             }
             mine += take ? 1 : 0;
+            const float sc = __fdividef(P.w * ir, r2 + e2);
+            if (take) {
+                bx = fmaf(dx, sc, bx);
+                by = fmaf(dy, sc, by);
+                bz = fmaf(dz, sc, bz);
+            }
         }
-        // P.w = G m ls^2: the sum comes out in the caller's units
-        float sc;
-        if (kOneRsq && !kGeneral) {
-            const float t = r2 + e2;
-            sc = P.w * rsqrtf(r2 * t * t);
-        } else {
-            sc = __fdividef(P.w * ir, r2 + e2);
+        cnt_g += (unsigned long long)mine;
+    } else {
+        if (cnt & 1) {  // an odd list ends with a pair whose high entry no lane takes
+            if (lane == 0) put_entry(W, cnt, make_float4(0.f, 0.f, 0.f, 0.f), 0u);
+            __syncwarp();
         }
-        if (take) {  // predicated accumulation
-            bx = fmaf(dx, sc, bx);
-            by = fmaf(dy, sc, by);
-            bz = fmaf(dz, sc, bz);
+        const float2 nox = f2(-ox, -ox), noy = f2(-oy, -oy), noz = f2(-oz, -oz), e2 = f2(eps02, eps02);
+        float2 px = f2(0.f, 0.f), py = f2(0.f, 0.f), pz = f2(0.f, 0.f);
+        const int np = (cnt + 1) >> 1;
+#pragma unroll 2
+        for (int p = 0; p < np; p++) {
+            const float4 A = W.lpair[2 * p], B = W.lpair[2 * p + 1];
+            const uint2 M = reinterpret_cast<const uint2 *>(W.lmask)[p];
+            const float2 dx = __fadd2_rn(f2(A.x, A.y), nox), dy = __fadd2_rn(f2(A.z, A.w), noy),
+                         dz = __fadd2_rn(f2(B.x, B.y), noz);
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            const float2 t = __fadd2_rn(r2, e2);
+            float2 sc;
+            if (kOneRsq) {
+                const float2 q = __fmul2_rn(__fmul2_rn(r2, t), t);
+                sc = __fmul2_rn(f2(B.z, B.w), f2(rsqrtf(q.x), rsqrtf(q.y)));
+            } else {
+                const float2 num = __fmul2_rn(f2(B.z, B.w), f2(rsqrtf(r2.x), rsqrtf(r2.y)));
+                sc = f2(__fdividef(num.x, t.x), __fdividef(num.y, t.y));
+            }
+            sc.x = ((M.x >> lane) & 1u) ? sc.x : 0.f;
+            sc.y = ((M.y >> lane) & 1u) ? sc.y : 0.f;
+            px = __ffma2_rn(dx, sc, px);
+            py = __ffma2_rn(dy, sc, py);
+            pz = __ffma2_rn(dz, sc, pz);
         }
+        bx = px.x + px.y;
+        by = py.x + py.y;
+        bz = pz.x + pz.y;
+        // every set mask bit is one interaction: count them lane-parallel
+        for (int j = lane; j < cnt; j += 32) cnt_g += (unsigned long long)__popc(W.lmask[j]);
     }
     kahan_add(sx, kx, bx);
     kahan_add(sy, ky, by);
     kahan_add(sz, kz, bz);
-    if (kGeneral) {
-        cnt_g += (unsigned long long)mine;
-    } else {
-        // every set mask bit is one interaction: count them lane-parallel
-        for (int j = lane; j < cnt; j += 32) cnt_g += (unsigned long long)__popc(W.lmask[j]);
-    }
 }
 
 // Rare path of the FP32 walk: an opening test within the guard band of the
@@ -489,12 +556,12 @@ __device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, co
     return decision;
 }
 
-// kRetry: the second pass over the groups the first one could not hold in its
-// stack (a.retry_groups, ctl->retry_count of them), with the full stack.
-template <bool kGeneral, bool kGas, int kMinBlocks, bool kRetry = false>
+// kStk = kStack: the second pass over the groups the first one could not hold
+// in its stack (a.retry_groups, ctl->retry_count of them), with the full stack.
+template <bool kGeneral, bool kGas, int kMinBlocks, int kStk>
 __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
 {
-    constexpr int kStk = kRetry ? kStack : kStackFast;
+    constexpr bool kRetry = kStk == kStack;
     using WS = WarpSmemT<kStk>;
     __shared__ WS sm_all[kWalkBlock / 32];
     const int lane = threadIdx.x & 31;
@@ -726,11 +793,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                     }
                     sp += __popc(om);
                 }
-                if (acc) {
-                    const int q = nl + __popc(am & below);
-                    W.lpos[q] = W.cpos[j];
-                    W.lmask[q] = keep;
-                }
+                if (acc) put_entry(W, nl + __popc(am & below), W.cpos[j], keep);
                 nl += __popc(am);
             }
             __syncwarp();
@@ -739,30 +802,46 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
             // lanes that accept / open that child, and the entries are placed at once
             if (mixed) {
                 const unsigned below = (1u << lane) - 1u;
+                const int nm = __popc(mixed);
                 if ((mixed >> lane) & 1u) {
                     const int q = __popc(mixed & below);
                     W.mq[q] = (unsigned char)lane;
-                    W.mpos[q] = W.cpos[lane];
-                    W.mthr[q] = W.cthr[lane];
+                    const float4 P = W.cpos[lane], T = W.cthr[lane];
+                    float *M = reinterpret_cast<float *>(W.mpair) + 12 * (q >> 1) + (q & 1);
+                    M[0] = P.x;
+                    M[2] = P.y;
+                    M[4] = P.z;
+                    M[6] = T.w;
+                    M[8] = T.y;
+                    M[10] = T.z;
                     W.mkeep[q] = W.bkeep[lane];
                 }
+                if (lane == 0 && (nm & 1)) W.mkeep[nm] = 0u;  // the high half of the last pair: no lane
                 __syncwarp();
-                const int nm = __popc(mixed);
                 unsigned accb = 0u, opnb = 0u, sphb = 0u, rqb = 0u;
-#pragma unroll 4
-                for (int q = 0; q < nm; q++) {
-                    const unsigned bit = 1u << q;
-                    // the lanes that evaluate this child, except the one whose own leaf it is
-                    if ((W.mkeep[q] >> lane) & 1u) {
-                        const float4 Pc = W.mpos[q];
-                        const float4 T = W.mthr[q];
-                        const float dx = Pc.x - ox, dy = Pc.y - oy, dz = Pc.z - oz;
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        const bool acc = r2 > T.w, opn = r2 > T.y && r2 < T.z;
-                        if (acc) accb |= bit;
-                        if (opn) opnb |= bit;
-                        if (!(acc || opn)) rqb |= bit;
-                        if (kGas && gas_i && acc && r2 < h2x4) sphb |= bit;
+                {
+                    // two children per iteration: r^2 of both in packed FP32 (the
+                    // same roundings per element as fmaf(dx, dx, fmaf(dy, dy, dz*dz))),
+                    // then each child's tests for the lanes that decide it (all
+                    // but the one whose own leaf it is)
+                    const float2 nox = f2(-ox, -ox), noy = f2(-oy, -oy), noz = f2(-oz, -oz);
+                    const int npair = (nm + 1) >> 1;
+#pragma unroll 2
+                    for (int p = 0; p < npair; p++) {
+                        const float4 A = W.mpair[3 * p], B = W.mpair[3 * p + 1], T = W.mpair[3 * p + 2];
+                        const uint2 K = reinterpret_cast<const uint2 *>(W.mkeep)[p];
+                        const float2 dx = __fadd2_rn(f2(A.x, A.y), nox), dy = __fadd2_rn(f2(A.z, A.w), noy),
+                                     dz = __fadd2_rn(f2(B.x, B.y), noz);
+                        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                        const bool k0 = (K.x >> lane) & 1u, k1 = (K.y >> lane) & 1u;
+                        const bool a0 = k0 && r2.x > B.z, a1 = k1 && r2.y > B.w;
+                        const bool o0 = k0 && r2.x > T.x && r2.x < T.z, o1 = k1 && r2.y > T.y && r2.y < T.w;
+                        const unsigned b0 = 1u << (2 * p), b1 = b0 << 1;
+                        accb |= (a0 ? b0 : 0u) | (a1 ? b1 : 0u);
+                        opnb |= (o0 ? b0 : 0u) | (o1 ? b1 : 0u);
+                        rqb |= (k0 && !(a0 || o0) ? b0 : 0u) | (k1 && !(a1 || o1) ? b1 : 0u);
+                        if (kGas && gas_i)
+                            sphb |= (a0 && r2.x < h2x4 ? b0 : 0u) | (a1 && r2.y < h2x4 ? b1 : 0u);
                     }
                 }
                 // the rare tests decided in FP64 (near zero distance, or the guard band)
@@ -860,11 +939,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                 const int jq = lane < nm ? (int)W.mq[lane] : 0;
                 const bool ha = lane < nm && accb != 0u, ho = lane < nm && opnb != 0u;
                 const unsigned hab = __ballot_sync(0xffffffffu, ha), hob = __ballot_sync(0xffffffffu, ho);
-                if (ha) {
-                    const int p = nl + __popc(hab & below);
-                    W.lpos[p] = W.cpos[jq];
-                    W.lmask[p] = accb;
-                }
+                if (ha) put_entry(W, nl + __popc(hab & below), W.cpos[jq], accb);
                 nl += __popc(hab);
                 const int nop = __popc(hob);
                 if (sp + nop > kStk) {
@@ -1134,15 +1209,16 @@ int run_forces(Ctx *c)
             if (gas) WALK((k_walk64<false, true>)); else WALK((k_walk64<false, false>));
         }
     } else {
-        // register budget variant (autotuned): 0 = compiler's choice, 1 = 80, 2 = 64
+        // the autotuned variant (kVariants: register budget and first-pass stack)
         const int v = c->walk_variant;
 #define W32(G, S)                                                                 \
     do {                                                                          \
-        if (v == 1) WALK((k_walk32<G, S, 6>));                                    \
-        else if (v == 2) WALK((k_walk32<G, S, 8>));                               \
-        else WALK((k_walk32<G, S, 1>));                                           \
+        if (v == 1) WALK((k_walk32<G, S, 6, 256>));                               \
+        else if (v == 2) WALK((k_walk32<G, S, 7, 128>));                          \
+        else if (v == 3) WALK((k_walk32<G, S, 8, 64>));                           \
+        else WALK((k_walk32<G, S, 1, 256>));                                      \
         /* groups whose stack outgrew the first pass (none in the usual case) */  \
-        AG2_LAUNCH(c, (k_walk32<G, S, 1, true>), dev_sms, kWalkBlock, 0, a);      \
+        AG2_LAUNCH(c, (k_walk32<G, S, 1, kStack>), dev_sms, kWalkBlock, 0, a);    \
     } while (0)
         if (general) {
             if (gas) W32(true, true); else W32(true, false);
@@ -1155,38 +1231,65 @@ int run_forces(Ctx *c)
     return AG2_OK;
 }
 
-int run_autotune(Ctx *c, int *chosen)
+// Walk time of each candidate (variant x group size) on the current tree,
+// keeping the fastest.  The group size changes the groups' centres and hence
+// the FP32 sums in their last bits (within the accuracy contract); the variant
+// changes nothing in the results.
+int run_autotune(Ctx *c, int *chosen, ag2_walk_config *out, int max_out, int *count)
 {
+    if (count) *count = 0;
     if (!c->have_tree) return set_err(c, AG2_E_INVALID, "ag2_autotune needs a tree (call ag2_build_tree)");
     if (c->prm.precision != AG2_PREC_FP32 || c->n == 0) {
         *chosen = c->walk_variant;
         return AG2_OK;
     }
+    static const int kGroupSizes[] = {32, 16};
     cudaEvent_t e0, e1;
     AG2_CUDA(c, cudaEventCreate(&e0));
     AG2_CUDA(c, cudaEventCreate(&e1));
+    const int gs0 = c->prm.group_size;
     float best = 1e30f;
-    int best_v = 0;
-    for (int v = 0; v < kWalkVariants; v++) {
-        c->walk_variant = v;
-        float ms = 0;
-        for (int rep = 0; rep < 2; rep++) {  // first run warms caches
-            AG2_CUDA(c, cudaEventRecord(e0, c->stream));
-            int rc = run_forces(c);
-            if (rc) return rc;
-            AG2_CUDA(c, cudaEventRecord(e1, c->stream));
-            AG2_CUDA(c, cudaEventSynchronize(e1));
-            cudaEventElapsedTime(&ms, e0, e1);
+    int best_v = 0, best_gs = 32, k = 0;
+    int rc = AG2_OK;
+    for (int gs : kGroupSizes) {
+        c->prm.group_size = gs;
+        if ((rc = build_groups(c))) break;
+        for (int v = 0; v < kWalkVariants && !rc; v++) {
+            c->walk_variant = v;
+            float ms = 0;
+            for (int rep = 0; rep < 2 && !rc; rep++) {  // the first run warms caches
+                cudaEventRecord(e0, c->stream);
+                if ((rc = run_forces(c))) break;
+                cudaEventRecord(e1, c->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess) rc = set_err(c, AG2_E_CUDA, "autotune timing failed");
+                cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (rc) break;
+            if (out && k < max_out)
+                out[k] = ag2_walk_config{v, kVariants[v].regs, kVariants[v].min_blocks > 1 ? kVariants[v].min_blocks : 0,
+                                         kVariants[v].stack, gs, ms};
+            k++;
+            if (ms < best) {
+                best = ms;
+                best_v = v;
+                best_gs = gs;
+            }
         }
-        if (ms < best) {
-            best = ms;
-            best_v = v;
-        }
+        if (rc) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (rc) {
+        c->prm.group_size = gs0;
+        build_groups(c);
+        return rc;
+    }
     c->walk_variant = best_v;
+    c->prm.group_size = best_gs;
+    if ((rc = build_groups(c))) return rc;
+    c->graph_epoch++;
     *chosen = best_v;
+    if (count) *count = k;
     return AG2_OK;
 }
 

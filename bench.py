@@ -389,7 +389,7 @@ def our_arm(args, wl, d):
     ctx.build_tree()
     ctx.sph_density()
     ctx.forces()
-    variant = ctx.autotune() if args.precision == "fp32" else None
+    tuning = ctx.autotune_walk() if args.precision == "fp32" else None
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
     clk = ClockSampler(int(vis) if vis.isdigit() else D.local_rank)
 
@@ -621,12 +621,20 @@ def our_arm(args, wl, d):
             tcpu, _, sample = cpu_step_time(d, wl, args.cpu_walk_fraction, threads)
         cpu = {"value": n / tcpu, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
 
-    traffic = None
+    # DRAM bytes of one walk launch, from the committed ncu summary; it states
+    # the walk source it was measured on, so a changed kernel shows as stale
+    traffic, traffic_src = None, None
     tpath = os.path.join(REPO, "profiles", "walk_traffic.json")
     if os.path.exists(tpath):
         try:
+            import hashlib
+
             tj = json.load(open(tpath))
             traffic = tj.get(args.workload, {}).get(args.precision)
+            cur = hashlib.sha256(open(os.path.join(REPO, "astrogenesis2.0_gb300", "csrc", "ag2_walk.cu"),
+                                      "rb").read()).hexdigest()[:16]
+            traffic_src = {"file": "profiles/walk_traffic.json", "walk_source_sha": tj.get("walk_source_sha"),
+                           "current_walk_source_sha": cur, "current": tj.get("walk_source_sha") == cur}
         except (OSError, ValueError):
             traffic = None
 
@@ -637,10 +645,11 @@ def our_arm(args, wl, d):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic", "config": config_block(args, wl, d), "method": our_method(args), "e2e": e2e,
             "gpu_launches": launches, "clocks": clocks,
-            "walk_variant": variant,
+            "walk_tuning": tuning,
             "roofline": {"bound": "fp32", "kernel": "k_walk32" if args.precision == "fp32" else "k_walk64",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_source": "measured FP32 FMA throughput (ag2_fp32_peak_probe, "
+                         "traffic": traffic, "traffic_source": traffic_src,
+                         "peak_source": "measured FP32 FMA throughput (ag2_fp32_peak_probe, "
                                                             "this run)", "walk_ms": walk_avg_s * 1e3,
                          "flop_per_launch": flop_per_walk},
             "roofline_build": {"bound": "hbm", "kernel": "octree build (every build kernel, one step)",
@@ -863,7 +872,7 @@ def ensemble_leg(args):
     ctx.set_instances(d["first"])
     ctx.build_tree()
     ctx.forces()
-    tune = ctx.autotune()
+    tune = ctx.autotune_walk()
     for _ in range(3):
         ctx.step(dt)
     torch.cuda.synchronize()

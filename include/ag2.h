@@ -81,7 +81,8 @@ typedef struct ag2_params {
                                 many particles; the reference uses
                                 omp_get_max_threads()*100 (Node.cpp:420) */
     int32_t precision;    /* enum ag2_precision */
-    int32_t group_size;   /* particles per walk group (32; reserved for tuning) */
+    int32_t group_size;   /* particles per FP32/FP64 walk group, 1..32 (0 = 32); ag2_autotune_walk
+                             may change it */
     int32_t reserved;
 } ag2_params;
 
@@ -204,10 +205,30 @@ int ag2_step_graphs(ag2_ctx *ctx, int enable);
 int ag2_block_init(ag2_ctx *ctx, double eta, double min_dt, double max_dt, double global_time);
 int ag2_block_step(ag2_ctx *ctx, double H0, int with_visual, double Rv, double *global_time, int64_t *active);
 
-/* Time the FP32 walk's compiled variants (register budget per thread, hence
- * warps resident per SM) on the current tree and keep the fastest for later
- * ag2_forces calls of this context; *variant receives its index. */
+/* Walk autotuner.  Times each FP32-walk candidate on the current tree and
+ * keeps the fastest for later ag2_forces calls of this context.  A candidate
+ * is a compiled variant (register budget per thread and first-pass stack
+ * depth, which together set the warps resident per SM) with a walk group size
+ * (particles per warp group: 32 or 16).  The chosen group size is written to
+ * the context's params.group_size.  Variant and stack depth do not change the
+ * results; the group size changes the FP32 sums in their last bits, within
+ * the walk's accuracy contract.  ag2_autotune returns the chosen variant;
+ * ag2_autotune_walk also reports every candidate with its time (up to max
+ * entries; *count = candidates timed, *chosen = index of the choice). */
+typedef struct ag2_walk_config {
+    int32_t variant;        /* compiled variant of the FP32 walk */
+    int32_t regs;           /* register budget per thread (0 = the compiler's choice) */
+    int32_t blocks_per_sm;  /* resident 4-warp blocks per SM the budget is built for (0 = compiler) */
+    int32_t stack;          /* first-pass stack entries per warp (deeper groups go to a retry pass) */
+    int32_t group_size;     /* particles per walk group */
+    float ms;               /* measured walk time on the context's tree */
+} ag2_walk_config;
 int ag2_autotune(ag2_ctx *ctx, int *variant);
+int ag2_autotune_walk(ag2_ctx *ctx, int max, ag2_walk_config *out, int *count, int *chosen);
+/* Use FP32-walk variant `variant` (an ag2_walk_config.variant, 0..3) without
+ * timing anything, e.g. a choice kept from an earlier ag2_autotune_walk;
+ * the group size is params.group_size. */
+int ag2_set_walk_variant(ag2_ctx *ctx, int variant);
 
 /* Phase timers (CUDA events on the context's stream).  When enabled,
  * ag2_build_tree records its sub-phases and ag2_step records the phases the
