@@ -230,16 +230,21 @@ def _kick(vel, acc, ts, idx):
 
 
 def block_steps(world: World, type_, eta: float, dmin: float, dmax: float, e0: float, theta: float,
-                massInH: float, steps: int, t: float = 0.0, H0: float = 0.0, threads: int = 1):
+                massInH: float, steps: int, t: float = 0.0, H0: float = 0.0, threads: int = 1,
+                end_time: float | None = None):
     """`steps` iterations of the reference's block-time-step loop
     (Simulation.cpp:188-341) on the port, starting from the world's current acc
-    (after its initial forces).  Returns [(global time, particles integrated)]
-    and the final (step, next time) arrays."""
+    (after its initial forces); with `end_time`, iterations while the global
+    time is below it, as Simulation::run's `while (globalTime < endTime)`
+    (Simulation.cpp:210).  Returns [(global time, particles integrated)] and
+    the final (step, next time) arrays."""
     type_ = np.asarray(type_)
     ts = block_dt(world.get("acc"), eta, e0, dmin, dmax)
     tn = t + ts
     log = []
-    for _ in range(steps):
+    k = 0
+    while (t < end_time) if end_time is not None else (k < steps):
+        k += 1
         due = t >= tn
         if due.any():
             ts[due] = block_dt(world.get("acc")[due], eta, e0, dmin, dmax)

@@ -18,12 +18,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "Simulation.h"
 #include "Tree.h"
 #include "TimeIntegration.h"
 #include "DataManager.h"
+#include "Log.h"
 
 #include <unistd.h>
 
@@ -194,6 +196,50 @@ void orc_set(orc_world *w, int f, const double *in)
 }
 
 double orc_root_radius(orc_world *w) { return (w->tree && w->tree->root) ? w->tree->root->radius : 0.0; }
+
+// The reference's own step loop with block time steps: Simulation::run
+// (Simulation.cpp:166-364) on the world's particles, which must carry their
+// initial accelerations (orc_build + orc_forces, as Simulation::init computes
+// them before run).  run() starts at globalTime 0, gives every particle its
+// power-of-two step from |acc| (eta, min_dt, max_dt) and loops while
+// globalTime < end_time: renew due steps, advance to the earliest next time,
+// kick+drift, build, visual and gas density, walk, close (Ueuler, Hubble
+// factor, kick).  Snapshots are switched off (fixedStep beyond end_time) and
+// the phase log goes to logdir.  Inside run(), Tree::calculateForces sets the
+// OpenMP thread count to std::thread::hardware_concurrency() (Tree.cpp:59-60),
+// so every build after the first walk splits at 100 * that count; *cores
+// returns it.  Outputs: the final globalTime, and per particle its time step
+// and next integration time.
+int orc_ref_run(orc_world *w, const char *logdir, double eta, double min_dt, double max_dt, double end_time,
+                double e0, double theta, double massInH, double H0, double *global_time, double *tstep,
+                double *tnext, int *cores)
+{
+    Simulation *s = w->sim;
+    Log::setOutputDir(logdir);
+    s->eta = eta;
+    s->minTimeStep = min_dt;
+    s->maxTimeStep = max_dt;
+    s->endTime = end_time;
+    s->fixedStep = 1e300;
+    s->fixedTimeSteps = 1;
+    s->numParticlesOutput = 0;
+    s->e0 = e0;
+    s->theta = theta;
+    s->massInH = massInH;
+    s->H0 = H0;
+    s->starFormation = false;
+    s->coolingEnabled = false;
+    s->run();
+    delete w->tree;  // run() built and deleted its own trees; the world's old one is stale
+    w->tree = nullptr;
+    *global_time = s->globalTime;
+    for (size_t i = 0; i < s->particles.size(); i++) {
+        tstep[i] = s->particles[i]->timeStep;
+        tnext[i] = s->particles[i]->nextIntegrationTime;
+    }
+    *cores = (int)std::thread::hardware_concurrency();
+    return 0;
+}
 
 static int64_t count_nodes(const Node *n)
 {

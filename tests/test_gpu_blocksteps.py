@@ -64,3 +64,36 @@ def test_block_steps_with_equal_limits_match_plain_steps():
         b.step(dt)
     for f in ("pos", "vel", "acc", "U"):
         np.testing.assert_array_equal(a.download(f), b.download(f), err_msg=f)
+
+
+def test_block_steps_match_reference_run():
+    """Against the reference's own Simulation::run with block time steps
+    (tests/golden/blocksteps/plummer2k.npz): ag2_block_init from the same
+    initial accelerations, then ag2_block_step while the global time is below
+    endTime, with the serial-switch threshold run() used (100 * the cores of
+    the host that made the fixture).  The final global time and every
+    particle's step and next integration time are bit-exact; positions and
+    velocities agree to the FP64 walk's tolerance."""
+    import os
+
+    import ag2
+
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blocksteps", "plummer2k.npz"))
+    p = {k[2:]: float(z[k]) for k in z.files if k.startswith("p_")}
+    n = len(z["in_mass"])
+    c = ag2.Context(n, e0=p["e0"], theta=p["theta"], split_threshold=100 * int(z["cores"]), precision="fp64")
+    c.upload(z["in_pos"], z["in_mass"], z["in_type"], vel=z["in_vel"], U=z["in_U"])
+    c.set_field("acc", z["acc0"])
+    c.block_init(p["eta"], p["min_dt"], p["max_dt"], 0.0)
+    t, iters, partial = 0.0, 0, False
+    while t < p["end_time"]:
+        t, k = c.block_step()
+        iters += 1
+        partial |= k < n
+    assert t == float(z["global_time"]) and iters >= 4 and partial
+    np.testing.assert_array_equal(c.download("tstep"), z["tstep"])
+    np.testing.assert_array_equal(c.download("tnext"), z["tnext"])
+    scale = np.max(np.abs(z["pos"]))
+    np.testing.assert_allclose(c.download("pos"), z["pos"], rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(c.download("vel"), z["vel"], rtol=1e-9, atol=1e-12)
+    c.close()

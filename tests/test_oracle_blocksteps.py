@@ -57,3 +57,27 @@ def test_steps_are_powers_of_two_and_time_grows():
     assert len(set(ts)) > 1  # the steps really differ
     # everyone is due together only where the step sizes line up
     assert all(0 < k <= 800 for _, k in log) and any(k < 800 for _, k in log)
+
+
+def test_restatement_matches_the_reference_run():
+    """Against the reference's own Simulation::run with block time steps
+    (tests/golden/blocksteps/plummer2k.npz, made by make_blocksteps_golden.py):
+    the same final global time, the same step and next integration time per
+    particle (exact: powers of two), and the state to the FP64 tolerance of
+    node moments summed in another order (run() builds at 100 * its host's
+    cores per serial switch; the restatement builds with as many threads)."""
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blocksteps", "plummer2k.npz"))
+    p = {k[2:]: float(z[k]) for k in z.files if k.startswith("p_")}
+    w = oracle.World(z["in_pos"], z["in_mass"], z["in_type"], z["in_vel"], z["in_U"], kind="port")
+    w.set("acc", z["acc0"])
+    log, ts, tn = oracle.block_steps(w, z["in_type"], p["eta"], p["min_dt"], p["max_dt"], p["e0"], p["theta"], 0.0,
+                                     0, threads=int(z["cores"]), end_time=p["end_time"])
+    assert log[-1][0] == float(z["global_time"]) and len(log) >= 4
+    assert any(k < len(ts) for _, k in log)  # not every particle is due at every iteration
+    np.testing.assert_array_equal(ts, z["tstep"])
+    np.testing.assert_array_equal(tn, z["tnext"])
+    scale = np.max(np.abs(z["pos"]))
+    np.testing.assert_allclose(w.get("pos"), z["pos"], rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(w.get("vel"), z["vel"], rtol=1e-9, atol=1e-12)
