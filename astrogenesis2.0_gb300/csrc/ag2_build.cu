@@ -759,9 +759,8 @@ struct Sums {
             ng += 1;
         }
     }
-    __device__ void add_node(const Nodes &nd, int64_t c)
+    __device__ void add_sum(const NodeSum &t)
     {
-        const NodeSum t = nd.tsum[c];
         if (t.first_id < first_id) {
             first_id = t.first_id;
             first_m = t.first_m;
@@ -817,9 +816,12 @@ struct RecArgs {
     const double *inst_R;  // root half-width per instance (walk_scale)
 };
 
+// first_child and leafslot are the node's nd.first and nd.leafpos, which the
+// callers already hold (a leaf's first is -1; an internal node's leafpos is -1)
 __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particles &P, const Sums &tot, double mass,
                                            double cx, double cy, double cz, double gas, double mvx, double mvy,
-                                           double mvz, int32_t ng, uint8_t cmask, bool leaf, int32_t lp, RecArgs ra)
+                                           double mvz, int32_t ng, uint8_t cmask, bool leaf, int32_t lp,
+                                           int32_t first_child, int32_t leafslot, RecArgs ra)
 {
     NodeSum ts;
     ts.m = tot.m;
@@ -863,7 +865,7 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
         mac = q * q;
     }
     w.B = make_float4(lx, ly, lz, mac);
-    w.C = make_int4(nd.first[nid], nd.leafpos[nid], (int)cmask, 0);
+    w.C = make_int4(first_child, leafslot, (int)cmask, 0);
     if (leaf && lp >= 0)
         w.D = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)scale2(gas, 2 * k));
     else
@@ -958,7 +960,8 @@ __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Parti
                 cx = cy = cz = 0.0;
             }
         }
-        store_node(nd, nid, P, t, mp, cx, cy, cz, t.g, mvx, mvy, mvz, t.ng, 0, true, i, ra);
+        // one particle inside its bounds: it sits at the leaf's first slot (leafpos)
+        store_node(nd, nid, P, t, mp, cx, cy, cz, t.g, mvx, mvy, mvz, t.ng, 0, true, i, -1, i, ra);
         return;
     }
     Sums tot, own;  // tot: whole routed range; own: the reference's mass set
@@ -971,7 +974,8 @@ __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Parti
         for (int32_t k = 0; k < cnt - ndrop; k++) own.add_particle(P, idx(k));
     }
     double mass, cx, cy, cz, gas, mvx, mvy, mvz;
-    const bool has = nd.leafpos[nid] >= 0;
+    const int32_t lslot = nd.leafpos[nid];
+    const bool has = lslot >= 0;
     const int32_t lp = has ? idx(0) : -1;
     if (has) {
         const double mp = P.m[lp];
@@ -1008,7 +1012,7 @@ __device__ __forceinline__ void moments_leaf(Nodes &nd, int64_t nid, const Parti
     } else {
         finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
     }
-    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, 0, true, lp, ra);
+    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, 0, true, lp, -1, lslot, ra);
 }
 
 // Internal-node moments after its children's: sums over the children in octant
@@ -1019,7 +1023,7 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
                                                  const double *gas_prefix, const int32_t *gas_off,
                                                  const uint8_t *gas_uni, RecArgs ra)
 {
-    const int32_t cnt = nd.count[nid], ndrop = nd.ndrop[nid], first = nd.first[nid];
+    const int32_t ndrop = nd.ndrop[nid], first = nd.first[nid];
     const uint8_t mode = nd.mode[nid];
     Sums tot, own;
     own.zero();
@@ -1027,15 +1031,24 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
     for (int o = 0; o < 8; o++) {
         const int64_t c = first + o;
         if (nd.count[c] == 0) continue;
-        own.add_node(nd, c);
-        if ((dbits(nd.mom[c].mass) << 1) != 0) cmask |= (uint8_t)(1u << o);  // mass != 0, on the bits
+        const NodeSum t = nd.tsum[c];
+        own.add_sum(t);
+        // bit o: the child's own mass != 0 (on the bits).  Without an
+        // out-of-bounds tail that mass is its routed sum t.m, bit for bit (the
+        // same terms in the same order; a one-particle leaf's is the particle's
+        // mass); with one, it is the mass the child stored.
+        const double cm = nd.ndrop[c] ? nd.mom[c].mass : t.m;
+        if ((dbits(cm) << 1) != 0) cmask |= (uint8_t)(1u << o);
     }
     tot = own;
-    for (int32_t k = cnt - ndrop; k < cnt; k++) tot.add_particle(P, idx(k));
+    if (ndrop) {  // the node's own out-of-bounds tail ends its range
+        const int32_t cnt = nd.count[nid];
+        for (int32_t k = cnt - ndrop; k < cnt; k++) tot.add_particle(P, idx(k));
+    }
     if (mode == MODE_PAR) own = tot;  // the parallel path sums escapers too (Node.cpp:477-499)
     double mass, cx, cy, cz, gas, mvx, mvy, mvz;
     finish_sums(nd, nid, mode, own, gas_prefix, gas_off, gas_uni, mass, cx, cy, cz, gas, mvx, mvy, mvz);
-    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, ra);
+    store_node(nd, nid, P, tot, mass, cx, cy, cz, gas, mvx, mvy, mvz, own.ng, cmask, false, -1, first, -1, ra);
 }
 
 // Leaves (every level at once), on the state in tree order, one thread per
@@ -1050,7 +1063,9 @@ __global__ void __launch_bounds__(kBlock) k_moments_leaf(int n, const int32_t *_
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const int32_t v = pnode[s];
-        if (v < 0 || nd.first[v] >= 0 || nd.start[v] != s) continue;
+        // a leaf's slots all settled in it, so its first slot is the one whose
+        // left neighbour settled elsewhere (a coalesced read, not nd.start[v])
+        if (v < 0 || (s > 0 && pnode[s - 1] == v) || nd.first[v] >= 0) continue;
         moments_leaf(nd, v, P, [=](int32_t k) { return s + k; }, gas_prefix, gas_off, gas_uni, ra);
     }
 }
@@ -1071,8 +1086,8 @@ __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32
     }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt_lvl; t += gridDim.x * blockDim.x) {
         const int64_t nid = list[t];
-        const int32_t start = nd.start[nid];
-        moments_internal(nd, nid, P, [=](int32_t k) { return start + k; }, gas_prefix, gas_off, gas_uni, ra);
+        // the node's start is read only for an out-of-bounds tail
+        moments_internal(nd, nid, P, [=](int32_t k) { return nd.start[nid] + k; }, gas_prefix, gas_off, gas_uni, ra);
     }
 }
 

@@ -59,6 +59,7 @@ def port_tree(d, massInH):
 
 
 def check_tree(c, w, massInH, label):
+    """Returns the node count and both roots' (mass, centre of mass): GPU, restatement."""
     nn = c.node_count()[0]
     assert nn == w.node_count(), (label, nn, w.node_count())
     assert c.root_radius() == w.root_radius(), label
@@ -66,22 +67,23 @@ def check_tree(c, w, massInH, label):
     for k in ("depth", "is_leaf", "particle", "cp_count", "cp_hash", "center", "radius"):
         assert np.array_equal(t[k], ref[k]), (label, k)
     np.testing.assert_array_equal(c.particle_node(), w.leaf_index())
+    roots = ((t["mass"][0], t["com"][0].copy()), (ref["mass"][0], ref["com"][0].copy()))
     del t, ref
     if massInH:
         c.sph_density()
         np.testing.assert_array_equal(c.download("h"), w.get("h"))
         np.testing.assert_allclose(c.download("rho"), w.get("rho"), rtol=1e-12, atol=0)
-    return nn
+    return nn, roots
 
 
-def check_forces(c, ref_acc, idx, precision, label):
+def check_forces(c, ref_acc, idx, precision, label, fp64_bound=(1e-12, 1e-11, 5e-11)):
     c.forces()
     acc = c.download("acc")
     e = rel_err(acc[idx], ref_acc[idx])
     med, p999, mx = float(np.median(e)), float(np.quantile(e, 0.999)), float(e.max())
     print(f"\n{label} {precision}: {idx.size} particles, rel err median {med:.2e} p99.9 {p999:.2e} max {mx:.2e}")
     if precision == "fp64":
-        assert med <= 1e-12 and p999 <= 1e-11 and mx <= 5e-11, (label, med, p999, mx)
+        assert med <= fp64_bound[0] and p999 <= fp64_bound[1] and mx <= fp64_bound[2], (label, med, p999, mx)
     else:
         assert med <= 1e-5 and p999 <= 1e-3, (label, med, p999)
 
@@ -105,7 +107,7 @@ def test_disk1m_against_port():
     for precision in ("fp64", "fp32"):
         c = ctx_for(d, e0, theta, mih, precision)
         c.build_tree()
-        nn = check_tree(c, w, mih, "disk1m")
+        nn, _ = check_tree(c, w, mih, "disk1m")
         check_forces(c, ref_acc, idx, precision, f"disk1m ({nn} nodes)")
         c.close()
 
@@ -129,7 +131,20 @@ def test_merger262k_theta_sweep_against_port(theta):
 
 def test_merger4m_against_port():
     """The benchmark's own 4,194,304-particle merger at theta = 0.5: the whole
-    tree, h and rho bit for bit, and the walk on 65,536 seeded particles."""
+    tree, h and rho bit for bit, and the walk on 65,536 seeded particles.
+
+    The FP64 accelerations are held to median 1e-11, 99.9th percentile 1e-10
+    and max 1e-9.  At this size the reference's own node sums carry rounding
+    that grows with their lists: a parallel node adds its particles' masses and
+    mass-weighted positions one after another in list order (Node.cpp:465-506),
+    up to 4,194,304 terms here, where the GPU sums them as a tree.  The
+    restatement's root mass is off by 3.7e-11 relative (the GPU's by ~1e-16),
+    and a particle pulled mostly by the other galaxy feels that directly.  The
+    test measures it: both roots' mass and centre of mass against the exactly
+    rounded values (math.fsum of the masses and of the same rounded products
+    x*m), and the GPU's are the closer."""
+    import math
+
     d = ics.merger(2097152, seed=3)
     e0, theta, mih = 0.02, 0.5, d["massInH"]
     w = port_tree(d, mih)
@@ -141,10 +156,18 @@ def test_merger4m_against_port():
         c = ctx_for(d, e0, theta, mih, precision)
         c.build_tree()
         if precision == "fp64":
-            check_tree(c, w, mih, "merger4m")
+            _, ((gm, gc), (rm, rc)) = check_tree(c, w, mih, "merger4m")
+            m, x = d["mass"], d["pos"]
+            M = math.fsum(m)
+            exact = np.array([math.fsum(x[:, k] * m) / M for k in range(3)])
+            egm, erm = abs(gm - M) / M, abs(rm - M) / M
+            egc, erc = np.abs(gc - exact).max(), np.abs(rc - exact).max()
+            print(f"\nmerger4m root against exactly rounded sums: mass rel err GPU {egm:.2e} restatement {erm:.2e}; "
+                  f"centre of mass abs err GPU {egc:.2e} restatement {erc:.2e}")
+            assert egm <= erm and egm <= 1e-14 and egc <= erc
         else:
             c.sph_density()
-        check_forces(c, ref_acc, idx, precision, "merger4m")
+        check_forces(c, ref_acc, idx, precision, "merger4m", fp64_bound=(1e-11, 1e-10, 1e-9))
         c.close()
 
 
