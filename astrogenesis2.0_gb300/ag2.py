@@ -53,7 +53,8 @@ class Params(ctypes.Structure):
 class WalkConfig(ctypes.Structure):
     """ag2_walk_config (include/ag2.h)."""
     _fields_ = [("variant", ctypes.c_int32), ("regs", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("stack", ctypes.c_int32), ("group_size", ctypes.c_int32), ("ms", ctypes.c_float)]
+                ("stack", ctypes.c_int32), ("prefetch", ctypes.c_int32), ("group_size", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
 
 
 class AG2Error(RuntimeError):
@@ -416,7 +417,7 @@ class Context:
         self._check(self.L.ag2_autotune_walk(self.h, 16, out, ctypes.byref(cnt), ctypes.byref(chosen)))
         self.params.group_size = self._get_params().group_size
         cands = [{"variant": c.variant, "regs": c.regs, "blocks_per_sm": c.blocks_per_sm, "stack": c.stack,
-                  "group_size": c.group_size, "ms": c.ms} for c in out[:min(cnt.value, 16)]]
+                  "prefetch": c.prefetch, "group_size": c.group_size, "ms": c.ms} for c in out[:min(cnt.value, 16)]]
         return {"candidates": cands, "chosen": cands[chosen.value] if 0 <= chosen.value < len(cands) else None}
 
     def set_walk_variant(self, variant: int):

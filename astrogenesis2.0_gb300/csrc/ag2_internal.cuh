@@ -420,7 +420,7 @@ int run_block_step(Ctx *c, double H0, int with_visual, double Rv, double *t_out,
 int run_fma_probe(Ctx *c, double *gflops);
 int io_reset_tags(Ctx *c, size_t n);
 void io_release(Ctx *c);
-constexpr int kWalkVariantCount = 4;  // FP32 walk variants (ag2_walk.cu kVariants)
+constexpr int kWalkVariantCount = 6;  // FP32 walk variants (ag2_walk.cu kVariants)
 int run_autotune(Ctx *c, int *chosen, ag2_walk_config *out = nullptr, int max_out = 0, int *count = nullptr);
 
 // physical constants of the reference (Constants.h:14-15, Particle.h:40)

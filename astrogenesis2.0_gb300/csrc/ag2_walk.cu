@@ -35,11 +35,10 @@ namespace {
 
 constexpr int kWalkBlock = 128;  // 4 warps
 constexpr int kStack = 512;      // stack entries per warp (FP64 walk, potential, FP32 retry pass)
-// The FP32 walk's first pass uses half that: six blocks fit an SM (shared
-// memory) instead of five.  The deepest stack measured on the bench workloads
-// is under 50 entries; a group that would overflow leaves its sums, goes to a
+// The FP32 walk's first pass uses a shallower stack (a variant parameter):
+// more blocks fit an SM.  The deepest stack measured on the bench workloads is
+// under 50 entries; a group that would overflow leaves its sums, goes to a
 // retry list and is walked again by a second launch with the full stack.
-constexpr int kStackFast = 256;
 constexpr float kGuard = 1e-5f;
 // FP32 walk variants the autotuner chooses among: the register budget (through
 // the resident 4-warp blocks per SM it is built for; 1 = the compiler's
@@ -48,11 +47,16 @@ constexpr float kGuard = 1e-5f;
 // registers), 24 (80 registers, 256 entries), 28 (72 registers, 128 entries),
 // 32 (64 registers, 64 entries; 8 blocks of ~27 KB).  A shallower stack sends
 // more groups to the retry pass; the deepest stack on the bench workloads is
-// under 50 entries.  Results do not depend on the variant.
+// under 50 entries.  The prefetch variants also ask for the child records of
+// every node they push for opening (512 bytes from its first child) to be
+// brought into L1, so that the next batch's staging, which takes exactly those
+// children, finds them there.  Results do not depend on the variant.
 struct WalkVariant {
     int min_blocks, stack, regs;
+    bool prefetch;
 };
-constexpr WalkVariant kVariants[] = {{1, 256, 0}, {6, 256, 80}, {7, 128, 72}, {8, 64, 64}};
+constexpr WalkVariant kVariants[] = {{1, 256, 0, false}, {6, 256, 80, false}, {7, 128, 72, false},
+                                     {8, 64, 64, false},  {6, 256, 80, true},  {7, 128, 72, true}};
 constexpr int kWalkVariants = kWalkVariantCount;
 static_assert(sizeof(kVariants) / sizeof(kVariants[0]) == kWalkVariants, "variant table");
 
@@ -556,9 +560,22 @@ __device__ __noinline__ int recheck_fp64(const WalkArgs &a, int c, bool leaf, co
     return decision;
 }
 
+// The child block of a node pushed for opening, its 8 walk records (512 bytes
+// from the first child, 4 or 5 cache lines), into L1 ahead of the batch that
+// stages them.  A hint: nothing waits for it.
+__device__ __forceinline__ void prefetch_children(const WalkRec *r)
+{
+    const char *p = reinterpret_cast<const char *>(r);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 128));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 256));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 384));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 511));
+}
+
 // kStk = kStack: the second pass over the groups the first one could not hold
 // in its stack (a.retry_groups, ctl->retry_count of them), with the full stack.
-template <bool kGeneral, bool kGas, int kMinBlocks, int kStk>
+template <bool kGeneral, bool kGas, int kMinBlocks, int kStk, bool kPrefetch = false>
 __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
 {
     constexpr bool kRetry = kStk == kStack;
@@ -790,6 +807,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                         const int q = sp + __popc(om & below);
                         W.stk[q] = make_int2(W.cfirst[j], (int)bm);
                         W.stkcm[q] = W.ccm[j];
+                        if (kPrefetch) prefetch_children(a.wrec + W.cfirst[j]);
                     }
                     sp += __popc(om);
                 }
@@ -949,6 +967,7 @@ __global__ void __launch_bounds__(kWalkBlock, kMinBlocks) k_walk32(WalkArgs a)
                         const int p = sp + __popc(hob & below);
                         W.stk[p] = make_int2(W.cfirst[jq], (int)opnb);
                         W.stkcm[p] = W.ccm[jq];
+                        if (kPrefetch) prefetch_children(a.wrec + W.cfirst[jq]);
                     }
                     sp += nop;
                 }
@@ -1216,6 +1235,8 @@ int run_forces(Ctx *c)
         if (v == 1) WALK((k_walk32<G, S, 6, 256>));                               \
         else if (v == 2) WALK((k_walk32<G, S, 7, 128>));                          \
         else if (v == 3) WALK((k_walk32<G, S, 8, 64>));                           \
+        else if (v == 4) WALK((k_walk32<G, S, 6, 256, true>));                    \
+        else if (v == 5) WALK((k_walk32<G, S, 7, 128, true>));                    \
         else WALK((k_walk32<G, S, 1, 256>));                                      \
         /* groups whose stack outgrew the first pass (none in the usual case) */  \
         AG2_LAUNCH(c, (k_walk32<G, S, 1, kStack>), dev_sms, kWalkBlock, 0, a);    \
@@ -1267,7 +1288,7 @@ int run_autotune(Ctx *c, int *chosen, ag2_walk_config *out, int max_out, int *co
             if (rc) break;
             if (out && k < max_out)
                 out[k] = ag2_walk_config{v, kVariants[v].regs, kVariants[v].min_blocks > 1 ? kVariants[v].min_blocks : 0,
-                                         kVariants[v].stack, gs, ms};
+                                         kVariants[v].stack, kVariants[v].prefetch ? 1 : 0, gs, ms};
             k++;
             if (ms < best) {
                 best = ms;

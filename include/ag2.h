@@ -208,7 +208,8 @@ int ag2_block_step(ag2_ctx *ctx, double H0, int with_visual, double Rv, double *
 /* Walk autotuner.  Times each FP32-walk candidate on the current tree and
  * keeps the fastest for later ag2_forces calls of this context.  A candidate
  * is a compiled variant (register budget per thread and first-pass stack
- * depth, which together set the warps resident per SM) with a walk group size
+ * depth, which together set the warps resident per SM, and whether the child
+ * records of nodes to open are prefetched into L1) with a walk group size
  * (particles per warp group: 32 or 16).  The chosen group size is written to
  * the context's params.group_size.  Variant and stack depth do not change the
  * results; the group size changes the FP32 sums in their last bits, within
@@ -220,12 +221,13 @@ typedef struct ag2_walk_config {
     int32_t regs;           /* register budget per thread (0 = the compiler's choice) */
     int32_t blocks_per_sm;  /* resident 4-warp blocks per SM the budget is built for (0 = compiler) */
     int32_t stack;          /* first-pass stack entries per warp (deeper groups go to a retry pass) */
+    int32_t prefetch;       /* 1: child records of nodes pushed for opening are prefetched into L1 */
     int32_t group_size;     /* particles per walk group */
     float ms;               /* measured walk time on the context's tree */
 } ag2_walk_config;
 int ag2_autotune(ag2_ctx *ctx, int *variant);
 int ag2_autotune_walk(ag2_ctx *ctx, int max, ag2_walk_config *out, int *count, int *chosen);
-/* Use FP32-walk variant `variant` (an ag2_walk_config.variant, 0..3) without
+/* Use FP32-walk variant `variant` (an ag2_walk_config.variant, 0..5) without
  * timing anything, e.g. a choice kept from an earlier ag2_autotune_walk;
  * the group size is params.group_size. */
 int ag2_set_walk_variant(ag2_ctx *ctx, int variant);

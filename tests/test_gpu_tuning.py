@@ -4,7 +4,8 @@ params.group_size) on the GPU.
 * Every candidate is timed and reported; the one kept is the fastest and is
   what later walks use.
 * The compiled variants (register budget, first-pass stack depth down to 64
-  entries, whose overflowing groups go to the retry pass) give the same FP32
+  entries, whose overflowing groups go to the retry pass, L1 prefetch of the
+  children to open) give the same FP32
   accelerations bit for bit: the arithmetic is explicit (no contraction) and a
   retried group is walked again from the start.
 * The FP64 walk's per-particle sums do not depend on the group size (each
@@ -41,8 +42,8 @@ def test_autotune_reports_candidates_and_keeps_the_fastest():
     c.forces()
     r = c.autotune_walk()
     cands = r["candidates"]
-    assert len(cands) == 8 and {x["group_size"] for x in cands} == {32, 16}
-    assert {x["variant"] for x in cands} == {0, 1, 2, 3}
+    assert len(cands) == 12 and {x["group_size"] for x in cands} == {32, 16}
+    assert {x["variant"] for x in cands} == {0, 1, 2, 3, 4, 5}
     assert all(x["ms"] > 0 for x in cands)
     best = min(cands, key=lambda x: x["ms"])
     assert r["chosen"] == best
@@ -61,7 +62,7 @@ def test_variants_give_identical_results():
     c = _ctx(d, precision="fp32")
     ref = None
     zero = np.zeros(len(d["mass"]))
-    for v in range(4):
+    for v in range(6):
         c.set_walk_variant(v)
         c.set_field("dUdt", zero)  # forces adds the SPH heating to dUdt
         c.forces()
