@@ -448,10 +448,12 @@ def our_arm(args, wl, d):
     walk_ms = [e[0].elapsed_time(e[1]) for e in walk_ev]
     build_ms = [e[2].elapsed_time(e[3]) for e in walk_ev]
     _, n_internal, _ = ctx.node_count()
-    # algorithmic build bytes per step: N (32 read pos+mass + 12 write key+index) + N 24 (sort pass) +
-    # N (33 + 32) (gather/scatter into tree order) + occupied nodes x 2 x 64 (write, then read for moments);
-    # occupied nodes = internal nodes + at most N non-empty leaves
-    build_bytes = n * (32 + 12 + 24 + 33 + 32) + (n_internal + n) * 128
+    # algorithmic build bytes per step, with the records this build writes:
+    # N (32 read pos+mass + 12 write key+index) + N 24 (one sort pass) + N 2 x 153 (the particle state
+    # read and written in tree order) + occupied nodes x (80 + 64 + 64 written: NodeSum, NodeMom and
+    # WalkRec, + 80 read: the NodeSum its parent adds up); occupied nodes = internal nodes + at most N
+    # non-empty leaves
+    build_bytes = n * (32 + 12 + 24 + 2 * 153) + (n_internal + n) * (80 + 64 + 64 + 80)
     build_avg_s = sum(build_ms) / len(build_ms) / 1e3
     walk_avg_s = sum(walk_ms) / len(walk_ms) / 1e3
     flop_per_walk = (FLOP_GRAV * inter_g + FLOP_SPH * inter_s) / args.steps
@@ -621,6 +623,21 @@ def our_arm(args, wl, d):
             tcpu, _, sample = cpu_step_time(d, wl, args.cpu_walk_fraction, threads)
         cpu = {"value": n / tcpu, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
 
+    # DRAM bytes of one build (every build kernel of one step), likewise
+    btraffic, btraffic_src = None, None
+    bpath = os.path.join(REPO, "profiles", "build_traffic.json")
+    if os.path.exists(bpath):
+        try:
+            import hashlib
+
+            bj = json.load(open(bpath))
+            btraffic = bj.get(args.workload)
+            cur = hashlib.sha256(open(os.path.join(REPO, "astrogenesis2.0_gb300", "csrc", "ag2_build.cu"),
+                                      "rb").read()).hexdigest()[:16]
+            btraffic_src = {"file": "profiles/build_traffic.json", "build_source_sha": bj.get("build_source_sha"),
+                            "current_build_source_sha": cur, "current": bj.get("build_source_sha") == cur}
+        except (OSError, ValueError):
+            btraffic = None
     # DRAM bytes of one walk launch, from the committed ncu summary; it states
     # the walk source it was measured on, so a changed kernel shows as stale
     traffic, traffic_src = None, None
@@ -654,7 +671,11 @@ def our_arm(args, wl, d):
                          "flop_per_launch": flop_per_walk},
             "roofline_build": {"bound": "hbm", "kernel": "octree build (every build kernel, one step)",
                                "achieved": build_bytes / build_avg_s / 1e9, "peak": HBM_PEAK_GBS, "unit": "GB/s",
-                               "frac": build_bytes / build_avg_s / 1e9 / HBM_PEAK_GBS, "traffic": None,
+                               "frac": build_bytes / build_avg_s / 1e9 / HBM_PEAK_GBS, "traffic": btraffic,
+                               "traffic_over_algorithmic": btraffic / build_bytes if btraffic else None,
+                               "dram_achieved": btraffic / build_avg_s / 1e9 if btraffic else None,
+                               "dram_frac": btraffic / build_avg_s / 1e9 / HBM_PEAK_GBS if btraffic else None,
+                               "traffic_source": btraffic_src,
                                "bytes_per_build": build_bytes, "build_ms": build_avg_s * 1e3,
                                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "cpu_baseline": cpu,
