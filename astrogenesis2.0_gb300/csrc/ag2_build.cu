@@ -769,11 +769,13 @@ struct Sums {
         mx += t.mx;
         my += t.my;
         mz += t.mz;
-        g += t.g;
-        gvx += t.gvx;
-        gvy += t.gvy;
-        gvz += t.gvz;
-        ng += t.ng;
+        if (t.ng) {  // without gas the four sums are exact zeros: adding them changes nothing
+            g += t.g;
+            gvx += t.gvx;
+            gvy += t.gvy;
+            gvz += t.gvz;
+            ng += t.ng;
+        }
     }
 };
 
@@ -866,7 +868,9 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     }
     w.B = make_float4(lx, ly, lz, mac);
     w.C = make_int4(first_child, leafslot, (int)cmask, 0);
-    if (leaf && lp >= 0)
+    if ((dbits(gas) << 1) == 0)
+        w.D = make_float4(0.f, 0.f, 0.f, 0.f);  // no gas: the walk reads none of it (its SPH needs D.w > 0)
+    else if (leaf && lp >= 0)
         w.D = make_float4((float)P.vx[lp], (float)P.vy[lp], (float)P.vz[lp], (float)scale2(gas, 2 * k));
     else
         w.D = make_float4((float)mvx, (float)mvy, (float)mvz, (float)scale2(gas, 2 * k));

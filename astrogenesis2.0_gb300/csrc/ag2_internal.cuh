@@ -52,8 +52,8 @@ struct alignas(64) NodeMom {
 // (hi floats) and mass * ls^2; B = centre of mass (lo floats) and the opening
 // threshold (radius * ls / theta)^2 (-1 for a leaf); C = first child (-1 leaf),
 // leaf particle slot (-1 none), child mask, 0; D = gas velocity (mVel, or the
-// leaf particle's velocity) and gasMass * ls^2.  One 64-byte record, so a staged
-// child is two sectors of one cache line.
+// leaf particle's velocity) and gasMass * ls^2, zeros for a node without gas.
+// One 64-byte record, so a staged child is two sectors of one cache line.
 struct alignas(64) WalkRec {
     float4 A, B;
     int4 C;

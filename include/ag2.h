@@ -254,7 +254,7 @@ int ag2_topology(ag2_ctx *ctx, int32_t *depth, int32_t *is_leaf, int32_t *partic
  * (zeros for an empty node): centre of mass as hi floats and mass * ls^2; the
  * lo floats of the centre of mass and (radius * ls / theta)^2 (-1 for a leaf);
  * first child, leaf particle slot, child mask and 0 as int32 bits; gas velocity
- * and gasMass * ls^2.  ls = 2^k with k = 1022 - (the biased exponent of the
+ * and gasMass * ls^2 (zeros for a node that holds no gas mass).  ls = 2^k with k = 1022 - (the biased exponent of the
  * instance's root half-width), so scaled lengths are below 1.  A diagnostic of
  * the records the reference's calculateGravityForce reads as doubles
  * (Node.cpp:285-305); the reference has no such view. */

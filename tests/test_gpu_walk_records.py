@@ -1,7 +1,7 @@
 """The FP32 walk's node records against numpy's roundings of the exported FP64
 moments, bit for bit: centre of mass as a two-float split in the instance's
 scaled units, mass and gasMass scaled by ls^2, the opening threshold and the
-gas velocity.  numpy's float32 casts round to nearest even, as the device's
+gas velocity (zeros for a node without gas).  numpy's float32 casts round to nearest even, as the device's
 conversions do.  The inputs add values on rounding ties, exact zeros and
 magnitudes whose floats are subnormal or zero."""
 import numpy as np
@@ -53,7 +53,10 @@ def _check(d, theta=0.5, e0=0.02, G=1.0):
     np.testing.assert_array_equal(_bits(B[:, 3]), _bits(mac))
     part = t["particle"][live][ok]
     own = leaf & (part >= 0)
+    gm = t["gas_mass"][live][ok]
+    # the gas velocity: a leaf's own particle's, else the node's mVel; zeros without gas
     vel = np.where(own[:, None], d["vel"][np.maximum(part, 0)], t["mvel"][live][ok])
+    vel = np.where((gm != 0)[:, None], vel, 0.0)
     np.testing.assert_array_equal(_bits(D[:, :3]), _bits(vel.astype(np.float32)))
     return int(ok.sum())
 
