@@ -482,7 +482,9 @@ int ag2_destroy(ag2_ctx *c)
     for (int b = 0; b < 2; b++) {
         if (c->dl_gathered[b]) cudaEventDestroy(c->dl_gathered[b]);
         if (c->dl_copied[b]) cudaEventDestroy(c->dl_copied[b]);
+        if (c->up_ev[b]) cudaEventDestroy(c->up_ev[b]);
     }
+    if (c->acc_stage) cudaFree(c->acc_stage);
     if (c->blk_key) cudaFree(c->blk_key);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -897,15 +899,59 @@ int ag2_step(ag2_ctx *c, double dt, double hubble_factor, int with_visual, doubl
     return rc;
 }
 
+// ag2_upload followed by ag2_set_field(AG2_ACC, acc), the same result bit for
+// bit, with the accelerations' host-to-device copy on the copy stream, queued
+// behind the other fields' copies: it crosses the link while the slot-order
+// gather of those fields runs, instead of after it.
+static int upload_with_acc(Ctx *c, size_t n, const double *pos, const double *vel, const double *mass,
+                           const double *U, const uint8_t *type, const double *acc)
+{
+    if (n > c->cap) return set_err(c, AG2_E_CAPACITY, "more particles than the context capacity");
+    if (!pos || !mass || !type) return set_err(c, AG2_E_INVALID, "pos, mass and type are required");
+    int rc;
+    if ((rc = dl_begin(c))) return rc;  // the copy stream
+    if (!c->acc_stage) {
+        if (cudaMalloc(&c->acc_stage, 3 * c->cap * sizeof(double)) != cudaSuccess) {
+            c->acc_stage = nullptr;
+            cudaGetLastError();
+            return set_err(c, AG2_E_NOMEM, "acceleration staging allocation failed");
+        }
+        for (auto &e : c->up_ev) AG2_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    Particles &spare = c->st[1];
+    double *pos_d = c->staging, *vel_d = vel ? c->staging + 3 * n : nullptr;
+    AG2_CUDA(c, cudaMemcpyAsync(pos_d, pos, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (vel) AG2_CUDA(c, cudaMemcpyAsync(vel_d, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(spare.m, mass, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (U) AG2_CUDA(c, cudaMemcpyAsync(spare.U, U, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(c->staging_u8, type, n, cudaMemcpyHostToDevice, c->stream));
+    // the accelerations after those copies (the link is shared), beside the gather
+    AG2_CUDA(c, cudaEventRecord(c->up_ev[0], c->stream));
+    AG2_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->up_ev[0], 0));
+    AG2_CUDA(c, cudaMemcpyAsync(c->acc_stage, acc, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->copy_stream));
+    AG2_CUDA(c, cudaEventRecord(c->up_ev[1], c->copy_stream));
+    rc = upload_common(c, n, pos_d, vel_d, spare.m, U ? spare.U : nullptr, c->staging_u8);
+    if (!rc) rc = io_reset_tags(c, n);
+    // the scatter waits for the copy; a failure above still has to let it land
+    AG2_CUDA(c, cudaStreamWaitEvent(c->stream, c->up_ev[1], 0));
+    if (rc) return rc;
+    AG2_LAUNCH(c, k_scatter_in, grid_for(n, kBlock), kBlock, 0, (int)n, c->S(), AG2_ACC, c->acc_stage);
+    c->graph_epoch++;
+    return AG2_OK;
+}
+
 // The step itself; ag2_step_host routes every failure through dl_abort, since
 // the position and acceleration read-backs start before the step ends.
 static int step_host(ag2_ctx *c, size_t n, double dt, double hubble_factor, int with_visual, double Rv,
                      const ag2_host_io *io)
 {
     int rc;
-    if ((rc = ag2_upload(c, n, io->pos, io->vel, io->mass, io->U, io->type))) return rc;
+    if (io->acc) {
+        if ((rc = upload_with_acc(c, n, io->pos, io->vel, io->mass, io->U, io->type, io->acc))) return rc;
+    } else if ((rc = ag2_upload(c, n, io->pos, io->vel, io->mass, io->U, io->type))) {
+        return rc;
+    }
     if (io->first && (rc = ag2_set_instances(c, io->n_inst, io->first, io->massInH))) return rc;
-    if (io->acc && (rc = ag2_set_field(c, AG2_ACC, io->acc, 0))) return rc;
     if ((rc = dl_begin(c))) return rc;
     phase_reset(c);
     if ((rc = run_kick_drift(c, dt))) return rc;

@@ -237,6 +237,10 @@ struct Ctx {
     // the gathers of the context's stream (two staging halves)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t dl_gathered[2] = {}, dl_copied[2] = {};
+    // ag2_step_host's accelerations: their own staging (3 doubles per particle
+    // of capacity, made on first use) and the events that order their copy
+    double *acc_stage = nullptr;
+    cudaEvent_t up_ev[2] = {};
     // gasMass tables: instance k's sequential partial sums start at gas_off[k]
     int32_t *gas_off = nullptr;     // device
     uint8_t *gas_uni = nullptr;     // device: instance's gas particles share one mass

@@ -94,3 +94,46 @@ def test_bad_instance_layouts():
         c.set_instances(np.array([0, 10, 5, first[-1]]))
     with pytest.raises(ag2.AG2Error):
         c.set_instances(np.array([1, first[-1]]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_ragged_forest_with_empty_and_single_particle_simulations(precision):
+    """A forest whose simulations include an empty one, single-particle ones
+    and an all-gas one: the others are bit-identical to their lone runs, the
+    single particles feel no force, and the empty simulation changes nothing."""
+    import ag2
+
+    gas = ics.small_gas_cloud(600, seed=47, gas_fraction=1.0)
+    one = ics.plummer(1, seed=48)
+    parts = [ics.plummer(500, seed=46), {k: v[:0] for k, v in one.items() if hasattr(v, "__len__")}, one, gas,
+             ics.plummer(1, seed=49), ics.plummer(300, seed=50)]
+    mih = [0.0, 0.0, 0.0, gas["massInH"], 0.0, 0.0]
+    n = sum(len(p["mass"]) for p in parts)
+    c = ag2.Context(n, e0=0.01, precision=precision)
+    cat = lambda k: np.concatenate([p[k] for p in parts])  # noqa: E731
+    c.upload(cat("pos"), cat("mass"), cat("type").astype(np.uint8), vel=cat("vel"), U=cat("U"))
+    first = np.cumsum([0] + [len(p["mass"]) for p in parts])
+    c.set_instances(first, mih)
+    c.build_tree()
+    c.sph_density()
+    c.forces()
+    for _ in range(2):
+        c.step(1e-3)
+    got = {k: c.download(k) for k in ("pos", "acc", "h", "rho")}
+    for k, p in enumerate(parts):
+        if len(p["mass"]) == 0:
+            continue
+        a = ag2.Context(len(p["mass"]), e0=0.01, precision=precision, massInH=mih[k])
+        a.upload(p["pos"], p["mass"], p["type"].astype(np.uint8), vel=p["vel"], U=p["U"])
+        a.build_tree()
+        a.sph_density()
+        a.forces()
+        for _ in range(2):
+            a.step(1e-3)
+        sl = slice(first[k], first[k + 1])
+        for f in got:
+            np.testing.assert_array_equal(got[f][sl], a.download(f), err_msg=f"{f} of simulation {k}")
+        if len(p["mass"]) == 1:
+            assert not got["acc"][sl].any()
+        a.close()
+    c.close()
