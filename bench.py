@@ -1051,7 +1051,7 @@ def main():
     ap.add_argument("--workload", default="merger4m", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--plain-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--error-samples", type=int, default=65536)
     ap.add_argument("--cpu-walk-fraction", type=int, default=1)
     ap.add_argument("--ref-walk-fraction", type=int, default=1)
