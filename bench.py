@@ -594,9 +594,11 @@ def our_arm(args, wl, d):
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
         hpos, hvel, hmass = pin(ctx.download("pos")), pin(ctx.download("vel")), pin(d["mass"])
         hU, htype, hacc = pin(ctx.download("U")), pin(d["type"]), pin(ctx.download("acc"))
+        outs = {"pos": hpos, "vel": hvel, "acc": hacc, "U": hU}
+        for _ in range(3):  # warm-up: the first call makes the acceleration staging and the copy stream
+            ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs, first=d.get("first"))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        outs = {"pos": hpos, "vel": hvel, "acc": hacc, "U": hU}
         for _ in range(args.e2e_steps):  # one call: upload, step, read-back (positions during the walk)
             ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs, first=d.get("first"))
         te = time.perf_counter() - t0
@@ -937,11 +939,13 @@ def ensemble_leg(args):
     hpos, hvel, hmass, hU, htype, hacc = (pin(ctx.download("pos")), pin(ctx.download("vel")), pin(d["mass"]),
                                           pin(ctx.download("U")), pin(d["type"]), pin(a32))
     outs = {"pos": hpos, "vel": hvel, "acc": hacc, "U": hU}
+    for _ in range(3):  # warm-up
+        ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs, first=d["first"])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(3):
+    for _ in range(args.e2e_steps):
         ctx.step_host(dt, hpos, hmass, htype, vel=hvel, U=hU, acc=hacc, out=outs, first=d["first"])
-    te = (time.perf_counter() - t0) / 3
+    te = (time.perf_counter() - t0) / args.e2e_steps
     ctx.close()
     per_launch = one_sim_per_launch(d, wl, args.plain_steps, stream)
     value = n / t
