@@ -15,8 +15,9 @@ benchmark runs, not only at fixture sizes:
 
 Tolerances (as tests/test_gpu_parity.py): node count, per-node depth / leaf
 flag / leaf particle / childParticles count and membership hash / centre /
-half-width, Particle::node, the root half-width and h bit-exact; rho relative
-1e-12; acc of the FP64 walk relative median <= 1e-12, 99.9th percentile <=
+half-width, Particle::node, the root half-width and h bit-exact; rho and
+visualDensity relative 1e-12; dU/dt within 1e-10 (FP64) and 1e-4 (FP32) of
+its largest value; acc of the FP64 walk relative median <= 1e-12, 99.9th percentile <=
 1e-11 and max <= 5e-11 per particle: node masses and centres of mass are
 summed bottom-up, not as the reference's running mean (1e-12 relative), and a
 particle whose net acceleration nearly cancels magnifies that relative to its
@@ -88,6 +89,16 @@ def check_forces(c, ref_acc, idx, precision, label, fp64_bound=(1e-12, 1e-11, 5e
         assert med <= 1e-5 and p999 <= 1e-3, (label, med, p999)
 
 
+def check_dudt(c, ref_du, gas, precision, label):
+    """dU/dt of the gas (the SPH heating the walk adds): FP64 within 1e-10
+    and FP32 within 1e-4 of the largest |dU/dt|."""
+    du = c.download("dUdt")
+    scale = max(np.max(np.abs(ref_du[gas])), 1e-300)
+    err = np.max(np.abs(du[gas] - ref_du[gas])) / scale
+    print(f"\n{label} {precision}: dU/dt max diff {err:.2e} of scale")
+    assert err <= (1e-10 if precision == "fp64" else 1e-4), (label, err)
+
+
 def ctx_for(d, e0, theta, massInH, precision):
     import ag2
 
@@ -101,14 +112,20 @@ def test_disk1m_against_port():
     d = ics.disk_galaxy(seed=2)
     e0, theta, mih = 0.02, 0.5, d["massInH"]
     w = port_tree(d, mih)
+    Rv = w.root_radius() / 1e5  # Simulation.cpp:126
+    w.visual_density(Rv)
     w.forces(e0, theta, THREADS)
-    ref_acc = w.get("acc")
+    ref_acc, ref_du, ref_vd = w.get("acc"), w.get("dUdt"), w.get("vdens")
+    gas = d["type"] == 2
     idx = np.arange(len(d["mass"]))
     for precision in ("fp64", "fp32"):
         c = ctx_for(d, e0, theta, mih, precision)
         c.build_tree()
         nn, _ = check_tree(c, w, mih, "disk1m")
+        c.visual_density(Rv)
+        np.testing.assert_allclose(c.download("vdens"), ref_vd, rtol=1e-12, atol=0)
         check_forces(c, ref_acc, idx, precision, f"disk1m ({nn} nodes)")
+        check_dudt(c, ref_du, gas, precision, "disk1m")
         c.close()
 
 
@@ -119,13 +136,14 @@ def test_merger262k_theta_sweep_against_port(theta):
     e0, mih = 0.02, d["massInH"]
     w = port_tree(d, mih)
     w.forces(e0, theta, THREADS)
-    ref_acc = w.get("acc")
+    ref_acc, ref_du = w.get("acc"), w.get("dUdt")
     idx = np.arange(len(d["mass"]))
     for precision in ("fp64", "fp32"):
         c = ctx_for(d, e0, theta, mih, precision)
         c.build_tree()
         check_tree(c, w, mih, f"merger262k theta {theta}")
         check_forces(c, ref_acc, idx, precision, f"merger262k theta {theta}")
+        check_dudt(c, ref_du, d["type"] == 2, precision, f"merger262k theta {theta}")
         c.close()
 
 
