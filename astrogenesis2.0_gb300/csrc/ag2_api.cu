@@ -430,7 +430,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     bool ok = alloc_particles(c, c->st[0], cap) == AG2_OK && alloc_particles(c, c->st[1], cap) == AG2_OK;
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->refnode, cap * 4) == cudaSuccess && cudaMalloc(&c->slot_of, cap * 4) == cudaSuccess && cudaMalloc(&c->rdist, cap * sizeof(double)) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
+         cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->refnode, cap * 4) == cudaSuccess && cudaMalloc(&c->slot_of, cap * 4) == cudaSuccess && cudaMalloc(&c->rdist, cap * sizeof(double2)) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->drop_list, 65536 * 4) == cudaSuccess && cudaMalloc(&c->digit, 2 * cap) == cudaSuccess &&
          cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&

@@ -92,17 +92,24 @@ __global__ void k_slot_of(int n, const int32_t *__restrict__ id, int32_t *__rest
     if (i < n) slot_of[id[i]] = i;
 }
 
-// first level: task (first caller index, count, destination) over particles
-// |x| of every particle once, in tree order (coalesced; the FP64 square root
-// is the costly part on this part)
+// |x| of every particle once, in tree order, with its square: (d, d*d) pairs.
+// Both are the products the reference's sums take (Tree.cpp:99-103); the
+// sequential sums below then chain only their additions.  On this part one
+// FP64 instruction holds a warp's FP64 pipe for about 64 cycles whatever its
+// active lanes, so a 4096-term sequential sum is bound by its FP64
+// instructions, and taking the squares out of it removes a third of them.
 __global__ void k_dist(int n, const double *__restrict__ px, const double *__restrict__ py,
-                       const double *__restrict__ pz, double *__restrict__ dist)
+                       const double *__restrict__ pz, double2 *__restrict__ dist)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dist[i] = dist0(px[i], py[i], pz[i]);
+    if (i < n) {
+        const double d = dist0(px[i], py[i], pz[i]);
+        dist[i] = make_double2(d, __dmul_rn(d, d));
+    }
 }
 
-__global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const double *__restrict__ dist,
+// first level: task (first caller index, count, destination) over particles
+__global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const double2 *__restrict__ dist,
                                  const int32_t *slot_of, double *buf)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -110,9 +117,9 @@ __global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const
     const int4 q = task[t];
     double s = 0.0, s2 = 0.0;
     for (int j = 0; j < q.y; j++) {
-        const double d = dist[slot_of[q.x + j]];
-        s = __dadd_rn(s, d);
-        s2 = __dadd_rn(s2, __dmul_rn(d, d));
+        const double2 d = dist[slot_of[q.x + j]];
+        s = __dadd_rn(s, d.x);
+        s2 = __dadd_rn(s2, d.y);
     }
     buf[2 * (int64_t)q.z] = s;
     buf[2 * (int64_t)q.z + 1] = s2;
@@ -152,7 +159,7 @@ __global__ void k_width_thr(int n_inst, const int64_t *first, const int32_t *fin
 }
 
 // R = max |x| over |x| <= thr (Tree.cpp:107-116); a NaN threshold keeps R = 0
-__global__ void k_width_max(int n, const double *__restrict__ dist, const int32_t *pinst, const double *thr,
+__global__ void k_width_max(int n, const double2 *__restrict__ dist, const int32_t *pinst, const double *thr,
                             double *R)
 {
     __shared__ int32_t kmin, kmax;
@@ -161,7 +168,7 @@ __global__ void k_width_max(int n, const double *__restrict__ dist, const int32_
     const int k = i < n ? pinst[i] : -1;
     unsigned long long best = 0ull;
     if (i < n) {
-        const double d = dist[i];
+        const double d = dist[i].x;
         if (d <= thr[k] && d > 0.0) best = (unsigned long long)__double_as_longlong(d);
     }
     if (threadIdx.x == 0) {

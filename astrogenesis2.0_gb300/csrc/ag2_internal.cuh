@@ -176,7 +176,7 @@ struct Ctx {
     int32_t *pnode = nullptr;     // deepest node whose range holds a tree-order slot
     int32_t *refnode = nullptr;   // the reference's Particle::node per slot (-1 = null)
     int32_t *slot_of = nullptr;   // tree-order slot of each upload index
-    double *rdist = nullptr;      // |x| of each particle (tree order) for the root half-width
+    double2 *rdist = nullptr;     // |x| of each particle and its square (tree order) for the root half-width
     int32_t *finalnode = nullptr; // SPH / visual density result node per slot
     int32_t *nodelist = nullptr;  // compacted node list (SPH density nodes)
     int32_t *drop_list = nullptr; // nodes with out-of-bounds tails (65536 entries)
