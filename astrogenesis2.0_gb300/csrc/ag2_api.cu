@@ -333,7 +333,7 @@ int ensure_instance_tables(Ctx *c)
         std::vector<std::pair<int32_t, int32_t>> cur(K);  // per instance: (first pair, count) of its current level
         for (int k = 0; k < K; k++) {
             const int64_t b = c->inst_first_h[k], n = c->inst_first_h[k + 1] - b;
-            const int64_t run = n <= kSeqWidthMax ? std::max<int64_t>(n, 1) : 64;
+            const int64_t run = n <= kSeqWidthMax ? std::max<int64_t>(n, 1) : kWsumRun;
             const int32_t cnt = (int32_t)((n + run - 1) / run);
             cur[k] = {nbuf, std::max(cnt, 1)};
             for (int64_t j = 0; j < std::max<int64_t>(n, 1); j += run)
@@ -372,6 +372,17 @@ int ensure_instance_tables(Ctx *c)
                                     c->stream));
         AG2_CUDA(c, cudaMemcpyAsync(c->wsum_final, fin.data(), K * sizeof(int32_t), cudaMemcpyHostToDevice,
                                     c->stream));
+        // the long sequential sums, which the particle-level kernel leaves to k_wsum_long
+        std::vector<int32_t> longt;
+        for (int32_t t = 0; t < c->wsum_level[1]; t++)
+            if (all[t].y > kWsumRun) longt.push_back(t);
+        c->nwsum_long = (int32_t)longt.size();
+        if (!longt.empty()) {
+            if (!realloc_dev(c->wsum_long, longt.size()))
+                return set_err(c, AG2_E_NOMEM, "root width table allocation failed");
+            AG2_CUDA(c, cudaMemcpyAsync(c->wsum_long, longt.data(), longt.size() * sizeof(int32_t),
+                                        cudaMemcpyHostToDevice, c->stream));
+        }
         AG2_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     {
@@ -466,7 +477,7 @@ int ag2_destroy(ag2_ctx *c)
     free_nodes(c->nd);
     void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->slot_of, c->rdist, c->finalnode,
                   c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
-                  c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->ctl, c->pinst, c->groups, c->retry_groups, c->inst_first, c->inst_R,
+                  c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->wsum_long, c->ctl, c->pinst, c->groups, c->retry_groups, c->inst_first, c->inst_R,
                   c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax,
                   c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);

@@ -115,6 +115,7 @@ __global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntask) return;
     const int4 q = task[t];
+    if (q.y > kWsumRun) return;  // a long sequential sum: k_wsum_long
     double s = 0.0, s2 = 0.0;
     for (int j = 0; j < q.y; j++) {
         const double2 d = dist[slot_of[q.x + j]];
@@ -123,6 +124,33 @@ __global__ void k_wsum_particles(int ntask, const int4 *__restrict__ task, const
     }
     buf[2 * (int64_t)q.z] = s;
     buf[2 * (int64_t)q.z + 1] = s2;
+}
+
+// The long first-level tasks: one sequential sum per instance of 65..4096
+// particles (Tree.cpp:99-103), up to 4096 dependent FP64 additions.  Two warps
+// per task, one per chain (sum of |x|, sum of |x|^2), so that each chain has
+// an SM partition's FP64 pipe to itself; the lanes load 32 terms at a time in
+// parallel and every lane adds them in order, taking them by shuffle (the
+// same sums on every lane, bit for bit those of one thread).
+__global__ void k_wsum_long(int nlong, const int32_t *__restrict__ longt, const int4 *__restrict__ task,
+                            const double2 *__restrict__ dist, const int32_t *__restrict__ slot_of, double *buf)
+{
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= 2 * nlong) return;
+    const int chain = w & 1;
+    const int4 q = task[longt[w >> 1]];
+    double s = 0.0;
+    for (int j0 = 0; j0 < q.y; j0 += 32) {
+        const int j = j0 + lane;
+        double v = 0.0;
+        if (j < q.y) {
+            const double2 d = dist[slot_of[q.x + j]];
+            v = chain ? d.y : d.x;
+        }
+        const int m = min(32, q.y - j0);
+        for (int u = 0; u < m; u++) s = __dadd_rn(s, __shfl_sync(0xffffffffu, v, u));
+    }
+    if (lane == 0) buf[2 * (int64_t)q.z + chain] = s;
 }
 
 // higher levels: task (first source sum, count, destination)
@@ -1881,10 +1909,13 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         for (size_t l = 0; l + 1 < c->wsum_level.size(); l++) {
             const int nt = c->wsum_level[l + 1] - c->wsum_level[l];
             const int4 *tk = c->wsum_task + c->wsum_level[l];
-            if (l == 0)
+            if (l == 0) {
                 AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->rdist, c->slot_of,
                            c->width_part);
-            else
+                if (c->nwsum_long > 0)
+                    AG2_LAUNCH(c, k_wsum_long, grid_for(64 * (size_t)c->nwsum_long, kBlock), kBlock, 0,
+                               c->nwsum_long, c->wsum_long, tk, c->rdist, c->slot_of, c->width_part);
+            } else
                 AG2_LAUNCH(c, k_wsum_sums, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->width_part);
         }
     }

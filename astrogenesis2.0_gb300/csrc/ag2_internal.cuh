@@ -193,6 +193,8 @@ struct Ctx {
     int4 *wsum_task = nullptr;    // root-width summation tasks, level after level
     int32_t *wsum_final = nullptr; // per instance: position of its final pair
     std::vector<int32_t> wsum_level;  // task offsets of each level
+    int32_t *wsum_long = nullptr;     // level-0 tasks of more than kWsumRun terms
+    int32_t nwsum_long = 0;
     double *width_thr = nullptr;  // mean + 10 sigma per instance
     double gas_table_mass = -1.0; // gas particle mass the gasMass table was built for
     int32_t gas_table_n = -1;
@@ -371,6 +373,9 @@ __host__ __device__ inline double scale2(double x, int k)
 // the root half-width's sums are sequential (the reference's, bit for bit) up to
 // this many particles per instance, a 64-ary tree of sequential runs above
 constexpr int kSeqWidthMax = 4096;
+// root-width tasks of more terms than this (the one sequential sum of an
+// instance of 65..4096 particles) run on warps of their own (k_wsum_long)
+constexpr int kWsumRun = 64;
 
 // status helpers
 int set_err(Ctx *c, int code, const std::string &msg);
