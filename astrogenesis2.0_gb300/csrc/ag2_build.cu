@@ -1912,9 +1912,11 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             if (l == 0) {
                 AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->rdist, c->slot_of,
                            c->width_part);
+                // one task (its two warps) per block, so that the tasks spread
+                // over the SMs and no two chains share a partition's FP64 pipe
                 if (c->nwsum_long > 0)
-                    AG2_LAUNCH(c, k_wsum_long, grid_for(64 * (size_t)c->nwsum_long, kBlock), kBlock, 0,
-                               c->nwsum_long, c->wsum_long, tk, c->rdist, c->slot_of, c->width_part);
+                    AG2_LAUNCH(c, k_wsum_long, (unsigned)c->nwsum_long, 64, 0, c->nwsum_long, c->wsum_long, tk,
+                               c->rdist, c->slot_of, c->width_part);
             } else
                 AG2_LAUNCH(c, k_wsum_sums, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->width_part);
         }
