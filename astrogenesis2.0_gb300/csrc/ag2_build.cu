@@ -147,8 +147,13 @@ __global__ void k_wsum_long(int nlong, const int32_t *__restrict__ longt, const 
             const double2 d = dist[slot_of[q.x + j]];
             v = chain ? d.y : d.x;
         }
-        const int m = min(32, q.y - j0);
-        for (int u = 0; u < m; u++) s = __dadd_rn(s, __shfl_sync(0xffffffffu, v, u));
+        if (q.y - j0 >= 32) {
+            // a full block: every shuffle can issue ahead of the chain of additions
+#pragma unroll
+            for (int u = 0; u < 32; u++) s = __dadd_rn(s, __shfl_sync(0xffffffffu, v, u));
+        } else {
+            for (int u = 0; u < q.y - j0; u++) s = __dadd_rn(s, __shfl_sync(0xffffffffu, v, u));
+        }
     }
     if (lane == 0) buf[2 * (int64_t)q.z + chain] = s;
 }
