@@ -129,7 +129,10 @@ int ag2_download(ag2_ctx *ctx, int field, double *dst, int dst_is_device);
  * are page-locked (cudaHostAlloc / cudaHostRegister); with pageable memory each
  * copy blocks until it has landed and the stages after it queue behind it.
  * The arrays are written until the call returns, on success and on failure
- * alike (a failing call waits for the copies it started before returning). */
+ * alike (a failing call waits for the copies it started before returning).
+ * The first call with acc != NULL allocates a staging buffer of 3 doubles per
+ * particle of capacity for the accelerations (kept until ag2_destroy), whose
+ * copy then runs beside the gather of the other fields. */
 typedef struct ag2_host_io {
     const double *pos, *vel, *mass, *U, *acc;
     const uint8_t *type;
