@@ -246,6 +246,21 @@ __device__ __forceinline__ void set_bounds(Nodes nd, int64_t c, double r)
 {
     set_bounds_v(nd, c, nd.cx[c], nd.cy[c], nd.cz[c], r);
 }
+// The same nine keys of node v, formed from its centre and half-width where
+// they are used: the serial subtrees (k_local) keep none in memory.
+__device__ __forceinline__ void local_keys(const Nodes &nd, int64_t v, int64_t *k)
+{
+    const double x = nd.cx[v], y = nd.cy[v], z = nd.cz[v], r = nd.radius[v];
+    k[0] = okey(__dsub_rn(x, r));
+    k[1] = okey(__dsub_rn(y, r));
+    k[2] = okey(__dsub_rn(z, r));
+    k[3] = okey(__dadd_rn(x, r));
+    k[4] = okey(__dadd_rn(y, r));
+    k[5] = okey(__dadd_rn(z, r));
+    k[6] = okey(x);
+    k[7] = okey(y);
+    k[8] = okey(z);
+}
 
 // root of instance k is node k (Tree.cpp:28-33: centre at the origin, half-width
 // from calcTreeWidth, depth 0)
@@ -535,7 +550,8 @@ __global__ void __launch_bounds__(kBlock) k_nodes(LevelPair lpair, int thresh, i
             nd.cx[c] = x;
             nd.cy[c] = y;
             nd.cz[c] = z;
-            if (cm != MODE_VEC1) set_bounds_v(nd, c, x, y, z, rc);
+            // a serial root's keys are formed by k_local from this centre and half-width
+            if (cm != MODE_VEC1 && !clocal) set_bounds_v(nd, c, x, y, z, rc);
         }
     }
     const bool clocal = split && b.local_ok && cm == MODE_SER_ENTRY;
@@ -1072,9 +1088,13 @@ __device__ __forceinline__ void moments_internal(Nodes &nd, int64_t nid, const P
     Sums tot, own;
     own.zero();
     uint8_t cmask = 0;
-    for (int o = 0; o < 8; o++) {
+    unsigned live = 0;
+#pragma unroll
+    for (int o = 0; o < 8; o++) live |= (nd.count[first + o] != 0 ? 1u : 0u) << o;
+    while (live) {
+        const int o = __ffs(live) - 1;
+        live &= live - 1;
         const int64_t c = first + o;
-        if (nd.count[c] == 0) continue;
         const NodeSum t = nd.tsum[c];
         own.add_sum(t);
         // bit o: the child's own mass != 0 (on the bits).  Without an
@@ -1324,8 +1344,16 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
                     bigm &= bigm - 1;
                     const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
                     int64_t b[9];
+                    {
+                        // lane k < 9 forms key k (one FP64 addition for the warp), every lane takes all nine
+                        const int ax = lane % 3;
+                        const double x = ax == 0 ? nd.cx[v] : ax == 1 ? nd.cy[v] : nd.cz[v];
+                        const double r = nd.radius[v];
+                        const double t = lane < 6 ? __dadd_rn(x, lane < 3 ? -r : r) : x;
+                        const int64_t key = okey(t);
 #pragma unroll
-                    for (int k = 0; k < 9; k++) b[k] = nd.bkey[9 * (int64_t)v + k];
+                        for (int k = 0; k < 9; k++) b[k] = __shfl_sync(full, key, k);
+                    }
                     int cn[9];
 #pragma unroll
                     for (int d = 0; d < 9; d++) cn[d] = 0;
@@ -1351,8 +1379,7 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
                 const int32_t v = fnc[f], ls = fsc[f], cnt = fcc[f];
                 if (cnt > kCoop) continue;
                 int64_t b[9];
-#pragma unroll
-                for (int k = 0; k < 9; k++) b[k] = nd.bkey[9 * (int64_t)v + k];
+                local_keys(nd, v, b);
                 int16_t *hh = FH + 9 * f;
 #pragma unroll
                 for (int d = 0; d < 9; d++) hh[d] = 0;
@@ -1550,7 +1577,6 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
                 nd.cx[c] = x;
                 nd.cy[c] = y;
                 nd.cz[c] = z;
-                set_bounds_v(nd, c, x, y, z, rc);
             }
             __syncwarp();
             if (nn) deepest = max(deepest, level + 1);
@@ -2085,6 +2111,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     const unsigned gl = capture ? fixed_grid : std::max(1u, grid_for(n, kBlock));
     AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, n, c->pnode, c->nd, c->S(), c->gas_prefix, c->gas_off,
                c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
+    phase_mark(c, "build: leaf moments");
     const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
     AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint);
     if (capture) {
@@ -2116,7 +2143,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
                        c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
         }
     }
-    phase_mark(c, "build: moments");
+    phase_mark(c, "build: internal moments");
     c->have_tree = true;  // (inside a capture: for the launches that follow it)
     c->tree_theta = c->prm.theta;
     return AG2_OK;
