@@ -840,8 +840,7 @@ static int run_step_graph(Ctx *c, double dt, double hubble, int with_visual, dou
     AG2_CUDA(c, cudaStreamSynchronize(c->stream));
     c->cur ^= 1;
     const Ctx::Ctl &h = *c->ctl_host;
-    int mlevels = 0;
-    for (int L = 0; L < AG2_MAX_DEPTH; L++) mlevels += h.lvl_cnt[L] ? 1 : 0;
+    const int mlevels = moments_launches(h.lvl_cnt);
     c->launches += c->graph_launches[from] + 4 * (int64_t)(h.level + 1) + 2 * (int64_t)mlevels;
     c->inter_grav = (int64_t)h.inter_grav;
     c->inter_sph = (int64_t)h.inter_sph;

@@ -584,7 +584,10 @@ __global__ void __launch_bounds__(kBlock) k_nodes(LevelPair lpair, int thresh, i
 // Partition of every active slot's particle by digit; settled particles go to
 // their final slot, the others (and their keys) to the next level's buffers.
 // The next level's active slots are the slots that land in a child that is
-// split again; they are listed in slot order within each thread block.
+// split again; the thread that moves a particle there lists its new slot.  The
+// list's order (like the order of the particles within a child, which the
+// cursor atomics set) changes no result: a node's final range is its children
+// in octant order followed by its out-of-bounds tail in upload order.
 __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, Ctx::Ctl *ctl)
 {
     __shared__ int32_t sh[kBlock / 32 + 1];
@@ -613,16 +616,20 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
                 b.kx_next[np] = kx;
                 b.ky_next[np] = ky;
                 b.kz_next[np] = kz;
-                if (cn == 1) {
-                    // its digit in the child for the next level, and the child's histogram
-                    // (k_nodes of this level has left the histogram zero)
-                    const int d2 = octant_digit(nd.bkey + 9 * (int64_t)child, kx, ky, kz);
-                    b.digit_next[np] = (uint8_t)d2;
-                    agg_inc(b.hist, 9 * nd.nlx[child] + d2);
-                }
             }
             if (cn == 1) {
+                // its digit in the child for the next level, and the child's histogram
+                // (k_nodes of this level has left the histogram zero); its new
+                // slot np is active at the next level, under the child's entry
+                // in the next split list
+                const int32_t cj = nd.nlx[child];
+                const int d2 = octant_digit(nd.bkey + 9 * (int64_t)child, kx, ky, kz);
+                b.digit_next[np] = (uint8_t)d2;
+                agg_inc(b.hist, 9 * cj + d2);
                 b.perm_next[np] = p;
+                act = true;
+                i = np;
+                nj = cj;
             } else {
                 b.perm_final[np] = p;
                 b.pnode[np] = child;  // single-particle leaf, or a serial root for k_local
@@ -630,20 +637,6 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
         } else {
             b.perm_final[np] = p;
             b.pnode[np] = nid;  // leaf of a serial node, or the node's out-of-bounds tail
-        }
-        // the child whose range holds slot i from the next level on: child
-        // starts are non-decreasing in octant order, so the last one at or
-        // below i (an empty child shares its successor's start)
-        if (first >= 0 && i < nd.start[nid] + nd.count[nid] - nd.ndrop[nid]) {
-            int o = 0;
-            if (nd.start[first + 4] <= i) o = 4;
-            if (nd.start[first + o + 2] <= i) o += 2;
-            if (nd.start[first + o + 1] <= i) o += 1;
-            const int32_t cnode = first + o;
-            if (nd.needs[cnode] == 1) {
-                act = true;
-                nj = nd.nlx[cnode];
-            }
         }
     }
     const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
@@ -1136,9 +1129,42 @@ __global__ void __launch_bounds__(kBlock) k_moments_leaf(int n, const int32_t *_
 
 // Internal nodes of one level, after the level below: the level's list
 // segment given explicitly, or (kDev) the level ctl->mlev of the control block.
+//
+// Levels of at most kFewNodes internal nodes are finished by one thread block,
+// a run of them in one launch with a block barrier between levels: a level
+// that small would otherwise pay a whole dependent launch for one pass of its
+// nodes' load chains (the top levels of the level loop, the deepest levels of
+// the serial subtrees).
+constexpr int kFewNodes = 2 * kBlock;
+
+// levels hi down to lo (deepest first) by the calling block alone
+__device__ __forceinline__ void moments_levels(int hi, int lo, const int32_t *__restrict__ lil, const Ctx::Ctl *ctl,
+                                               Nodes &nd, const Particles &P, const double *gas_prefix,
+                                               const int32_t *gas_off, const uint8_t *gas_uni, RecArgs ra)
+{
+    for (int L = hi; L >= lo; L--) {
+        const int32_t cnt = ctl->lvl_cnt[L];
+        const int32_t *list = lil + ctl->lvl_start[L];
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int64_t nid = list[t];
+            moments_internal(nd, nid, P, [=](int32_t k) { return nd.start[nid] + k; }, gas_prefix, gas_off, gas_uni,
+                             ra);
+        }
+        __syncthreads();  // this level's records before the next level reads them
+    }
+}
+
+// the shallowest level of the run of small levels that starts at level hi
+__device__ __forceinline__ int few_run_end(const Ctx::Ctl *ctl, int hi)
+{
+    int lo = hi;
+    while (lo > 0 && ctl->lvl_cnt[lo - 1] <= kFewNodes) lo--;
+    return lo;
+}
+
 template <bool kDev>
 __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32_t *__restrict__ list,
-                                                        const Ctx::Ctl *ctl, Nodes nd, Particles P,
+                                                        Ctx::Ctl *ctl, Nodes nd, Particles P,
                                                         const double *gas_prefix, const int32_t *gas_off,
                                                         const uint8_t *gas_uni, RecArgs ra)
 {
@@ -1146,6 +1172,14 @@ __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32
         const int L = ctl->mlev;
         if (L < 0) return;
         cnt_lvl = ctl->lvl_cnt[L];
+        if (cnt_lvl <= kFewNodes) {  // a run of small levels: block 0 alone
+            if (blockIdx.x != 0) return;
+            const int lo = few_run_end(ctl, L);
+            moments_levels(L, lo, list, ctl, nd, P, gas_prefix, gas_off, gas_uni, ra);
+            if (threadIdx.x == 0) ctl->mlev_last = lo;
+            return;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mlev_last = L;
         list += ctl->lvl_start[L];
     }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt_lvl; t += gridDim.x * blockDim.x) {
@@ -1153,6 +1187,15 @@ __global__ void __launch_bounds__(kBlock) k_moments_int(int cnt_lvl, const int32
         // the node's start is read only for an out-of-bounds tail
         moments_internal(nd, nid, P, [=](int32_t k) { return nd.start[nid] + k; }, gas_prefix, gas_off, gas_uni, ra);
     }
+}
+
+// levels hi down to lo, each of at most kFewNodes internal nodes, in one block
+__global__ void __launch_bounds__(kBlock) k_moments_few(int hi, int lo, const int32_t *__restrict__ lil,
+                                                        const Ctx::Ctl *ctl, Nodes nd, Particles P,
+                                                        const double *gas_prefix, const int32_t *gas_off,
+                                                        const uint8_t *gas_uni, RecArgs ra)
+{
+    moments_levels(hi, lo, lil, ctl, nd, P, gas_prefix, gas_off, gas_uni, ra);
 }
 
 // internal nodes per level (one shared-memory histogram per block)
@@ -1197,7 +1240,7 @@ __global__ void k_lvl_prefix(Ctx::Ctl *ctl, cudaGraphConditionalHandle h, int us
 __global__ void k_mlev_next(Ctx::Ctl *ctl, cudaGraphConditionalHandle h, int use_h)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int L = ctl->mlev - 1;
+    int L = ctl->mlev_last - 1;
     while (L >= 0 && ctl->lvl_cnt[L] == 0) L--;
     ctl->mlev = L;
     if (use_h) cudaGraphSetConditional(h, L >= 0 ? 1u : 0u);
@@ -1657,6 +1700,20 @@ int grow(Ctx *c, T *&p, size_t old_n, size_t new_n)
 }
 
 }  // namespace
+
+// launches of the internal-moments passes for these per-level counts: one per
+// level of more than kFewNodes nodes, one per run of smaller levels
+int moments_launches(const int32_t *lvl_cnt)
+{
+    int k = 0;
+    for (int L = AG2_MAX_DEPTH - 1; L >= 0; L--) {
+        if (!lvl_cnt[L]) continue;
+        k++;
+        if (lvl_cnt[L] <= kFewNodes)
+            while (L > 0 && lvl_cnt[L - 1] <= kFewNodes) L--;
+    }
+    return k;
+}
 
 int ensure_node_capacity(Ctx *c, size_t need)
 {
@@ -2139,8 +2196,17 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         for (int L = AG2_MAX_DEPTH - 1; L >= 0; L--) {
             const int32_t cnt = c->lvl_cnt_h[L];
             if (!cnt) continue;
+            const RecArgs ra{(float)c->prm.theta, c->inst_R};
+            if (cnt <= kFewNodes) {  // this level and the small ones above it: one block
+                int lo = L;
+                while (lo > 0 && c->lvl_cnt_h[lo - 1] <= kFewNodes) lo--;
+                AG2_LAUNCH(c, k_moments_few, 1, kBlock, 0, L, lo, c->nd.lil, c->ctl, c->nd, c->S(), c->gas_prefix,
+                           c->gas_off, c->gas_uni, ra);
+                L = lo;
+                continue;
+            }
             AG2_LAUNCH(c, k_moments_int<false>, grid_for(cnt, kBlock), kBlock, 0, cnt, c->nd.lil + c->lvl_start_h[L],
-                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
+                       c->ctl, c->nd, c->S(), c->gas_prefix, c->gas_off, c->gas_uni, ra);
         }
     }
     phase_mark(c, "build: internal moments");

@@ -279,7 +279,7 @@ struct Ctx {
         int32_t lvl_off[AG2_MAX_DEPTH];  // bucketing cursors
         int32_t maxlev;         // deepest level of the serial subtrees
         int32_t nlocal_part;    // particles in serial subtrees
-        int32_t pad_;
+        int32_t mlev_last;      // moments: the shallowest level the last launch finished
         unsigned long long local_splits;  // split nodes of the serial subtrees
     };
     Ctl *ctl = nullptr;      // device
@@ -409,6 +409,7 @@ int ensure_instance_tables(Ctx *c);
 int build_groups(Ctx *c);
 int group_size_of(const ag2_params &p);
 int build_tree_captured(Ctx *c);
+int moments_launches(const int32_t *lvl_cnt);  // launches of a captured build's internal-moments loop
 void build_tree_finish_captured(Ctx *c);
 int prepare_captured_build(Ctx *c);
 int ensure_node_capacity(Ctx *c, size_t need);
