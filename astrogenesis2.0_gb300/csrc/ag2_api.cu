@@ -482,6 +482,7 @@ int ag2_destroy(ag2_ctx *c)
                   c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->pkey, c->lroots};
     for (void *q : ps) cudaFree(q);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    if (c->gas_pin) cudaFreeHost(c->gas_pin);
     if (c->ctl_snap) cudaFreeHost(c->ctl_snap);
     for (auto &e : c->snap_ev)
         if (e) cudaEventDestroy(e);

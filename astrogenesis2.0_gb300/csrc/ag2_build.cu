@@ -1636,23 +1636,70 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
 }
 
 // count, min and max mass of each instance's gas particles (order-preserving
-// integer atomics; peers of one instance in a warp combine first)
-__global__ void k_gas_stats(int n, const double *m, const uint8_t *type, const int32_t *pinst, int32_t *cnt,
-                            long long *kmin, long long *kmax)
+// integer atomics)
+constexpr int kGasPer = 16;  // particles per thread of k_gas_stats
+
+__global__ void __launch_bounds__(kBlock) k_gas_stats(int n, const double *m, const uint8_t *type,
+                                                      const int32_t *pinst, int32_t *cnt, long long *kmin,
+                                                      long long *kmax)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool g = i < n && type[i] == 2;
-    const int k = g ? pinst[i] : -1;
-    long long lo = g ? okey(m[i]) : LLONG_MAX, hi = g ? okey(m[i]) : LLONG_MIN;
-    int c = g ? 1 : 0;
-    const unsigned peers = __match_any_sync(0xffffffffu, k);
-    lo = group_reduce(peers, lo, [](long long a, long long b) { return a < b ? a : b; });
-    hi = group_reduce(peers, hi, [](long long a, long long b) { return a > b ? a : b; });
-    c = group_reduce(peers, c, [](int a, int b) { return a + b; });
-    if (g &&(threadIdx.x & 31) == __ffs(peers) - 1) {
-        atomicMin(&kmin[k], lo);
-        atomicMax(&kmax[k], hi);
-        atomicAdd(&cnt[k], c);
+    // a block takes kBlock * kGasPer consecutive slots, which an instance's
+    // contiguous slot range nearly always covers alone: then the block sends
+    // one update per statistic, not one per warp to the same three words
+    __shared__ int32_t s_kmin, s_kmax, s_c;
+    __shared__ long long s_lo, s_hi;
+    if (threadIdx.x == 0) {
+        s_kmin = INT32_MAX;
+        s_kmax = -1;
+        s_c = 0;
+        s_lo = LLONG_MAX;
+        s_hi = LLONG_MIN;
+    }
+    __syncthreads();
+    int k0 = -1, c = 0;
+    long long lo = LLONG_MAX, hi = LLONG_MIN;
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kGasPer;
+    for (int r = 0; r < kGasPer; r++) {
+        const int64_t i = base + (int64_t)r * blockDim.x + threadIdx.x;
+        if (i >= n || type[i] != 2) continue;
+        const int k = pinst[i];
+        if (k != k0) {  // the thread's slots enter another instance: send the last one's now
+            if (k0 >= 0) {
+                atomicMin(&kmin[k0], lo);
+                atomicMax(&kmax[k0], hi);
+                atomicAdd(&cnt[k0], c);
+            }
+            k0 = k;
+            lo = LLONG_MAX;
+            hi = LLONG_MIN;
+            c = 0;
+        }
+        const long long key = okey(m[i]);
+        lo = key < lo ? key : lo;
+        hi = key > hi ? key : hi;
+        c++;
+    }
+    if (k0 >= 0) {
+        atomicMin_block(&s_kmin, k0);
+        atomicMax_block(&s_kmax, k0);
+    }
+    __syncthreads();
+    if (s_kmin == s_kmax) {  // one instance left in the whole block
+        if (k0 >= 0) {
+            atomicMin_block(&s_lo, lo);
+            atomicMax_block(&s_hi, hi);
+            atomicAdd_block(&s_c, c);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicMin(&kmin[s_kmin], s_lo);
+            atomicMax(&kmax[s_kmin], s_hi);
+            atomicAdd(&cnt[s_kmin], s_c);
+        }
+    } else if (k0 >= 0) {
+        atomicMin(&kmin[k0], lo);
+        atomicMax(&kmax[k0], hi);
+        atomicAdd(&cnt[k0], c);
     }
 }
 
@@ -1754,21 +1801,47 @@ static int ensure_hist(Ctx *c, size_t nodes_in_level)
 
 // Gas statistics depend only on masses, types and instances, so they are
 // refreshed when those change (upload, ag2_set_field of the mass,
-// ag2_set_instances), not every build.
-static int prepare_gas_tables(Ctx *c, int n)
+// ag2_set_instances), not every build.  gas_stats_begin computes them on the
+// device and queues their copy into pinned memory without waiting;
+// gas_stats_finish reads them after a later synchronisation of the stream and
+// rebuilds the gasMass tables only when they changed.  So an upload of the
+// same particles costs the build no extra round trip to the host.
+static int gas_stats_begin(Ctx *c, int n)
 {
     if (!c->gas_stats_dirty) return AG2_OK;
     const int K = c->n_inst;
+    if ((size_t)K > c->gas_pin_cap) {
+        if (c->gas_pin) cudaFreeHost(c->gas_pin);
+        c->gas_pin = nullptr;
+        c->gas_pin_cap = 0;
+        AG2_CUDA(c, cudaMallocHost(&c->gas_pin, (size_t)K * 20));
+        c->gas_pin_cap = K;
+    }
     Particles &S = c->S();
     AG2_LAUNCH(c, k_gas_stats_init, grid_for(K, kBlock), kBlock, 0, K, c->gas_cnt, c->gas_kmin, c->gas_kmax);
-    AG2_LAUNCH(c, k_gas_stats, grid_for(n, kBlock), kBlock, 0, n, S.m, S.type, c->pinst, c->gas_cnt, c->gas_kmin,
-               c->gas_kmax);
-    std::vector<int32_t> cnt(K);
+    AG2_LAUNCH(c, k_gas_stats, grid_for(n, kBlock * kGasPer), kBlock, 0, n, S.m, S.type, c->pinst, c->gas_cnt,
+               c->gas_kmin, c->gas_kmax);
+    // pinned layout: kmin (K x 8 B), kmax (K x 8 B), count (K x 4 B)
+    unsigned char *pin = static_cast<unsigned char *>(c->gas_pin);
+    AG2_CUDA(c, cudaMemcpyAsync(pin, c->gas_kmin, K * 8, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(pin + 8 * (size_t)K, c->gas_kmax, K * 8, cudaMemcpyDeviceToHost, c->stream));
+    AG2_CUDA(c, cudaMemcpyAsync(pin + 16 * (size_t)K, c->gas_cnt, K * 4, cudaMemcpyDeviceToHost, c->stream));
+    c->gas_pending = true;
+    return AG2_OK;
+}
+
+// after a synchronisation of the stream that followed gas_stats_begin
+static int gas_stats_finish(Ctx *c)
+{
+    if (!c->gas_pending) return AG2_OK;
+    c->gas_pending = false;
+    const int K = c->n_inst;
+    const unsigned char *pin = static_cast<const unsigned char *>(c->gas_pin);
     std::vector<long long> lo(K), hi(K);
-    AG2_CUDA(c, cudaMemcpyAsync(cnt.data(), c->gas_cnt, K * 4, cudaMemcpyDeviceToHost, c->stream));
-    AG2_CUDA(c, cudaMemcpyAsync(lo.data(), c->gas_kmin, K * 8, cudaMemcpyDeviceToHost, c->stream));
-    AG2_CUDA(c, cudaMemcpyAsync(hi.data(), c->gas_kmax, K * 8, cudaMemcpyDeviceToHost, c->stream));
-    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<int32_t> cnt(K);
+    std::memcpy(lo.data(), pin, K * 8);
+    std::memcpy(hi.data(), pin + 8 * (size_t)K, K * 8);
+    std::memcpy(cnt.data(), pin + 16 * (size_t)K, K * 4);
     std::vector<int32_t> off(K);
     std::vector<uint8_t> uni(K);
     size_t total = 0;
@@ -1802,6 +1875,15 @@ static int prepare_gas_tables(Ctx *c, int n)
     c->gas_tab_hi = hi;
     c->gas_stats_dirty = false;
     return AG2_OK;
+}
+
+// both at once (before a captured build, which reads the tables inside the graph)
+static int prepare_gas_tables(Ctx *c, int n)
+{
+    int rc = gas_stats_begin(c, n);
+    if (rc || !c->gas_pending) return rc;
+    AG2_CUDA(c, cudaStreamSynchronize(c->stream));
+    return gas_stats_finish(c);
 }
 
 // buffers of a level: w = level & 1 selects the current half of each pair
@@ -1975,7 +2057,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     int rc;
     if (!capture) {
         if ((rc = ensure_instance_tables(c)) != AG2_OK) return rc;
-        if ((rc = prepare_gas_tables(c, n)) != AG2_OK) return rc;
+        if ((rc = gas_stats_begin(c, n)) != AG2_OK) return rc;  // read at the first synchronisation below
         // the histogram holds a level's split list (at most n/2 nodes plus the roots);
         // it is sized before the level loop, which fills the next level's while it
         // consumes this one's
@@ -2053,6 +2135,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost,
                                     c->stream));
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        if ((rc = gas_stats_finish(c)) != AG2_OK) return rc;
         c->root_radius = c->inst_R_h[0];
         // The levels run one ahead of the host: level k + 1 is queued before
         // the host waits for level k's counts (a snapshot of the control block

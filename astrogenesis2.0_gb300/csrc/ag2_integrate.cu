@@ -159,7 +159,15 @@ __global__ void k_block_sched(int n, Particles s, double eta, double e0, double 
         k = okey(tn);
     }
     for (int o = 16; o > 0; o >>= 1) k = min(k, __shfl_xor_sync(0xffffffffu, k, o));
-    if ((threadIdx.x & 31) == 0 && k != LLONG_MAX) atomicMin(tkey, k);
+    // one update per block: warps of every block updating the one word serialise there
+    __shared__ long long wmin[32];
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = k;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long b = LLONG_MAX;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) b = min(b, wmin[w]);
+        if (b != LLONG_MAX) atomicMin(tkey, b);
+    }
 }
 
 __device__ __forceinline__ double key_to_double(long long k)
@@ -184,7 +192,14 @@ __global__ void k_block_flags(int n, const Particles s, const long long *tkey, u
     const bool a = i < n && s.tnext[i] == key_to_double(*tkey);
     if (i < n) active[i] = a ? 1 : 0;
     const unsigned b = __ballot_sync(0xffffffffu, a);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, __popc(b));
+    __shared__ int32_t wcnt[32];  // one update per block, as in k_block_sched
+    if ((threadIdx.x & 31) == 0) wcnt[threadIdx.x >> 5] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t t = 0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) t += wcnt[w];
+        if (t) atomicAdd(count, t);
+    }
 }
 
 // second half for the due particles (Simulation.cpp:294-337): Ueuler for gas,

@@ -187,6 +187,9 @@ struct Ctx {
     bool hist_dirty = false;      // a failed build may have left histogram entries set
     double *gas_prefix = nullptr; // sequential sums k*m_gas (uniform gas mass)
     size_t gas_prefix_cap = 0;
+    void *gas_pin = nullptr;     // pinned read-back of the gas statistics (kmin, kmax, count per instance)
+    size_t gas_pin_cap = 0;      // instances it holds
+    bool gas_pending = false;    // statistics queued for read-back, not yet compared
     double *staging = nullptr;    // 6n doubles for upload/download
     uint8_t *staging_u8 = nullptr;
     double *width_part = nullptr; // partial sums of the root width (pairs), laid out by the task table
