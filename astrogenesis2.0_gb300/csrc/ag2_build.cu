@@ -1594,7 +1594,6 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
                     nd.radius[c] = rc;
                     nd.inst[c] = nd.inst[v];
                     nd.mode[c] = cc ? MODE_SER : MODE_EMPTY;
-                    nd.needs[c] = 0;
                     nd.leafpos[c] = -1;
                     join = cc > 0;
                 }

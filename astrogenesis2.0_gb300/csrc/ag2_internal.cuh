@@ -74,12 +74,12 @@ struct Nodes {
     int32_t *start, *count, *ndrop, *first, *parent, *leafpos;
     int8_t *level;
     uint8_t *mode;
-    uint8_t *needs;      // node gets a digit pass at its level
+    uint8_t *needs;      // node gets a digit pass at its level (level loop's nodes only)
     uint8_t *childmask;  // bit o: child o has mass != 0
     double *cx, *cy, *cz;
     double *radius;      // half-width (the root's R halved per level, exactly as Node.cpp:440)
     int32_t *inst;       // simulation instance the node belongs to
-    int64_t *bkey;       // 9 ordered-integer keys per node: lo xyz, hi xyz, centre xyz
+    int64_t *bkey;       // 9 ordered-integer keys per level-loop node: lo xyz, hi xyz, centre xyz
     // moments (reference semantics, FP64), one record per node
     NodeMom *mom;
     // sums over the whole routed range (bottom-up helper), one record per node
