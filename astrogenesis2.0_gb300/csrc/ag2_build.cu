@@ -2130,27 +2130,23 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     } else {
         cudaGraphConditionalHandle none = 0;
         AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 0, (int)AG2_MAX_DEPTH, none, 0);
-        c->inst_R_h.resize(K);
-        AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost,
-                                    c->stream));
-        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-        if ((rc = gas_stats_finish(c)) != AG2_OK) return rc;
-        c->root_radius = c->inst_R_h[0];
         // The levels run one ahead of the host: level k + 1 is queued before
         // the host waits for level k's counts (a snapshot of the control block
-        // copied behind it), so the device does not idle between levels.  The
-        // level queued after the last one finds no split node and changes
+        // copied behind it), so the device does not idle between levels.  A
+        // level queued past the last one finds no split node and changes
         // nothing.  Kernels take their counts from the control block (grid-
-        // stride launches of a fixed grid, as in a captured build).
+        // stride launches of a fixed grid, as in a captured build).  The first
+        // levels are queued on bounds (at most one split per root, at most n
+        // active slots), so the host does not wait for the root half-widths.
         if (!c->ctl_snap) {
             AG2_CUDA(c, cudaMallocHost(&c->ctl_snap, 2 * sizeof(Ctx::Ctl)));
             for (auto &e : c->snap_ev) AG2_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
-        int64_t known_nodes = c->ctl_host->node_count;  // nodes after the last level read back
-        int64_t nnl = c->ctl_host->cur_nnl;             // split nodes of the level after it
-        int64_t nap = c->ctl_host->cur_nap;             // and its active slots
+        int64_t known_nodes = K;  // nodes after the last level read back
+        int64_t nnl = K;          // split nodes of the level after it (a bound until the first read)
+        int64_t nap = n;          // and its active slots (likewise)
         int queued = 0, seen = 0;
-        bool more = nnl > 0;
+        bool more = n > 0;
         while (more) {
             // pool room for the levels in flight: the one read back next
             // allocates 8 * nnl children; of those, the ones the level queued
@@ -2180,7 +2176,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
                 if (c->ctl_host->err_code == AG2_E_NOMEM) local_nomem = true;  // grow the pool and build again
                 return build_error(c, c->ctl_host->err_code);
             }
-            c->level_base.push_back(h.node_count);
+            if (h.level + 2 > (int)c->level_base.size()) c->level_base.push_back(h.node_count);  // a new level
             known_nodes = h.node_count;
             nnl = h.cur_nnl;
             nap = h.cur_nap;
@@ -2188,8 +2184,13 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         }
         // the host mirror after the loop (the serial subtrees' launch reads its
         // counts): the level queued past the last one left the block unchanged
+        c->inst_R_h.resize(K);
+        AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream));
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
         if (c->ctl_host->err_code) return build_error(c, c->ctl_host->err_code);
+        c->root_radius = c->inst_R_h[0];
+        if ((rc = gas_stats_finish(c)) != AG2_OK) return rc;
         AG2_LAUNCH(c, k_mark_loop_nodes, 1, 32, 0, c->ctl);
     }
     phase_mark(c, "build: levels");
