@@ -661,7 +661,11 @@ __global__ void k_level_next(Ctx::Ctl *ctl, int inc, int max_depth, cudaGraphCon
     ctl->cur_nap = ctl->next_active;
     ctl->next_needs = 0;
     ctl->next_active = 0;
-    if (use_h) cudaGraphSetConditional(h, (ctl->cur_nnl > 0 && ctl->err_code == 0 && ctl->level < max_depth) ? 1u : 0u);
+    // a captured loop runs on after an error until no node splits: a node that
+    // could not split (pool exhausted, maximum depth) is a leaf holding its
+    // particles, so every slot settles and the kernels after the build read a
+    // whole tree; the host then reports the error
+    if (use_h) cudaGraphSetConditional(h, (ctl->cur_nnl > 0 && ctl->level < max_depth) ? 1u : 0u);
 }
 
 // Out-of-bounds tails are the only ranges whose order the partition leaves
@@ -1199,15 +1203,15 @@ __global__ void __launch_bounds__(kBlock) k_moments_few(int hi, int lo, const in
 }
 
 // internal nodes per level (one shared-memory histogram per block)
-__global__ void __launch_bounds__(kBlock) k_lvl_hist(Ctx::Ctl *ctl, const int2 *__restrict__ lint)
+__global__ void __launch_bounds__(kBlock) k_lvl_hist(Ctx::Ctl *ctl, const int2 *__restrict__ lint, int64_t cap)
 {
     __shared__ int32_t hs[AG2_MAX_DEPTH];
     for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x) hs[k] = 0;
     __syncthreads();
-    const int n = ctl->nlint;
+    const int n = (int)min((int64_t)ctl->nlint, cap);  // entries a failed reservation counted are not there
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int2 e = lint[t];
-        if (e.x >= 0) atomicAdd(&hs[e.y], 1);
+        if (e.x >= 0 && e.y >= 0 && e.y < AG2_MAX_DEPTH) atomicAdd(&hs[e.y], 1);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x)
@@ -1246,13 +1250,33 @@ __global__ void k_mlev_next(Ctx::Ctl *ctl, cudaGraphConditionalHandle h, int use
     if (use_h) cudaGraphSetConditional(h, L >= 0 ? 1u : 0u);
 }
 
-// internal nodes into one list segment per level (cursors start at the segments)
-__global__ void k_bucket(Ctx::Ctl *ctl, const int2 *__restrict__ lint, int32_t *lil)
+// internal nodes into one list segment per level (cursors start at the
+// segments).  A block ranks its entries per level in shared memory and takes
+// one range per level from the global cursor: the ~20 cursors are the same
+// words for every block, and per-warp atomics on them serialise.  The order
+// within a segment changes no result (each node's moments are its own).
+__global__ void __launch_bounds__(kBlock) k_bucket(Ctx::Ctl *ctl, const int2 *__restrict__ lint, int32_t *lil,
+                                                   int64_t cap)
 {
-    const int n = ctl->nlint;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int2 e = lint[t];
-        if (e.x >= 0) lil[agg_inc(ctl->lvl_off, e.y)] = e.x;
+    __shared__ int32_t cnt[AG2_MAX_DEPTH], base[AG2_MAX_DEPTH];
+    const int n = (int)min((int64_t)ctl->nlint, cap);
+    for (int t0 = blockIdx.x * blockDim.x; t0 < n; t0 += gridDim.x * blockDim.x) {  // block-uniform trip count
+        for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x) cnt[k] = 0;
+        __syncthreads();
+        const int t = t0 + threadIdx.x;
+        int2 e = make_int2(-1, 0);
+        int r = 0;
+        if (t < n) {
+            e = lint[t];
+            if (e.y < 0 || e.y >= AG2_MAX_DEPTH) e.x = -1;
+            if (e.x >= 0) r = atomicAdd_block(&cnt[e.y], 1);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < AG2_MAX_DEPTH; k += blockDim.x)
+            if (cnt[k]) base[k] = atomicAdd(&ctl->lvl_off[k], cnt[k]);
+        __syncthreads();
+        if (e.x >= 0) lil[base[e.y] + r] = e.x;
+        __syncthreads();  // cnt and base are reset for the next stride
     }
 }
 
@@ -1441,21 +1465,35 @@ __global__ void __launch_bounds__(kLocalWarps * 32, kLocalBlocks) k_local(const 
             unsigned long long cbase = 0;
             if (ns) {
                 const unsigned long long need = 8ull * (unsigned long long)ns;
+                bool room = true;
                 if (pool + need > pool_end) {
                     const unsigned long long grab = need > (unsigned long long)kPoolChunk ? need : kPoolChunk;
                     unsigned long long b = 0;
                     if (lane == 0) b = atomicAdd((unsigned long long *)&ctl->node_count, grab);
                     b = __shfl_sync(full, b, 0);
-                    if ((int64_t)(b + grab) > node_cap) {
-                        if (lane == 0) atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
-                        return;
+                    room = (int64_t)(b + grab) <= node_cap;
+                    if (room) {
+                        pool = b;
+                        pool_end = b + grab;
                     }
-                    pool = b;
-                    pool_end = b + grab;
                 }
-                cbase = pool;
-                pool += need;
-                splits += ns;
+                if (room) {
+                    cbase = pool;
+                    pool += need;
+                    splits += ns;
+                } else {
+                    // pool exhausted: this level's split nodes stay leaves
+                    // holding their particles (as at the maximum depth), so
+                    // every slot still settles; the host reports the error
+                    if (lane == 0) atomicExch(&ctl->err_code, (int)AG2_E_NOMEM);
+                    for (int f = lane; f < nf; f += 32)
+                        if (FF[f] == 1) {
+                            FF[f] = -2;
+                            nd.first[fnc[f]] = -1;
+                            nd.leafpos[fnc[f]] = -1;
+                        }
+                    __syncwarp();
+                }
             }
             {
                 int run = 0;
@@ -2253,7 +2291,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
                c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
     phase_mark(c, "build: leaf moments");
     const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
-    AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint);
+    AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint, (int64_t)c->node_cap);
     if (capture) {
         cudaStreamCaptureStatus st;
         cudaGraph_t g = nullptr;
@@ -2261,7 +2299,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         cudaGraphConditionalHandle h;
         AG2_CUDA(c, cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
         AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, h, 1);
-        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil);
+        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil, (int64_t)c->node_cap);
         rc = capture_while(c, h, [&]() -> int {
             AG2_LAUNCH(c, k_moments_int<true>, fixed_grid, kBlock, 0, 0, c->nd.lil, c->ctl, c->nd, c->S(),
                        c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
@@ -2272,7 +2310,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     } else {
         cudaGraphConditionalHandle none = 0;
         AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, none, 0);
-        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil);
+        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil, (int64_t)c->node_cap);
         if ((rc = sync_ctl(c)) != AG2_OK) return rc;
         c->lvl_cnt_h.assign(c->ctl_host->lvl_cnt, c->ctl_host->lvl_cnt + AG2_MAX_DEPTH);
         c->lvl_start_h.assign(c->ctl_host->lvl_start, c->ctl_host->lvl_start + AG2_MAX_DEPTH);
