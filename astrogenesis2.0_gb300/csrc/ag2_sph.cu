@@ -117,69 +117,85 @@ __global__ void k_final(int n, TreeView t, const uint8_t *type, uint8_t *flag, i
     }
 }
 
-// The node's gas particles are gathered 32 at a time into a per-warp queue
-// (ballot over its range), so every FP64 square root and division runs on 32
-// gas lanes rather than on the one or two gas lanes of a mixed stretch (FP64
-// issues at 1/64 of the FP32 rate, whatever the active lanes).  alpha =
+// kRhoWarps warps per selected node, one block, each warp taking every
+// kRhoWarps-th stretch of 32 slots of the node's range: a few thousand nodes
+// with ~1000 slots each give a warp per node too little to wait on its loads
+// with.  The warps' sums are added in warp order, so the result is the same
+// on every run.  Each warp gathers its gas particles 32 at a time into a
+// queue (ballot over its stretch), so every FP64 square root and division runs
+// on 32 gas lanes rather than on the one or two gas lanes of a mixed stretch
+// (FP64 issues at 1/64 of the FP32 rate, whatever the active lanes).  alpha =
 // 1 / (pi h^3) is the same for every particle of the node (kernel.cpp:4-16
 // computes it per call from the same h).
-__global__ void __launch_bounds__(kBlock) k_rho(TreeView t, const double *px, const double *py, const double *pz,
-                                                const double *m, const uint8_t *type, const int32_t *list,
-                                                const Ctx::Ctl *ctl, double *rho_node)
+constexpr int kRhoWarps = 4;
+
+__global__ void __launch_bounds__(32 * kRhoWarps) k_rho(TreeView t, const double *px, const double *py,
+                                                        const double *pz, const double *m, const uint8_t *type,
+                                                        const int32_t *list, const Ctx::Ctl *ctl, double *rho_node)
 {
-    __shared__ int32_t queue[kBlock / 32][64];
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    __shared__ int32_t queue[kRhoWarps][64];
+    __shared__ double part[kRhoWarps];
+    const int wi = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    if (w >= ctl->list_count) return;
-    int32_t *q = queue[threadIdx.x >> 5];
+    const int nlist = ctl->list_count;
+    int32_t *q = queue[wi];
     const unsigned lt = (1u << lane) - 1u;
-    const int64_t nd = list[w];
-    const double h = t.radius[nd] * 2;  // h = radius * 2 (Node.cpp:765)
-    const double alpha = 1.0 / (kPi * h * h * h);
-    const double cx = t.mom[nd].cx, cy = t.mom[nd].cy, cz = t.mom[nd].cz;
-    const int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
-    const uint8_t md = t.mode[nd];
-    // the childParticles multiplicity of slot j: the parent's list plus serial
-    // insertion for a serial entry node (Node.cpp:518, 615), in-bounds only below it
-    auto mult = [&](int32_t j) -> int {
-        if (md == MODE_SER_ENTRY) return j < reached_end ? 2 : 1;
-        if (md == MODE_SER) return j < reached_end ? 1 : 0;
-        return 1;
-    };
-    double acc = 0.0;
-    auto add = [&](int32_t j) {
-        const double dx = px[j] - cx, dy = py[j] - cy, dz = pz[j] - cz;
-        const double r = sqrt(dx * dx + dy * dy + dz * dz);
-        const double qh = r / h;  // kernel::cubicSplineKernel (kernel.cpp:4-16)
-        double W = 0.0;
-        if (qh < 1.0) {
-            W = alpha * (1 - 1.5 * qh * qh + 0.75 * qh * qh * qh);
-        } else if (qh < 2.0) {
-            const double u = 2 - qh;
-            W = alpha * 0.25 * (u * u * u);
-        }
-        acc += mult(j) * (m[j] * W);
-    };
-    int qn = 0;
-    for (int32_t j0 = s; j0 < e; j0 += 32) {
-        const int32_t j = j0 + lane;
-        const bool g = j < e && type[j] == 2 && mult(j) != 0;
-        const unsigned bm = __ballot_sync(0xffffffffu, g);
-        if (g) q[qn + __popc(bm & lt)] = j;
-        qn += __popc(bm);
-        __syncwarp();
-        if (qn >= 32) {
-            const int32_t jj = q[lane];
+    for (int b = blockIdx.x; b < nlist; b += gridDim.x) {  // block-uniform
+        const int64_t nd = list[b];
+        const double h = t.radius[nd] * 2;  // h = radius * 2 (Node.cpp:765)
+        const double alpha = 1.0 / (kPi * h * h * h);
+        const double cx = t.mom[nd].cx, cy = t.mom[nd].cy, cz = t.mom[nd].cz;
+        const int32_t s = t.start[nd], e = s + t.count[nd], reached_end = e - t.ndrop[nd];
+        const uint8_t md = t.mode[nd];
+        // the childParticles multiplicity of slot j: the parent's list plus serial
+        // insertion for a serial entry node (Node.cpp:518, 615), in-bounds only below it
+        auto mult = [&](int32_t j) -> int {
+            if (md == MODE_SER_ENTRY) return j < reached_end ? 2 : 1;
+            if (md == MODE_SER) return j < reached_end ? 1 : 0;
+            return 1;
+        };
+        double acc = 0.0;
+        auto add = [&](int32_t j) {
+            const double dx = px[j] - cx, dy = py[j] - cy, dz = pz[j] - cz;
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            const double qh = r / h;  // kernel::cubicSplineKernel (kernel.cpp:4-16)
+            double W = 0.0;
+            if (qh < 1.0) {
+                W = alpha * (1 - 1.5 * qh * qh + 0.75 * qh * qh * qh);
+            } else if (qh < 2.0) {
+                const double u = 2 - qh;
+                W = alpha * 0.25 * (u * u * u);
+            }
+            acc += mult(j) * (m[j] * W);
+        };
+        int qn = 0;
+        for (int32_t j0 = s + 32 * wi; j0 < e; j0 += 32 * kRhoWarps) {
+            const int32_t j = j0 + lane;
+            const bool g = j < e && type[j] == 2 && mult(j) != 0;
+            const unsigned bm = __ballot_sync(0xffffffffu, g);
+            if (g) q[qn + __popc(bm & lt)] = j;
+            qn += __popc(bm);
             __syncwarp();
-            if (lane < qn - 32) q[lane] = q[32 + lane];
-            qn -= 32;
-            __syncwarp();
-            add(jj);
+            if (qn >= 32) {
+                const int32_t jj = q[lane];
+                __syncwarp();
+                if (lane < qn - 32) q[lane] = q[32 + lane];
+                qn -= 32;
+                __syncwarp();
+                add(jj);
+            }
         }
+        if (lane < qn) add(q[lane]);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) part[wi] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double r = part[0];
+            for (int k = 1; k < kRhoWarps; k++) r += part[k];
+            rho_node[nd] = r;
+        }
+        __syncthreads();  // part and the queues are free for the next node
     }
-    if (lane < qn) add(q[lane]);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) rho_node[nd] = acc;
 }
 
 __global__ void k_assign(int n, TreeView t, const int32_t *finalnode, const uint8_t *type, const double *U,
@@ -260,8 +276,10 @@ int run_sph_density(Ctx *c)
     AG2_LAUNCH(c, k_final, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->nd.flag, c->finalnode, c->nodelist,
                c->ctl);
     const int ngas = c->ngas;
-    AG2_LAUNCH(c, k_rho, grid_for((size_t)ngas * 32, kBlock), kBlock, 0, t, S.px, S.py, S.pz, S.m, S.type,
-               c->nodelist, c->ctl, c->nd.rho);
+    // one block per selected node (at most one per gas particle), striding over the list
+    const unsigned rho_blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)ngas, (size_t)c->sms * 16));
+    AG2_LAUNCH(c, k_rho, rho_blocks, 32 * kRhoWarps, 0, t, S.px, S.py, S.pz, S.m, S.type, c->nodelist, c->ctl,
+               c->nd.rho);
     AG2_LAUNCH(c, k_assign, grid_for(n, kBlock), kBlock, 0, n, t, c->finalnode, S.type, S.U, c->nd.rho, S.h, S.rho,
                S.P, S.T);
     return AG2_OK;
