@@ -442,7 +442,7 @@ int ag2_create(ag2_ctx **out, const ag2_params *params, size_t capacity)
     ok = ok && cudaMalloc(&c->perm, cap * 4) == cudaSuccess && cudaMalloc(&c->perm2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->posnode, cap * 4) == cudaSuccess && cudaMalloc(&c->posnode2, cap * 4) == cudaSuccess &&
          cudaMalloc(&c->pnode, cap * 4) == cudaSuccess && cudaMalloc(&c->refnode, cap * 4) == cudaSuccess && cudaMalloc(&c->slot_of, cap * 4) == cudaSuccess && cudaMalloc(&c->rdist, cap * sizeof(double2)) == cudaSuccess && cudaMalloc(&c->finalnode, cap * 4) == cudaSuccess &&
-         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->drop_list, 65536 * 4) == cudaSuccess && cudaMalloc(&c->digit, 2 * cap) == cudaSuccess &&
+         cudaMalloc(&c->nodelist, cap * 4) == cudaSuccess && cudaMalloc(&c->gas_slots, cap * 4) == cudaSuccess && cudaMalloc(&c->drop_list, 65536 * 4) == cudaSuccess && cudaMalloc(&c->digit, 2 * cap) == cudaSuccess &&
          cudaMalloc(&c->staging, 6 * cap * sizeof(double)) == cudaSuccess &&
          cudaMalloc(&c->staging_u8, cap) == cudaSuccess &&
          cudaMalloc(&c->pinst, cap * 4) == cudaSuccess &&
@@ -476,7 +476,7 @@ int ag2_destroy(ag2_ctx *c)
     free_particles(c->st[1]);
     free_nodes(c->nd);
     void *ps[] = {c->perm, c->perm2, c->posnode, c->posnode2, c->pnode, c->refnode, c->slot_of, c->rdist, c->finalnode,
-                  c->nodelist, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
+                  c->nodelist, c->gas_slots, c->drop_list, c->digit, c->hist, c->cursor, c->gas_prefix, c->staging, c->staging_u8,
                   c->width_part, c->width_thr, c->wsum_task, c->wsum_final, c->wsum_long, c->ctl, c->pinst, c->groups, c->retry_groups, c->inst_first, c->inst_R,
                   c->inst_massInH, c->gas_off, c->gas_uni, c->gas_cnt, c->gas_kmin, c->gas_kmax,
                   c->perm_final, c->ap[0], c->ap[1], c->nl[0], c->nl[1], c->pkey, c->lroots};

@@ -179,6 +179,7 @@ struct Ctx {
     double2 *rdist = nullptr;     // |x| of each particle and its square (tree order) for the root half-width
     int32_t *finalnode = nullptr; // SPH / visual density result node per slot
     int32_t *nodelist = nullptr;  // compacted node list (SPH density nodes)
+    int32_t *gas_slots = nullptr; // SPH density: the gas particles' tree-order slots
     int32_t *drop_list = nullptr; // nodes with out-of-bounds tails (65536 entries)
     uint8_t *digit = nullptr;
     int32_t *hist = nullptr;      // 9 per node of a level
@@ -283,6 +284,8 @@ struct Ctx {
         int32_t maxlev;         // deepest level of the serial subtrees
         int32_t nlocal_part;    // particles in serial subtrees
         int32_t mlev_last;      // moments: the shallowest level the last launch finished
+        int32_t ngas_slots;     // SPH density: gas slots listed by k_climb
+        int32_t pad_;
         unsigned long long local_splits;  // split nodes of the serial subtrees
     };
     Ctl *ctl = nullptr;      // device

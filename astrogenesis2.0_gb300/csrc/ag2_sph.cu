@@ -70,10 +70,32 @@ __device__ __forceinline__ bool cp_member(const TreeView &t, int64_t n, int i)
     return md != MODE_EMPTY;
 }
 
-__global__ void k_climb(int n, TreeView t, const uint8_t *type, const double *inst_massInH, uint8_t *flag)
+// Every slot: a gas slot is listed for k_final and k_assign, which then run
+// over the gas alone (one reservation per block: warps of every block taking
+// places on one counter serialise there), and climbs to its density node.
+__global__ void __launch_bounds__(kBlock) k_climb(int n, TreeView t, const uint8_t *type,
+                                                  const double *inst_massInH, uint8_t *flag, int32_t *gas_slots,
+                                                  Ctx::Ctl *ctl)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || type[i] != 2) return;
+    __shared__ int32_t wcnt[kBlock / 32], bbase;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool gas = i < n && type[i] == 2;
+    const unsigned gm = __ballot_sync(0xffffffffu, gas);
+    if (lane == 0) wcnt[w] = __popc(gm);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t tot = 0;
+        for (int k = 0; k < kBlock / 32; k++) {
+            const int32_t c = wcnt[k];
+            wcnt[k] = tot;
+            tot += c;
+        }
+        bbase = tot ? atomicAdd(&ctl->ngas_slots, tot) : 0;
+    }
+    __syncthreads();
+    if (!gas) return;
+    gas_slots[bbase + wcnt[w] + __popc(gm & ((1u << lane) - 1u))] = i;
     const double M = inst_massInH[t.pinst[i]];
     int pn = t.refnode[i];
     if (pn < 0) return;  // Particle::node is null
@@ -93,15 +115,13 @@ __global__ void k_climb(int n, TreeView t, const uint8_t *type, const double *in
     }
 }
 
-__global__ void k_final(int n, TreeView t, const uint8_t *type, uint8_t *flag, int32_t *finalnode,
-                        int32_t *list, Ctx::Ctl *ctl)
+// the gas slots k_climb listed
+__global__ void k_final(const int32_t *gas_slots, TreeView t, uint8_t *flag, int32_t *finalnode, int32_t *list,
+                        Ctx::Ctl *ctl)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (type[i] != 2) {
-        finalnode[i] = -1;
-        return;
-    }
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ctl->ngas_slots) return;
+    const int i = gas_slots[k];
     int64_t nd = t.pnode[i];
     int32_t fin = -1;
     while (nd >= 0) {
@@ -198,11 +218,13 @@ __global__ void __launch_bounds__(32 * kRhoWarps) k_rho(TreeView t, const double
     }
 }
 
-__global__ void k_assign(int n, TreeView t, const int32_t *finalnode, const uint8_t *type, const double *U,
-                         const double *rho_node, double *h, double *rho, double *P, double *T)
+// the gas slots k_climb listed
+__global__ void k_assign(const int32_t *gas_slots, const Ctx::Ctl *ctl, TreeView t, const int32_t *finalnode,
+                         const double *U, const double *rho_node, double *h, double *rho, double *P, double *T)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || type[i] != 2) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ctl->ngas_slots) return;
+    const int i = gas_slots[k];
     int32_t f = finalnode[i];
     if (f < 0) {
         h[i] = 0.0;  // Tree.cpp:123-133 resets h; rho, P, T keep their old values
@@ -270,18 +292,20 @@ int run_sph_density(Ctx *c)
     TreeView t = view(c);
     AG2_CUDA(c, cudaMemsetAsync(c->nd.flag, 0, std::min(((size_t)c->nnodes + 3) & ~(size_t)3, c->node_cap), c->stream));
     AG2_CUDA(c, cudaMemsetAsync(&c->ctl->list_count, 0, sizeof(int32_t), c->stream));
+    AG2_CUDA(c, cudaMemsetAsync(&c->ctl->ngas_slots, 0, sizeof(int32_t), c->stream));
     if (c->n_inst == 1 && !c->inst_explicit && !c->capturing)  // a single simulation follows ag2_set_params
         AG2_CUDA(c, cudaMemcpyAsync(c->inst_massInH, &c->prm.massInH, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->inst_massInH, c->nd.flag);
-    AG2_LAUNCH(c, k_final, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->nd.flag, c->finalnode, c->nodelist,
+    const int ngas = c->ngas;  // the gas slots k_climb lists
+    AG2_LAUNCH(c, k_climb, grid_for(n, kBlock), kBlock, 0, n, t, S.type, c->inst_massInH, c->nd.flag, c->gas_slots,
                c->ctl);
-    const int ngas = c->ngas;
+    AG2_LAUNCH(c, k_final, grid_for(ngas, kBlock), kBlock, 0, c->gas_slots, t, c->nd.flag, c->finalnode, c->nodelist,
+               c->ctl);
     // one block per selected node (at most one per gas particle), striding over the list
     const unsigned rho_blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)ngas, (size_t)c->sms * 16));
     AG2_LAUNCH(c, k_rho, rho_blocks, 32 * kRhoWarps, 0, t, S.px, S.py, S.pz, S.m, S.type, c->nodelist, c->ctl,
                c->nd.rho);
-    AG2_LAUNCH(c, k_assign, grid_for(n, kBlock), kBlock, 0, n, t, c->finalnode, S.type, S.U, c->nd.rho, S.h, S.rho,
-               S.P, S.T);
+    AG2_LAUNCH(c, k_assign, grid_for(ngas, kBlock), kBlock, 0, c->gas_slots, c->ctl, t, c->finalnode, S.U,
+               c->nd.rho, S.h, S.rho, S.P, S.T);
     return AG2_OK;
 }
 
