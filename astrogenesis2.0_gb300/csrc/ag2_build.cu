@@ -890,6 +890,7 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     ts.first_m = tot.first_m;
     ts.ng = tot.ng;
     ts.first_id = tot.first_id;
+    ts.pad[0] = ts.pad[1] = 0.0;
     nd.tsum[nid] = ts;
     nd.childmask[nid] = cmask;
     NodeMom mm;

@@ -62,11 +62,14 @@ struct alignas(64) WalkRec {
 
 // Sums of a node's whole routed range: mass, mass-weighted position, gas mass
 // and gas momentum, the mass of its lowest upload index, gas count and that
-// index.  80 bytes, written and read whole.
-struct alignas(16) NodeSum {
+// index.  80 bytes of data padded to three whole 32-byte sectors and written
+// whole (pad included): a record written at a scattered node index then
+// leaves no sector partly written for the memory system to merge.
+struct alignas(32) NodeSum {
     double m, mx, my, mz, g, gvx, gvy, gvz;
     double first_m;
     int32_t ng, first_id;
+    double pad[2];
 };
 
 struct Nodes {
