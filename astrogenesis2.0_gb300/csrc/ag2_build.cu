@@ -301,7 +301,7 @@ __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *
 
 __global__ void k_ctl_reset(Ctx::Ctl *ctl, int n_inst)
 {
-    ctl->node_count = n_inst;
+    ctl->node_count = first_pool_node(n_inst);
     ctl->next_needs = 0;
     ctl->err_code = 0;
     ctl->err_info = 0;
@@ -2055,7 +2055,7 @@ void build_tree_finish_captured(Ctx *c)
     const Ctx::Ctl &h = *c->ctl_host;
     c->max_level = std::max((int)h.level, (int)h.maxlev);
     c->nnodes = h.node_count;
-    c->nnodes_true = h.loop_nodes + 8 * (int64_t)h.local_splits;
+    c->nnodes_true = h.loop_nodes - (first_pool_node(c->n_inst) - c->n_inst) + 8 * (int64_t)h.local_splits;
     c->ninternal = (c->nnodes_true - c->n_inst) / 8;
     c->root_radius = c->inst_R_pin ? c->inst_R_pin[0] : 0.0;
     c->inst_R_h.assign(c->inst_R_pin, c->inst_R_pin + c->n_inst);
@@ -2181,7 +2181,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             AG2_CUDA(c, cudaMallocHost(&c->ctl_snap, 2 * sizeof(Ctx::Ctl)));
             for (auto &e : c->snap_ev) AG2_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
-        int64_t known_nodes = K;  // nodes after the last level read back
+        int64_t known_nodes = first_pool_node(K);  // nodes after the last level read back
         int64_t nnl = K;          // split nodes of the level after it (a bound until the first read)
         int64_t nap = n;          // and its active slots (likewise)
         int queued = 0, seen = 0;
@@ -2267,7 +2267,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         }
         c->max_level = std::max((int)c->level_base.size() - 2, (int)c->ctl_host->maxlev);
         c->nnodes = c->ctl_host->node_count;
-        c->nnodes_true = loop_nodes + 8 * (int64_t)c->ctl_host->local_splits;
+        c->nnodes_true = loop_nodes - (first_pool_node(K) - K) + 8 * (int64_t)c->ctl_host->local_splits;
         c->ninternal = (c->nnodes_true - K) / 8;
         if (c->ctl_host->ndrop_nodes > kMaxDropNodes) return build_error(c, AG2_E_CAPACITY);
         if (c->ctl_host->ndrop_nodes > 0)

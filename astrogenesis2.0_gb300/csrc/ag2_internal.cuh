@@ -72,6 +72,12 @@ struct alignas(32) NodeSum {
     double pad[2];
 };
 
+// The first node index after the roots (instance k's root is node k): the pool
+// starts on a multiple of 8, so that every node's 8-child block is 8-aligned
+// and the children's 4- and 8-byte fields fill whole 32-byte sectors.  The
+// indices in between are never reached (every traversal starts at a root).
+__host__ __device__ inline int64_t first_pool_node(int64_t n_inst) { return (n_inst + 7) & ~(int64_t)7; }
+
 struct Nodes {
     // topology (written by the level-wise build)
     int32_t *start, *count, *ndrop, *first, *parent, *leafpos;

@@ -1131,13 +1131,18 @@ __global__ void __launch_bounds__(256) k_energy_sums(int n, const double *m, con
         for (int q = 0; q < 3; q++) part[3 * blockIdx.x + q] = sh[q][0];
 }
 
+// Every index of the pool up to its high-water mark, the holes that no
+// traversal reaches included (their fields were never written): the instance
+// index is checked before it indexes the table.
 __global__ void k_update_mac(int64_t nnodes, const int32_t *first, const double *radius, const int32_t *inst,
-                             const double *inst_R, WalkRec *wrec, double theta)
+                             int n_inst, const double *inst_R, WalkRec *wrec, double theta)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     if (first[j] < 0) return;
-    const float q = (float)scale2(radius[j], walk_scale_exp(inst_R[inst[j]])) / (float)theta;
+    const int k = inst[j];
+    if (k < 0 || k >= n_inst) return;
+    const float q = (float)scale2(radius[j], walk_scale_exp(inst_R[k])) / (float)theta;
     wrec[j].B.w = q * q;
 }
 
@@ -1205,7 +1210,7 @@ int run_forces(Ctx *c)
     if (c->n == 0) return AG2_OK;
     if (c->prm.theta != c->tree_theta) {
         AG2_LAUNCH(c, k_update_mac, grid_for((size_t)c->nnodes, 256), 256, 0, c->nnodes, c->nd.first, c->nd.radius,
-                   c->nd.inst, c->inst_R, c->nd.wrec, c->prm.theta);
+                   c->nd.inst, c->n_inst, c->inst_R, c->nd.wrec, c->prm.theta);
         c->tree_theta = c->prm.theta;
     }
     WalkArgs a = walk_args(c);
