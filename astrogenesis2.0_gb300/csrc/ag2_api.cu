@@ -205,7 +205,7 @@ void free_particles(Particles &p)
 
 void free_nodes(Nodes &d)
 {
-    void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs, d.childmask,
+    void *ps[] = {d.start, d.count, d.ndrop, d.first, d.parent, d.leafpos, d.level, d.mode, d.needs,
                   d.cx,    d.cy,    d.cz,    d.bkey,  d.mom,   d.tsum,
                   d.wrec, d.flag, d.rho,
                   d.radius, d.inst, d.nlx, d.lint, d.lil};

@@ -892,7 +892,6 @@ __device__ __forceinline__ void store_node(Nodes &nd, int64_t nid, const Particl
     ts.first_id = tot.first_id;
     ts.pad[0] = ts.pad[1] = 0.0;
     nd.tsum[nid] = ts;
-    nd.childmask[nid] = cmask;
     NodeMom mm;
     mm.mass = mass;
     mm.cx = cx;
@@ -1810,7 +1809,7 @@ int ensure_node_capacity(Ctx *c, size_t need)
     int rc = AG2_OK;
 #define G(x) \
     if ((rc = grow(c, d.x, old, nc)) != AG2_OK) return rc;
-    G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs) G(childmask)
+    G(start) G(count) G(ndrop) G(first) G(parent) G(leafpos) G(level) G(mode) G(needs)
     G(cx) G(cy) G(cz) G(radius) G(inst) G(mom)
     G(tsum) G(wrec) G(flag)
     G(rho) G(nlx) G(lint) G(lil)

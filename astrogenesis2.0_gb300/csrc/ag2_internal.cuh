@@ -84,7 +84,6 @@ struct Nodes {
     int8_t *level;
     uint8_t *mode;
     uint8_t *needs;      // node gets a digit pass at its level (level loop's nodes only)
-    uint8_t *childmask;  // bit o: child o has mass != 0
     double *cx, *cy, *cz;
     double *radius;      // half-width (the root's R halved per level, exactly as Node.cpp:440)
     int32_t *inst;       // simulation instance the node belongs to

@@ -68,7 +68,6 @@ struct WalkArgs {
     double *ax, *ay, *az, *dUdt;
     const WalkRec *wrec;
     const int32_t *first, *leafpos;
-    const uint8_t *childmask;
     const int8_t *level;
     const NodeMom *mom;
     const double *radius;
@@ -320,7 +319,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_walk64(WalkArgs a)
             }
             const unsigned om = __ballot_sync(0xffffffffu, open);
             if (om) {
-                const unsigned cm = a.childmask[c];
+                const unsigned cm = (unsigned)a.wrec[c].C.z;  // bit o: child o has mass
                 const int nch = __popc(cm);
                 if (sp + nch > kStack) {
                     overflow = true;
@@ -1083,7 +1082,7 @@ __global__ void __launch_bounds__(kWalkBlock) k_potential(WalkArgs a, double *ph
             }
             const unsigned om = __ballot_sync(0xffffffffu, open);
             if (om) {
-                const unsigned cm = a.childmask[c];
+                const unsigned cm = (unsigned)a.wrec[c].C.z;  // bit o: child o has mass
                 if (sp + __popc(cm) > kStack) {
                     overflow = true;
                     break;
@@ -1160,7 +1159,7 @@ static WalkArgs walk_args(Ctx *c)
     a.pnode = c->pnode;
     a.ax = S.ax; a.ay = S.ay; a.az = S.az; a.dUdt = S.dUdt;
     a.wrec = c->nd.wrec;
-    a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.childmask = c->nd.childmask; a.level = c->nd.level;
+    a.first = c->nd.first; a.leafpos = c->nd.leafpos; a.level = c->nd.level;
     a.mom = c->nd.mom;
     a.radius = c->nd.radius;
     a.groups = c->groups;
