@@ -487,6 +487,7 @@ int ag2_destroy(ag2_ctx *c)
     for (auto &e : c->snap_ev)
         if (e) cudaEventDestroy(e);
     if (c->inst_R_pin) cudaFreeHost(c->inst_R_pin);
+    if (c->inst_R_rb) cudaFreeHost(c->inst_R_rb);
     for (auto &x : c->step_exec)
         if (x) cudaGraphExecDestroy(x);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);

@@ -2180,6 +2180,15 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             AG2_CUDA(c, cudaMallocHost(&c->ctl_snap, 2 * sizeof(Ctx::Ctl)));
             for (auto &e : c->snap_ev) AG2_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
+        // the root half-widths come back with the first snapshot
+        if (c->inst_R_rb_cap < (size_t)K) {
+            if (c->inst_R_rb) cudaFreeHost(c->inst_R_rb);
+            c->inst_R_rb = nullptr;
+            c->inst_R_rb_cap = 0;
+            AG2_CUDA(c, cudaMallocHost(&c->inst_R_rb, K * sizeof(double)));
+            c->inst_R_rb_cap = K;
+        }
+        AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_rb, c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         int64_t known_nodes = first_pool_node(K);  // nodes after the last level read back
         int64_t nnl = K;          // split nodes of the level after it (a bound until the first read)
         int64_t nap = n;          // and its active slots (likewise)
@@ -2221,12 +2230,17 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             more = nnl > 0;
         }
         // the host mirror after the loop (the serial subtrees' launch reads its
-        // counts): the level queued past the last one left the block unchanged
-        c->inst_R_h.resize(K);
-        AG2_CUDA(c, cudaMemcpyAsync(c->inst_R_h.data(), c->inst_R, K * sizeof(double), cudaMemcpyDeviceToHost,
-                                    c->stream));
-        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        // counts) is the last snapshot read: the level queued past the last
+        // one leaves the block unchanged.  Waiting on a snapshot also waited
+        // for the root half-widths' and the gas statistics' read-backs queued
+        // before the loop.
+        if (seen > 0) {
+            std::memcpy(c->ctl_host, c->ctl_snap + ((seen - 1) & 1), sizeof(Ctx::Ctl));
+        } else if ((rc = sync_ctl(c)) != AG2_OK) {
+            return rc;
+        }
         if (c->ctl_host->err_code) return build_error(c, c->ctl_host->err_code);
+        c->inst_R_h.assign(c->inst_R_rb, c->inst_R_rb + K);
         c->root_radius = c->inst_R_h[0];
         if ((rc = gas_stats_finish(c)) != AG2_OK) return rc;
         AG2_LAUNCH(c, k_mark_loop_nodes, 1, 32, 0, c->ctl);
@@ -2256,14 +2270,23 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             AG2_LAUNCH(c, k_local, blocks, lc.wpb * 32, lc.smem, c->lroots, lc.lcap, c->nd, c->ctl, c->pkey,
                        (int64_t)c->cap, c->perm_final, c->pnode, S.id,
                        (int)AG2_MAX_DEPTH, (int64_t)c->node_cap);
-            if ((rc = sync_ctl(c)) != AG2_OK) return rc;
-            const Ctx::Ctl &h = *c->ctl_host;
-            if (h.err_code) {
-                if (h.err_code == AG2_E_NOMEM) local_nomem = true;
-                return build_error(c, h.err_code);
-            }
-            phase_mark(c, "build: serial subtrees");
         }
+        // the internal-node list by level (these read the list within its
+        // capacity, so they are safe after a failed k_local), then one
+        // synchronisation for the serial subtrees' counts and errors and the
+        // levels' sizes
+        {
+            cudaGraphConditionalHandle none = 0;
+            AG2_LAUNCH(c, k_lvl_hist, fixed_grid, kBlock, 0, c->ctl, c->nd.lint, (int64_t)c->node_cap);
+            AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, none, 0);
+            AG2_LAUNCH(c, k_bucket, fixed_grid, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil, (int64_t)c->node_cap);
+        }
+        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        if (c->ctl_host->err_code) {
+            if (c->ctl_host->err_code == AG2_E_NOMEM) local_nomem = true;
+            return build_error(c, c->ctl_host->err_code);
+        }
+        if (nloc > 0) phase_mark(c, "build: serial subtrees");
         c->max_level = std::max((int)c->level_base.size() - 2, (int)c->ctl_host->maxlev);
         c->nnodes = c->ctl_host->node_count;
         c->nnodes_true = loop_nodes - (first_pool_node(K) - K) + 8 * (int64_t)c->ctl_host->local_splits;
@@ -2290,16 +2313,15 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     AG2_LAUNCH(c, k_moments_leaf, gl, kBlock, 0, n, c->pnode, c->nd, c->S(), c->gas_prefix, c->gas_off,
                c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
     phase_mark(c, "build: leaf moments");
-    const unsigned gi = capture ? fixed_grid : std::max(1u, grid_for(c->ctl_host->nlint, kBlock));
-    AG2_LAUNCH(c, k_lvl_hist, gi, kBlock, 0, c->ctl, c->nd.lint, (int64_t)c->node_cap);
     if (capture) {
+        AG2_LAUNCH(c, k_lvl_hist, fixed_grid, kBlock, 0, c->ctl, c->nd.lint, (int64_t)c->node_cap);
         cudaStreamCaptureStatus st;
         cudaGraph_t g = nullptr;
         AG2_CUDA(c, cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g));
         cudaGraphConditionalHandle h;
         AG2_CUDA(c, cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
         AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, h, 1);
-        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil, (int64_t)c->node_cap);
+        AG2_LAUNCH(c, k_bucket, fixed_grid, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil, (int64_t)c->node_cap);
         rc = capture_while(c, h, [&]() -> int {
             AG2_LAUNCH(c, k_moments_int<true>, fixed_grid, kBlock, 0, 0, c->nd.lil, c->ctl, c->nd, c->S(),
                        c->gas_prefix, c->gas_off, c->gas_uni, RecArgs{(float)c->prm.theta, c->inst_R});
@@ -2308,10 +2330,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         });
         if (rc) return rc;
     } else {
-        cudaGraphConditionalHandle none = 0;
-        AG2_LAUNCH(c, k_lvl_prefix, 1, 32, 0, c->ctl, none, 0);
-        AG2_LAUNCH(c, k_bucket, gi, kBlock, 0, c->ctl, c->nd.lint, c->nd.lil, (int64_t)c->node_cap);
-        if ((rc = sync_ctl(c)) != AG2_OK) return rc;
+        // the levels' sizes came back with the serial subtrees' synchronisation
         c->lvl_cnt_h.assign(c->ctl_host->lvl_cnt, c->ctl_host->lvl_cnt + AG2_MAX_DEPTH);
         c->lvl_start_h.assign(c->ctl_host->lvl_start, c->ctl_host->lvl_start + AG2_MAX_DEPTH);
         for (int L = AG2_MAX_DEPTH - 1; L >= 0; L--) {

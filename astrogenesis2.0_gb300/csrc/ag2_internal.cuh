@@ -116,6 +116,8 @@ struct Ctx {
     unsigned long long step_key = 0;     // parameters the graphs were captured for
     int64_t graph_launches[2] = {};      // kernels captured outside the loops
     double *inst_R_pin = nullptr;        // pinned copy of the root half-widths (step graphs)
+    double *inst_R_rb = nullptr;         // pinned read-back of the root half-widths (launched builds)
+    size_t inst_R_rb_cap = 0;
     // block time steps (ag2_block_init / ag2_block_step)
     bool blk_ready = false;
     double blk_eta = 0, blk_dmin = 0, blk_dmax = 0, blk_t = 0;
