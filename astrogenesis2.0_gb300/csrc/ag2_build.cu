@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes(LevelPair lpair, int thresh, i
 // list's order (like the order of the particles within a child, which the
 // cursor atomics set) changes no result: a node's final range is its children
 // in octant order followed by its out-of-bounds tail in upload order.
-__global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, Ctx::Ctl *ctl)
+__global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, Ctx::Ctl *ctl, int advance)
 {
     __shared__ int32_t sh[kBlock / 32 + 1];
     __shared__ int32_t sbase;
@@ -644,6 +644,29 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
         b.ap_next[q] = i;
         b.posnode_next[i] = nj;
     }
+    }
+    if (!advance) return;
+    // launched level loop: the last block to finish also advances the level
+    // (k_level_next's bookkeeping, without a launch of its own); a captured
+    // loop keeps k_level_next, which sets the loop's condition
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();  // this block's counts before its arrival
+        last = atomicAdd(&ctl->scatter_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();  // every block's counts before they are read
+        volatile Ctx::Ctl *v = ctl;
+        if (v->cur_nnl != 0) {  // a level queued past the last one leaves the block as it was
+            v->level += 1;
+            v->cur_nnl = v->next_needs;
+            v->cur_nap = v->next_active;
+            v->next_needs = 0;
+            v->next_active = 0;
+        }
+        v->scatter_done = 0u;
     }
 }
 
@@ -2159,7 +2182,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         rc = capture_while(c, h, [&]() -> int {
             AG2_LAUNCH(c, k_nodes, fixed_grid, kBlock, 0, lpair, thresh, (int64_t)c->node_cap, c->nd, c->ctl,
                        (int)AG2_MAX_DEPTH);
-            AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
+            AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl, 0);
             AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 1, (int)AG2_MAX_DEPTH, h, 1);
             return AG2_OK;
         });
@@ -2207,8 +2230,7 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
             lpair.b[0].local_ok = lpair.b[1].local_ok = local_ok;
             AG2_LAUNCH(c, k_nodes, fixed_grid, kBlock, 0, lpair, thresh, (int64_t)c->node_cap, c->nd, c->ctl,
                        (int)AG2_MAX_DEPTH);
-            AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl);
-            AG2_LAUNCH(c, k_level_next, 1, 32, 0, c->ctl, 1, (int)AG2_MAX_DEPTH, none, 0);
+            AG2_LAUNCH(c, k_scatter, fixed_grid, kBlock, 0, lpair, c->nd, c->ctl, 1);  // and advances the level
             const int slot = queued & 1;
             AG2_CUDA(c, cudaMemcpyAsync(c->ctl_snap + slot, c->ctl, sizeof(Ctx::Ctl), cudaMemcpyDeviceToHost,
                                         c->stream));

@@ -295,7 +295,7 @@ struct Ctx {
         int32_t nlocal_part;    // particles in serial subtrees
         int32_t mlev_last;      // moments: the shallowest level the last launch finished
         int32_t ngas_slots;     // SPH density: gas slots listed by k_climb
-        int32_t pad_;
+        uint32_t scatter_done;  // blocks of the running k_scatter that have finished (launched level loop)
         unsigned long long local_splits;  // split nodes of the serial subtrees
     };
     Ctl *ctl = nullptr;      // device
