@@ -780,8 +780,9 @@ static int capture_step(Ctx *c, double dt, double hubble, int with_visual, doubl
     c->capturing = false;
     c->have_tree = had_tree;
     // launches per replay: those outside the two loops; the loop bodies
-    // (4 level kernels, 2 moments kernels) are added per iteration
-    *nlaunch = c->launches - l0 - 6;
+    // (3 level kernels, 2 moments kernels, captured once here) are added per
+    // iteration
+    *nlaunch = c->launches - l0 - 5;
     c->launches = l0;
     if (!rc && e != cudaSuccess) rc = cuda_check(c, e, "cudaStreamEndCapture");
     if (!rc) {
@@ -843,7 +844,8 @@ static int run_step_graph(Ctx *c, double dt, double hubble, int with_visual, dou
     c->cur ^= 1;
     const Ctx::Ctl &h = *c->ctl_host;
     const int mlevels = moments_launches(h.lvl_cnt);
-    c->launches += c->graph_launches[from] + 4 * (int64_t)(h.level + 1) + 2 * (int64_t)mlevels;
+    // the level loop ran once per level it advanced, the moments loop once per launch of its levels
+    c->launches += c->graph_launches[from] + 3 * (int64_t)h.level + 2 * (int64_t)mlevels;
     c->inter_grav = (int64_t)h.inter_grav;
     c->inter_sph = (int64_t)h.inter_sph;
     if (h.err_code) {

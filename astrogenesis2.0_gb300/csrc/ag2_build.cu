@@ -173,6 +173,33 @@ __global__ void k_wsum_sums(int ntask, const int4 *__restrict__ task, double *bu
     buf[2 * (int64_t)q.z + 1] = s2;
 }
 
+// The levels above the particle level in one block, with a block barrier
+// between them: a level has few tasks (a few per 4096 particles), so a launch
+// per level mostly paid for launching.  The tasks and their sums are
+// k_wsum_sums'.
+constexpr int kWsumMaxLevels = 16;
+constexpr int kWsumUpperMax = 4096;  // tasks above the particle level that one block takes
+struct WsumLevels {
+    int n;                               // levels, the particle level included
+    int32_t start[kWsumMaxLevels + 1];   // each level's first task
+};
+__global__ void __launch_bounds__(1024) k_wsum_upper(WsumLevels lv, const int4 *__restrict__ task, double *buf)
+{
+    for (int l = 1; l < lv.n; l++) {
+        for (int t = lv.start[l] + threadIdx.x; t < lv.start[l + 1]; t += blockDim.x) {
+            const int4 q = task[t];
+            double s = 0.0, s2 = 0.0;
+            for (int j = 0; j < q.y; j++) {
+                s = __dadd_rn(s, buf[2 * ((int64_t)q.x + j)]);
+                s2 = __dadd_rn(s2, buf[2 * ((int64_t)q.x + j) + 1]);
+            }
+            buf[2 * (int64_t)q.z] = s;
+            buf[2 * (int64_t)q.z + 1] = s2;
+        }
+        __syncthreads();  // this level's sums before the next level adds them
+    }
+}
+
 // one thread per instance: threshold mean + 10 sigma from the instance's sums
 __global__ void k_width_thr(int n_inst, const int64_t *first, const int32_t *final_pos, const double *buf,
                             double *thr, double *R)
@@ -269,6 +296,9 @@ __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_inst) return;
+    // the pool starts after the roots (the rest of the control block is zero
+    // from the memset at the start of the build)
+    if (k == 0) ctl->node_count = first_pool_node(n_inst);
     const int32_t start = (int32_t)first[k];
     const int32_t n = (int32_t)(first[k + 1] - first[k]);
     nd.start[k] = start;
@@ -297,17 +327,6 @@ __global__ void k_root_init(int n_inst, Nodes nd, Ctx::Ctl *ctl, const int64_t *
     } else if (needs == 2) {
         lroots[atomicAdd(&ctl->nlocal, 1)] = k;
     }
-}
-
-__global__ void k_ctl_reset(Ctx::Ctl *ctl, int n_inst)
-{
-    ctl->node_count = first_pool_node(n_inst);
-    ctl->next_needs = 0;
-    ctl->err_code = 0;
-    ctl->err_info = 0;
-    ctl->any_drop = 0;
-    ctl->ndrop_nodes = 0;
-    ctl->next_active = 0;
 }
 
 // Block-wide reservation in a compact list: every thread of the block calls
@@ -2136,9 +2155,19 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     if (n > 0) {
         AG2_LAUNCH(c, k_slot_of, grid_for(n, kBlock), kBlock, 0, n, S.id, c->slot_of);
         AG2_LAUNCH(c, k_dist, grid_for(n, kBlock), kBlock, 0, n, S.px, S.py, S.pz, c->rdist);
-        for (size_t l = 0; l + 1 < c->wsum_level.size(); l++) {
+        const size_t nlev = c->wsum_level.size() - 1;  // levels, the particle level included
+        const bool one_block = nlev >= 2 && nlev <= (size_t)kWsumMaxLevels &&
+                               c->wsum_level[nlev] - c->wsum_level[1] <= kWsumUpperMax;
+        for (size_t l = 0; l < nlev; l++) {
             const int nt = c->wsum_level[l + 1] - c->wsum_level[l];
             const int4 *tk = c->wsum_task + c->wsum_level[l];
+            if (l > 0 && one_block) {  // the levels above the particle level, all at once
+                WsumLevels lv;
+                lv.n = (int)nlev;
+                for (size_t k = 0; k <= nlev; k++) lv.start[k] = c->wsum_level[k];
+                AG2_LAUNCH(c, k_wsum_upper, 1, 1024, 0, lv, c->wsum_task, c->width_part);
+                break;
+            }
             if (l == 0) {
                 AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->rdist, c->slot_of,
                            c->width_part);
@@ -2158,7 +2187,6 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     phase_mark(c, "build: root width");
     if (!capture && (rc = ensure_node_capacity(c, (size_t)K + 1024)) != AG2_OK) return rc;
     const int thresh = c->prm.split_threshold;
-    AG2_LAUNCH(c, k_ctl_reset, 1, 1, 0, c->ctl, K);
     // serial subtrees (fewer than split_threshold particles) are built one warp each when they fit
     const bool local_ok = thresh - 1 <= kLocalCapMax;
     AG2_LAUNCH(c, k_root_init, grid_for(K, kBlock), kBlock, 0, K, c->nd, c->ctl, c->inst_first, c->inst_R, thresh,
@@ -2265,7 +2293,6 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
         c->inst_R_h.assign(c->inst_R_rb, c->inst_R_rb + K);
         c->root_radius = c->inst_R_h[0];
         if ((rc = gas_stats_finish(c)) != AG2_OK) return rc;
-        AG2_LAUNCH(c, k_mark_loop_nodes, 1, 32, 0, c->ctl);
     }
     phase_mark(c, "build: levels");
 
