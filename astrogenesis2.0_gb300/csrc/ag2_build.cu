@@ -173,33 +173,6 @@ __global__ void k_wsum_sums(int ntask, const int4 *__restrict__ task, double *bu
     buf[2 * (int64_t)q.z + 1] = s2;
 }
 
-// The levels above the particle level in one block, with a block barrier
-// between them: a level has few tasks (a few per 4096 particles), so a launch
-// per level mostly paid for launching.  The tasks and their sums are
-// k_wsum_sums'.
-constexpr int kWsumMaxLevels = 16;
-constexpr int kWsumUpperMax = 4096;  // tasks above the particle level that one block takes
-struct WsumLevels {
-    int n;                               // levels, the particle level included
-    int32_t start[kWsumMaxLevels + 1];   // each level's first task
-};
-__global__ void __launch_bounds__(1024) k_wsum_upper(WsumLevels lv, const int4 *__restrict__ task, double *buf)
-{
-    for (int l = 1; l < lv.n; l++) {
-        for (int t = lv.start[l] + threadIdx.x; t < lv.start[l + 1]; t += blockDim.x) {
-            const int4 q = task[t];
-            double s = 0.0, s2 = 0.0;
-            for (int j = 0; j < q.y; j++) {
-                s = __dadd_rn(s, buf[2 * ((int64_t)q.x + j)]);
-                s2 = __dadd_rn(s2, buf[2 * ((int64_t)q.x + j) + 1]);
-            }
-            buf[2 * (int64_t)q.z] = s;
-            buf[2 * (int64_t)q.z + 1] = s2;
-        }
-        __syncthreads();  // this level's sums before the next level adds them
-    }
-}
-
 // one thread per instance: threshold mean + 10 sigma from the instance's sums
 __global__ void k_width_thr(int n_inst, const int64_t *first, const int32_t *final_pos, const double *buf,
                             double *thr, double *R)
@@ -2155,19 +2128,9 @@ static int build_tree_once(Ctx *c, bool &local_nomem, bool capture)
     if (n > 0) {
         AG2_LAUNCH(c, k_slot_of, grid_for(n, kBlock), kBlock, 0, n, S.id, c->slot_of);
         AG2_LAUNCH(c, k_dist, grid_for(n, kBlock), kBlock, 0, n, S.px, S.py, S.pz, c->rdist);
-        const size_t nlev = c->wsum_level.size() - 1;  // levels, the particle level included
-        const bool one_block = nlev >= 2 && nlev <= (size_t)kWsumMaxLevels &&
-                               c->wsum_level[nlev] - c->wsum_level[1] <= kWsumUpperMax;
-        for (size_t l = 0; l < nlev; l++) {
+        for (size_t l = 0; l + 1 < c->wsum_level.size(); l++) {
             const int nt = c->wsum_level[l + 1] - c->wsum_level[l];
             const int4 *tk = c->wsum_task + c->wsum_level[l];
-            if (l > 0 && one_block) {  // the levels above the particle level, all at once
-                WsumLevels lv;
-                lv.n = (int)nlev;
-                for (size_t k = 0; k <= nlev; k++) lv.start[k] = c->wsum_level[k];
-                AG2_LAUNCH(c, k_wsum_upper, 1, 1024, 0, lv, c->wsum_task, c->width_part);
-                break;
-            }
             if (l == 0) {
                 AG2_LAUNCH(c, k_wsum_particles, grid_for(nt, kBlock), kBlock, 0, nt, tk, c->rdist, c->slot_of,
                            c->width_part);
