@@ -327,6 +327,33 @@ __device__ __forceinline__ T block_reserve(bool flag, T *counter, T stride, int3
     return r;
 }
 
+// block_reserve for a loop that calls it once per round: the two rounds in
+// flight use the two halves of sh (kBlock / 32 entries each) and of sbase
+// alternately, so a round needs no barrier after reading its offsets.  A
+// thread writes a half again two rounds later, after the next round's first
+// barrier, which every thread reaches only after reading its offsets here.
+__device__ __forceinline__ int32_t block_reserve_rounds(bool flag, int32_t *counter, int32_t *sh, int32_t *sbase,
+                                                        int round)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int32_t *const shr = sh + (round & 1) * nw;
+    int32_t *const sb = sbase + (round & 1);
+    const unsigned b = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0) shr[w] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = 0; k < nw; k++) {
+            const int v = shr[k];
+            shr[k] = acc;
+            acc += v;
+        }
+        *sb = acc ? atomicAdd(counter, acc) : 0;
+    }
+    __syncthreads();
+    return flag ? *sb + shr[w] + __popc(b & ((1u << lane) - 1u)) : 0;
+}
+
 // Buffers of one level of the partition.  A slot is a position in the
 // partition; it is active while the node whose range holds it is still split.
 struct LevelBufs {
@@ -582,11 +609,12 @@ __global__ void __launch_bounds__(kBlock) k_nodes(LevelPair lpair, int thresh, i
 // in octant order followed by its out-of-bounds tail in upload order.
 __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, Ctx::Ctl *ctl, int advance)
 {
-    __shared__ int32_t sh[kBlock / 32 + 1];
-    __shared__ int32_t sbase;
+    __shared__ int32_t sh[2 * (kBlock / 32)];
+    __shared__ int32_t sbase[2];
     const int nap = ctl->cur_nap;
     const LevelBufs &b = lpair.b[ctl->level & 1];
-    for (int t0 = blockIdx.x * blockDim.x; t0 < nap; t0 += gridDim.x * blockDim.x) {  // block-uniform trip count
+    int round = 0;
+    for (int t0 = blockIdx.x * blockDim.x; t0 < nap; t0 += gridDim.x * blockDim.x, round++) {  // block-uniform trip count
     const int t = t0 + threadIdx.x;
     bool act = false;
     int i = 0, nj = 0;
@@ -631,7 +659,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(LevelPair lpair, Nodes nd, C
             b.pnode[np] = nid;  // leaf of a serial node, or the node's out-of-bounds tail
         }
     }
-    const int32_t q = block_reserve<int32_t>(act, &ctl->next_active, 1, sh, &sbase);
+    const int32_t q = block_reserve_rounds(act, &ctl->next_active, sh, sbase, round);
     if (act) {
         b.ap_next[q] = i;
         b.posnode_next[i] = nj;
